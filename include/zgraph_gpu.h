@@ -1,0 +1,217 @@
+/*
+ * zgraph_gpu.h — C ABI of libzgraph_gpu.so, the GB300 (sm_103a) implementation of
+ * ZGraph's ASAP neighbour-sampling estimator hot path.
+ *
+ * Every entry point returns an int status (ZG_OK == 0); none aborts, throws or
+ * falls back to the CPU.  Pointers are plain host pointers unless a parameter is
+ * named `cuda_stream` (a cudaStream_t passed as void*, NULL = legacy stream).
+ *
+ * Reference interfaces replaced (paths inside jy-yuan/sampling-graph-mining):
+ *   Graph<E> + CSRConstructor       include/Graph.hpp:148-166, src/Graph.cpp:215-377
+ *   GraphFilter (AllPredicate)      include/GraphFilters.hpp:9-18, src/GraphFilters.cpp:17-177
+ *   GraphSampler (ELP subsample)    include/Graph.hpp:234-244, src/Graph.cpp:629-780
+ *   ZGraphInstance::calculate       include/ZGraphInstance.hpp:125, src/ZGraphInstance.cpp:257-297
+ *   estimate() bodies               applications/<App>.cpp, src/SamplerGenerator.cpp:461-546
+ *   ZGraphInstanceWithCache         include/ZGraphInstance.hpp:196-214, src/ZGraphInstance.cpp:749-833
+ *   naive exact counters            naive_implementation/<Counter>.cpp
+ */
+#ifndef ZGRAPH_GPU_H
+#define ZGRAPH_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------- */
+#define ZG_OK                         0
+#define ZG_ERR_INVALID_ARG            1
+#define ZG_ERR_OOM                    2
+#define ZG_ERR_CUDA                   3
+#define ZG_ERR_INVALID_GRAPH          4  /* self-loop, duplicate edge, id out of range */
+#define ZG_ERR_UNSUPPORTED_ESTIMATOR  5
+#define ZG_ERR_TIMEOUT                6  /* a bounded device wait gave up */
+#define ZG_ERR_BOUND_NOT_MET          7
+#define ZG_ERR_NO_DEVICE              8
+#define ZG_ERR_OVERFLOW               9  /* an exact weight left the 192-bit range */
+#define ZG_ERR_TOO_LARGE             10  /* a size beyond a documented maximum */
+
+/* ---- estimator programs: the applications' estimate() bodies ------------- */
+#define ZG_PROG_TRIANGLE      1  /* applications/Triangle.cpp:48-73 (also the predicate apps) */
+#define ZG_PROG_FOUR_CLIQUE   2  /* applications/FourClique.cpp:199-234                         */
+#define ZG_PROG_THREE_CHAIN   3  /* applications/ThreeChain.cpp:315-330                         */
+#define ZG_PROG_FOUR_CHAIN    4  /* applications/FourChain.cpp:24-124                           */
+#define ZG_PROG_CHAIN         5  /* applications/ChainMining.cpp:240-84 (param = order k)       */
+#define ZG_PROG_PATTERN       6  /* SamplerGenerator<Empty>::estimate, src/SamplerGenerator.cpp */
+
+/* ---- exact counters: naive_implementation/<Counter>.cpp --------------------------- */
+#define ZG_EXACT_TRIANGLE     1  /* TriangleCounting.cpp            */
+#define ZG_EXACT_WEDGE        2  /* ThreeChain.cpp  (sum C(d,2))    */
+#define ZG_EXACT_THREE_PATH   3  /* FourChain.cpp   (3-edge paths)  */
+#define ZG_EXACT_FIVE_STAR    4  /* FiveStar.cpp    (sum C(d,4))    */
+#define ZG_EXACT_FOUR_CLIQUE  5  /* FourClique.cpp                  */
+
+/* ---- edge predicates for GraphFilter (std::function<bool(VertexId)>) ------ */
+#define ZG_PRED_GE            1  /* w >= t0       (AllPredicateWeightedTriangle.cpp:101-103) */
+#define ZG_PRED_LT            2  /* w <  t0       (AtLeastOnePredicateWeightedTriangle.cpp:138-140) */
+#define ZG_PRED_GT            3
+#define ZG_PRED_LE            4
+#define ZG_PRED_EQ            5
+#define ZG_PRED_NE            6
+#define ZG_PRED_RANGE         7  /* t0 <= w < t1  */
+
+#define ZG_NO_SHUFFLE         0xffffffffffffffffull
+
+/* Per-sample draw capacity and list capacity (MAX_LIST_SIZE, include/ZGraphInstance.hpp:16). */
+#define ZG_MAX_DRAWS          16
+#define ZG_MAX_LIST           16
+
+typedef struct zg_graph zg_graph;     /* device-resident graph (opaque)   */
+typedef struct zg_program zg_program; /* estimator program (opaque)       */
+
+/* Graph metadata.  num_edges / max_degree are the reference's Graph<E>::num_edges and
+ * ::max_degree (include/Graph.hpp:155-158), which GraphSampler/GraphFilter rescale; the
+ * sampler itself always uses the local edge count (num_local_edges). */
+typedef struct zg_graph_meta {
+  uint32_t num_vertices;
+  uint32_t weighted;
+  uint64_t num_local_edges;
+  uint64_t num_edges;
+  uint64_t max_degree;
+  uint64_t device_bytes;
+} zg_graph_meta;
+
+/* Result of one calculate()-style run.  The exact estimate is
+ *   sum_num / 2^den_log2 / samples
+ * where sum_num is a 320-bit little-endian integer: every sample's 1/p is
+ * numerator / 2^shift with numerator = m * prod(S_i) (* 3 for the four-chain program)
+ * and shift = #(conditional steps whose edge appeared twice among the anchors). */
+typedef struct zg_counters {
+  uint64_t samples;
+  uint64_t hits;           /* estimate() returned a non-zero weight                 */
+  uint64_t fails;          /* a primitive returned probability < 0 (no valid edge)   */
+  uint32_t den_log2;
+  uint32_t overflow;       /* non-zero: some numerator exceeded 192 bits            */
+  uint64_t sum_num[5];
+  double   sum_w;          /* sum of 1/p as doubles (fixed block order)             */
+  double   sum_w2;         /* sum of (1/p)^2 as doubles                             */
+  double   estimate;       /* exact mean, rounded once to double                    */
+  double   reserved;
+} zg_counters;
+
+/* Per-sample trace written by zg_run_debug: the draws a replayed Random::rand_int(min,max)
+ * (src/Random.cpp:11-14) must return, and the outcome the estimator must produce. */
+typedef struct zg_sample_trace {
+  uint32_t ndraws;
+  uint32_t hit;
+  uint32_t fail;
+  uint32_t shift;
+  double   w;              /* bit-exact reference value of estimate()               */
+  uint64_t num[3];         /* 192-bit exact numerator                               */
+  uint64_t lo[ZG_MAX_DRAWS];
+  uint64_t hi[ZG_MAX_DRAWS];
+  uint64_t val[ZG_MAX_DRAWS];
+} zg_sample_trace;
+
+/* ---- library / device --------------------------------------------------- */
+/* Returns the ABI version (monotonic). */
+int zg_version(void);
+/* Selects and checks the device (replaces NetworkInterface/SharedMemSys set-up,
+ * src/NetworkInterface.cpp:5-10, src/SharedMemSys.cpp:13-46). */
+int zg_init(int device);
+/* Human-readable text of the last error on this thread. */
+const char* zg_last_error(void);
+
+/* ---- graph store -------------------------------------------------------- */
+/* Uploads a COO edge list in edge-id order (edge id == position, src/Graph.cpp:295-306) and
+ * builds, on the device, the edge-id-ordered adjacency, the neighbour-sorted adjacency and
+ * per-edge ranks.  edges: 2*m uint32 (src,dst) pairs; weights: m uint32 or NULL.
+ * Replaces CSRConstructor::construct_bitmap_assisted_csr (src/Graph.cpp:215-377) minus its
+ * shuffle (the caller's order is kept; see zg_graph_permuted for a device shuffle). */
+int zg_graph_create(const uint32_t* edges, uint64_t m, uint32_t num_vertices,
+                    const uint32_t* weights, void* cuda_stream, zg_graph** out);
+/* Same as zg_graph_create after a seeded device permutation of the edge order, the
+ * rebuild's counterpart of the Fisher-Yates shuffle at src/Graph.cpp:218-231.
+ * parent_index (m entries, may be NULL) receives, for every new edge id, its input position. */
+int zg_graph_permuted(const uint32_t* edges, uint64_t m, uint32_t num_vertices,
+                      const uint32_t* weights, uint64_t shuffle_seed, void* cuda_stream,
+                      uint64_t* parent_index, zg_graph** out);
+int zg_graph_free(zg_graph* g);
+int zg_graph_get_meta(const zg_graph* g, zg_graph_meta* out);
+int zg_graph_set_meta(zg_graph* g, uint64_t num_edges, uint64_t max_degree);
+/* Copies the device arrays back (test/inspection).  Any pointer may be NULL.
+ *   edges   : 2*m (src,dst) in edge-id order     weights: m
+ *   offsets : V+1 int64                          adj_e  : 2*2m (nbr, edge_id) edge-id order
+ *   adj_n   : 2*2m (nbr, edge_id) neighbour order
+ *   suffix  : 2*m (entries after the edge in its src list, in its dst list) */
+int zg_graph_download(const zg_graph* g, uint32_t* edges, uint32_t* weights, int64_t* offsets,
+                      uint32_t* adj_e, uint32_t* adj_n, uint32_t* suffix);
+/* GraphFilter::generate_graph (src/GraphFilters.cpp:17-177): keeps the edges whose weight
+ * satisfies the predicate, in order, then permutes them with shuffle_seed (ZG_NO_SHUFFLE keeps
+ * the order) and rebuilds the adjacency.  num_edges/max_degree follow :90-135.
+ * parent_index (may be NULL, capacity m of the input) receives the input edge id of every
+ * output edge; *out_m its length. */
+int zg_graph_filter(const zg_graph* g, int pred_op, int64_t t0, int64_t t1,
+                    uint64_t shuffle_seed, void* cuda_stream, uint64_t* parent_index,
+                    uint64_t* out_m, zg_graph** out);
+/* GraphSampler::sample_graph (src/Graph.cpp:629-780): keeps edge e iff its draw in
+ * [1, 2^30] is <= floor(rate * 2^30), draws from keep_seed; then as zg_graph_filter. */
+int zg_graph_subsample(const zg_graph* g, double rate, uint64_t keep_seed,
+                       uint64_t shuffle_seed, void* cuda_stream, uint64_t* parent_index,
+                       uint64_t* out_m, zg_graph** out);
+
+/* ---- estimator programs -------------------------------------------------- */
+/* kind: ZG_PROG_*; param: chain order for ZG_PROG_CHAIN (3..16), else 0. */
+int zg_program_create(int kind, uint32_t param, zg_program** out);
+/* SamplerGenerator(graph, Pattern) (src/SamplerGenerator.cpp:393-445): pattern with
+ * num_vertices (<= 8) vertices and num_edges (<= 15) edges given as (src,dst) pairs. */
+int zg_program_create_pattern(uint32_t num_vertices, uint32_t num_edges,
+                              const uint32_t* edges, zg_program** out);
+int zg_program_free(zg_program* p);
+/* num_unique: number of unique relabelled patterns (SamplerGenerator's num_unique_patterns);
+ * cond_calls: conditional_sample_edge calls of a successful estimate (the ELP's probe);
+ * vertices: num_vertices_in_pattern. */
+int zg_program_info(const zg_program* p, uint32_t* num_unique, uint32_t* cond_calls,
+                    uint32_t* vertices);
+
+/* ---- sampling ------------------------------------------------------------ */
+/* Runs n estimators, sample indices [first_sample, first_sample+n), on Philox stream
+ * (seed, stream_id); the device counterpart of ZGraphInstance::calculate
+ * (src/ZGraphInstance.cpp:257-297) without the Estimation fold, which the host does. */
+int zg_run(const zg_graph* g, const zg_program* p, uint64_t n, uint64_t first_sample,
+           uint64_t seed, uint32_t stream_id, void* cuda_stream, zg_counters* out);
+/* As zg_run, one trace per sample (n <= 2^22). */
+int zg_run_debug(const zg_graph* g, const zg_program* p, uint64_t n, uint64_t first_sample,
+                 uint64_t seed, uint32_t stream_id, zg_sample_trace* traces);
+/* ThreeMotif (applications/ThreeMotif.cpp:43-122,149-196): n_chain 3-chain estimators
+ * (stream_chain) whose wedges are cached; the first min(n_chain, n_tri) triangle estimators
+ * close the cached wedges, the rest sample afresh on stream_tri. */
+int zg_run_three_motif(const zg_graph* g, uint64_t n_chain, uint64_t n_tri, uint64_t seed,
+                       uint32_t stream_chain, uint32_t stream_tri, void* cuda_stream,
+                       zg_counters* out_chain, zg_counters* out_tri);
+int zg_run_three_motif_debug(const zg_graph* g, uint64_t n_chain, uint64_t n_tri,
+                             uint64_t seed, uint32_t stream_chain, uint32_t stream_tri,
+                             zg_sample_trace* chain_traces, zg_sample_trace* tri_traces);
+
+/* ---- exact counts ---------------------------------------------------------- */
+/* out[0..1]: 128-bit little-endian count.  kind: ZG_EXACT_*. */
+int zg_exact_count(const zg_graph* g, int kind, void* cuda_stream, uint64_t out[2]);
+
+/* ---- synthetic inputs (host) ------------------------------------------------ */
+/* The reference reads SNAP files prepared by datasets/toolkits/edgelist_to_biedgelist.cpp;
+ * these seeded generators stand in for them.  Output: undirected, no self-loops or duplicates,
+ * random order and orientation.  edges == NULL only reports *m_out; otherwise capacity is the
+ * number of (src,dst) pairs edges can hold. */
+int zg_gen_rmat(uint32_t scale, uint32_t edge_factor, double a, double b, double c, uint64_t seed,
+                uint64_t capacity, uint32_t* edges, uint64_t* m_out);
+int zg_gen_chung_lu(uint32_t num_vertices, double exponent, double avg_degree, uint64_t seed,
+                    uint64_t capacity, uint32_t* edges, uint64_t* m_out);
+/* Edge data uniform in [0, max_value) (datasets/toolkits/get_weighted_datasets.cpp:28-43). */
+int zg_gen_weights(uint64_t m, uint32_t max_value, uint64_t seed, uint32_t* weights);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ZGRAPH_GPU_H */

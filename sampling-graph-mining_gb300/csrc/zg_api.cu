@@ -1,0 +1,149 @@
+// zg_api.cu — library entry points: device selection, errors, estimator programs.
+#include <stdarg.h>
+#include <stdio.h>
+
+#include <algorithm>
+#include <mutex>
+#include <set>
+#include <vector>
+
+#include "zg_internal.cuh"
+
+static thread_local char g_err[512] = "";
+
+const char* zg_set_error(int code, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  int n = snprintf(g_err, sizeof(g_err), "[zg %d] ", code);
+  vsnprintf(g_err + n, sizeof(g_err) - n, fmt, ap);
+  va_end(ap);
+  return g_err;
+}
+
+int zg_check_cuda(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return ZG_OK;
+  zg_set_error(ZG_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+  return e == cudaErrorMemoryAllocation ? ZG_ERR_OOM : ZG_ERR_CUDA;
+}
+
+int zg_num_sms() {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 1;
+  }
+  return sms;
+}
+
+extern "C" int zg_version(void) { return 1; }
+
+extern "C" const char* zg_last_error(void) { return g_err; }
+
+extern "C" int zg_init(int device) {
+  int count = 0;
+  cudaError_t e = cudaGetDeviceCount(&count);
+  if (e != cudaSuccess || count == 0) {
+    cudaGetLastError();
+    zg_set_error(ZG_ERR_NO_DEVICE, "no CUDA device: %s", cudaGetErrorString(e));
+    return ZG_ERR_NO_DEVICE;
+  }
+  if (device < 0 || device >= count) {
+    zg_set_error(ZG_ERR_INVALID_ARG, "device %d of %d", device, count);
+    return ZG_ERR_INVALID_ARG;
+  }
+  ZG_CUDA(cudaSetDevice(device));
+  cudaDeviceProp prop;
+  ZG_CUDA(cudaGetDeviceProperties(&prop, device));
+  if (prop.major * 10 + prop.minor != 103) {
+    zg_set_error(ZG_ERR_NO_DEVICE, "device %d is sm_%d%d; this build targets sm_103a", device, prop.major,
+                 prop.minor);
+    return ZG_ERR_NO_DEVICE;
+  }
+  ZG_CUDA(cudaFree(nullptr));
+  return ZG_OK;
+}
+
+// ---- programs ---------------------------------------------------------------------------
+static uint32_t pair_bit_host(uint32_t i, uint32_t j, uint32_t pv) {
+  if (i > j) std::swap(i, j);
+  return i * (2 * pv - i - 1) / 2 + (j - i - 1);
+}
+
+extern "C" int zg_program_create(int kind, uint32_t param, zg_program** out) {
+  if (!out) return zg_set_error(ZG_ERR_INVALID_ARG, "null output"), ZG_ERR_INVALID_ARG;
+  if (kind < ZG_PROG_TRIANGLE || kind > ZG_PROG_CHAIN)
+    return zg_set_error(ZG_ERR_UNSUPPORTED_ESTIMATOR, "unknown program kind %d", kind), ZG_ERR_UNSUPPORTED_ESTIMATOR;
+  if (kind == ZG_PROG_CHAIN && (param < 3 || param > ZG_MAX_LIST))
+    return zg_set_error(ZG_ERR_INVALID_ARG, "chain order %u outside [3, %d]", param, ZG_MAX_LIST),
+           ZG_ERR_INVALID_ARG;
+  zg_program* p = new zg_program();
+  memset(p, 0, sizeof(*p));
+  p->kind = kind;
+  p->param = kind == ZG_PROG_CHAIN ? param : 0;
+  *out = p;
+  return ZG_OK;
+}
+
+// SamplerGenerator ctor (src/SamplerGenerator.cpp:344-366, 393-445): every relabelling of the
+// pattern in generate_mapping's order, de-duplicated as edge sets; stored as sorted 28-bit masks.
+extern "C" int zg_program_create_pattern(uint32_t pv, uint32_t pe, const uint32_t* edges, zg_program** out) {
+  if (!out || !edges) return zg_set_error(ZG_ERR_INVALID_ARG, "null argument"), ZG_ERR_INVALID_ARG;
+  if (pv < 2 || pv > ZG_MAX_PATTERN_V || pe < 1 || pe > ZG_MAX_LIST - 1)
+    return zg_set_error(ZG_ERR_UNSUPPORTED_ESTIMATOR, "pattern with %u vertices / %u edges is outside 2..%d / 1..%d",
+                        pv, pe, ZG_MAX_PATTERN_V, ZG_MAX_LIST - 1),
+           ZG_ERR_UNSUPPORTED_ESTIMATOR;
+  for (uint32_t e = 0; e < pe; ++e)
+    if (edges[2 * e] >= pv || edges[2 * e + 1] >= pv || edges[2 * e] == edges[2 * e + 1])
+      return zg_set_error(ZG_ERR_INVALID_ARG, "pattern edge %u is invalid", e), ZG_ERR_INVALID_ARG;
+  std::vector<uint32_t> perm(pv);
+  for (uint32_t i = 0; i < pv; ++i) perm[i] = i;
+  std::set<uint32_t> masks;
+  do {
+    uint32_t mask = 0;
+    for (uint32_t e = 0; e < pe; ++e) mask |= 1u << pair_bit_host(perm[edges[2 * e]], perm[edges[2 * e + 1]], pv);
+    masks.insert(mask);
+  } while (std::next_permutation(perm.begin(), perm.end()));
+  std::vector<uint32_t> sorted(masks.begin(), masks.end());
+  zg_program* p = new zg_program();
+  memset(p, 0, sizeof(*p));
+  p->kind = ZG_PROG_PATTERN;
+  p->pv = pv;
+  p->pe = pe;
+  memcpy(p->pedges, edges, sizeof(uint32_t) * 2 * pe);
+  p->num_unique = (uint32_t)sorted.size();
+  cudaError_t e = cudaMalloc((void**)&p->d_masks, sizeof(uint32_t) * sorted.size());
+  if (e == cudaSuccess)
+    e = cudaMemcpy(p->d_masks, sorted.data(), sizeof(uint32_t) * sorted.size(), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    if (p->d_masks) cudaFree(p->d_masks);
+    delete p;
+    return zg_check_cuda(e, "pattern masks");
+  }
+  *out = p;
+  return ZG_OK;
+}
+
+extern "C" int zg_program_free(zg_program* p) {
+  if (!p) return ZG_OK;
+  if (p->d_masks) cudaFree(p->d_masks);
+  delete p;
+  return ZG_OK;
+}
+
+extern "C" int zg_program_info(const zg_program* p, uint32_t* num_unique, uint32_t* cond_calls, uint32_t* vertices) {
+  if (!p) return zg_set_error(ZG_ERR_INVALID_ARG, "null program"), ZG_ERR_INVALID_ARG;
+  uint32_t cc = 0, vv = 0;
+  switch (p->kind) {
+    case ZG_PROG_TRIANGLE: cc = 1; vv = 3; break;
+    case ZG_PROG_FOUR_CLIQUE: cc = 2; vv = 4; break;
+    case ZG_PROG_THREE_CHAIN: cc = 1; vv = 3; break;
+    case ZG_PROG_FOUR_CHAIN: cc = 2; vv = 4; break;
+    case ZG_PROG_CHAIN: cc = p->param - 2; vv = p->param; break;
+    default: cc = p->pe - 1; vv = p->pv; break;
+  }
+  if (num_unique) *num_unique = p->kind == ZG_PROG_PATTERN ? p->num_unique : 1;
+  if (cond_calls) *cond_calls = cc;
+  if (vertices) *vertices = vv;
+  return ZG_OK;
+}

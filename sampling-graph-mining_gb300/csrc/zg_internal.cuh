@@ -1,0 +1,157 @@
+// zg_internal.cuh — shared device/host definitions of libzgraph_gpu.
+//
+// Device graph layout (all arrays in HBM, built by zg_graph.cu):
+//   rec[m]    uint4 (src, dst, suf_src, suf_dst): COO in edge-id order (edge id = position,
+//             src/Graph.cpp:295-306) plus, per endpoint, how many entries follow this edge in that
+//             endpoint's edge-id-ordered list.  suf gives the first conditional step's suffix
+//             size S without a search and locates the edge inside either list.
+//   off[V+1]  int64 offsets shared by both adjacency arrays (outgoing_adj_index).
+//   adj_e[2m] uint2 (nbr, edge_id) sorted by edge id per vertex (outgoing_adj_list order,
+//             asserted at src/Graph.cpp:324-334): the sampling order.
+//   adj_n[2m] uint2 (nbr, edge_id) sorted by (nbr, edge_id) per vertex: closure look-ups.
+//   w[m]      uint32 edge data (Graph<VertexId>) or null.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/zgraph_gpu.h"
+
+#define ZG_STREAM_SHUFFLE 0xFFFFFFF0u
+#define ZG_STREAM_SUBSAMPLE 0xFFFFFFF1u
+
+struct ZgDevGraph {
+  uint32_t nv;
+  uint32_t pad;
+  uint64_t m;
+  const uint4* rec;
+  const int64_t* off;
+  const uint2* adj_e;
+  const uint2* adj_n;
+  const uint32_t* w;
+};
+
+struct zg_graph {
+  ZgDevGraph d;
+  uint4* rec;
+  int64_t* off;
+  uint2* adj_e;
+  uint2* adj_n;
+  uint32_t* w;
+  uint64_t num_edges;   // Graph::num_edges metadata
+  uint64_t max_degree;  // Graph::max_degree metadata
+  uint64_t bytes;
+};
+
+// Program descriptor (host copy; device parameters are passed by value).
+#define ZG_MAX_PATTERN_V 8
+#define ZG_MAX_UNIQUE 40320
+struct zg_program {
+  int kind;
+  uint32_t param;
+  uint32_t pv, pe;
+  uint32_t pedges[2 * ZG_MAX_LIST];
+  uint32_t num_unique;
+  uint32_t* d_masks;  // sorted unique relabelled edge masks (pattern programs)
+};
+
+struct ZgProgParams {
+  int kind;
+  uint32_t param;
+  uint32_t pv, pe;
+  uint32_t num_unique;
+  const uint32_t* masks;
+  uint32_t den_log2;
+};
+
+// Per-block partial of one run; reduced by a single-block finalize kernel.
+struct ZgPartial {
+  unsigned long long samples, hits, fails, overflow;
+  unsigned long long lane[8];  // 32-bit halves of the exact 256-bit sum, carry-saved
+  double sum_w, sum_w2;
+};
+
+// ----------------------------------------------------------------------------------------
+// Philox4x32-10 (Salmon et al., SC'11); identical to the CPU oracle's.
+__host__ __device__ __forceinline__ void zg_philox(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
+                                                   uint32_t k0, uint32_t k1, uint32_t& o0,
+                                                   uint32_t& o1) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    if (r) {
+      k0 += 0x9E3779B9u;
+      k1 += 0xBB67AE85u;
+    }
+#ifdef __CUDA_ARCH__
+    uint32_t hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
+    uint32_t hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
+#else
+    uint64_t p0 = (uint64_t)0xD2511F53u * c0, p1 = (uint64_t)0xCD9E8D57u * c2;
+    uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+    uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+#endif
+    uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+    c0 = n0;
+    c1 = lo1;
+    c2 = n2;
+    c3 = lo0;
+  }
+  o0 = c0;
+  o1 = c1;
+}
+
+__host__ __device__ __forceinline__ uint64_t zg_mulhi64(uint64_t a, uint64_t b) {
+#ifdef __CUDA_ARCH__
+  return __umul64hi(a, b);
+#else
+  return (uint64_t)(((unsigned __int128)a * b) >> 64);
+#endif
+}
+
+// Draw d of `sample` in [lo, hi]: counter (sample, d, stream), key seed; multiply-high mapping.
+__host__ __device__ __forceinline__ uint64_t zg_draw(uint64_t seed, uint32_t stream, uint64_t sample,
+                                                     uint32_t d, uint64_t lo, uint64_t hi) {
+  uint32_t o0, o1;
+  zg_philox((uint32_t)sample, (uint32_t)(sample >> 32), d, stream, (uint32_t)seed,
+            (uint32_t)(seed >> 32), o0, o1);
+  uint64_t r = ((uint64_t)o1 << 32) | o0;
+  uint64_t range = hi - lo + 1;
+  if (range == 0) return r;
+  return lo + zg_mulhi64(r, range);
+}
+
+// 192-bit unsigned numerator.
+struct ZgU192 {
+  uint64_t l[3];
+};
+__host__ __device__ __forceinline__ void zg_u192_set(ZgU192& a, uint64_t v) {
+  a.l[0] = v;
+  a.l[1] = 0;
+  a.l[2] = 0;
+}
+// a *= f; returns true on overflow beyond 192 bits.
+__host__ __device__ __forceinline__ bool zg_u192_mul(ZgU192& a, uint64_t f) {
+  uint64_t lo0 = a.l[0] * f, hi0 = zg_mulhi64(a.l[0], f);
+  uint64_t lo1 = a.l[1] * f, hi1 = zg_mulhi64(a.l[1], f);
+  uint64_t lo2 = a.l[2] * f, hi2 = zg_mulhi64(a.l[2], f);
+  uint64_t r1 = lo1 + hi0;
+  uint64_t c1 = r1 < lo1;
+  uint64_t r2 = lo2 + hi1;
+  uint64_t c2 = r2 < lo2;
+  uint64_t r2b = r2 + c1;
+  c2 += r2b < r2;
+  a.l[0] = lo0;
+  a.l[1] = r1;
+  a.l[2] = r2b;
+  return (hi2 | c2) != 0;
+}
+
+const char* zg_set_error(int code, const char* fmt, ...);
+int zg_check_cuda(cudaError_t e, const char* what);
+#define ZG_CUDA(call)                                   \
+  do {                                                  \
+    cudaError_t _e = (call);                            \
+    if (_e != cudaSuccess) return zg_check_cuda(_e, #call); \
+  } while (0)
+
+int zg_num_sms();

@@ -1,0 +1,1229 @@
+// zg_sample.cu — the neighbour-sampling estimator hot path on sm_103a.
+//
+// One estimator (sample) per thread on a persistent grid sized to the SM count.  Every
+// estimator draws from its own Philox4x32-10 counter stream (seed, stream_id, sample index,
+// draw index), so results do not depend on the launch shape.  Each program below restates one
+// application estimate() (cited) on the device layout of zg_internal.cuh:
+//   * the first conditional step reads its suffix sizes S from rec[] (no search);
+//   * later steps locate lower bounds by binary search inside ranges the per-edge suffix
+//     counts already narrow;
+//   * closure checks (conditional_close, src/ZGraphInstance.cpp:372-407) binary-search the
+//     shorter neighbour-sorted list instead of scanning every sampled vertex's list.
+// Weights are exact: numerator m*prod(S_i) (192-bit) over 2^shift; per-block partial sums are
+// reduced by a single-block finalize kernel in a fixed order.  The debug variant additionally
+// records every draw and the reference's double 1/p computed with the same IEEE operation
+// sequence as the application (x87 extended arithmetic restated in integers for ChainMining).
+#include <algorithm>
+#include <mutex>
+#include <vector>
+
+#include "zg_internal.cuh"
+
+namespace {
+
+#define ZG_LDG(p) __ldg(p)
+
+struct Ctx {
+  uint64_t seed;
+  uint64_t sample;
+  uint32_t stream;
+  uint32_t nd;
+  zg_sample_trace* tr;  // debug only
+  __device__ __forceinline__ uint64_t draw(uint64_t lo, uint64_t hi) {
+    uint64_t v = zg_draw(seed, stream, sample, nd, lo, hi);
+    if (tr && nd < ZG_MAX_DRAWS) {
+      tr->lo[nd] = lo;
+      tr->hi[nd] = hi;
+      tr->val[nd] = v;
+    }
+    ++nd;
+    return v;
+  }
+};
+
+struct Res {
+  bool hit;
+  bool fail;
+  bool ovf;
+  uint32_t shift;
+  ZgU192 num;
+  double w;  // debug: reference double
+};
+
+__device__ __forceinline__ void res_init(Res& r) {
+  r.hit = false;
+  r.fail = false;
+  r.ovf = false;
+  r.shift = 0;
+  zg_u192_set(r.num, 1);
+  r.w = 0.0;
+}
+__device__ __forceinline__ void res_mul(Res& r, uint64_t f) {
+  if (zg_u192_mul(r.num, f)) r.ovf = true;
+}
+
+// first index in adj_e[lo, hi) whose edge id >= key
+__device__ __forceinline__ int64_t lb_eid(const uint2* __restrict__ adj, int64_t lo, int64_t hi, uint32_t key) {
+  while (lo < hi) {
+    int64_t mid = (lo + hi) >> 1;
+    if (ZG_LDG(&adj[mid]).y < key)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
+// Does edge (x,y) exist with edge id >= min_valid?  Searches the shorter neighbour-sorted list
+// for the last entry with nbr == target (duplicates, if any, are ordered by edge id).
+__device__ __forceinline__ bool edge_after(int64_t bx, int64_t ex, int64_t by, int64_t ey, uint32_t x, uint32_t y,
+                                           uint32_t min_valid, const uint2* __restrict__ adj_n) {
+  int64_t lo = bx, hi = ex;
+  uint32_t t = y;
+  if (ex - bx > ey - by) {
+    lo = by;
+    hi = ey;
+    t = x;
+  }
+  int64_t b = lo;
+  while (lo < hi) {
+    int64_t mid = (lo + hi) >> 1;
+    if (ZG_LDG(&adj_n[mid]).x <= t)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  if (lo == b) return false;
+  uint2 a = ZG_LDG(&adj_n[lo - 1]);
+  return a.x == t && a.y >= min_valid;
+}
+
+__device__ __forceinline__ bool edge_after_v(const ZgDevGraph& g, uint32_t x, uint32_t y, uint32_t min_valid) {
+  int64_t bx = ZG_LDG(&g.off[x]), ex = ZG_LDG(&g.off[x + 1]);
+  int64_t by = ZG_LDG(&g.off[y]), ey = ZG_LDG(&g.off[y + 1]);
+  return edge_after(bx, ex, by, ey, x, y, min_valid, g.adj_n);
+}
+
+// ---- reference doubles (debug) ---------------------------------------------------------
+__device__ __forceinline__ double ddiv(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double u2d(uint64_t v) { return __ull2double_rn(v); }
+
+// x87 extended (64-bit mantissa, round-to-nearest-even), restated in integers.
+struct Ext {
+  uint64_t m;
+  int32_t e;
+};
+__device__ __forceinline__ Ext ext_from_double(double d) {
+  uint64_t b = (uint64_t)__double_as_longlong(d);
+  int ex = (int)((b >> 52) & 0x7ff);
+  Ext r;
+  r.m = ((b & ((1ull << 52) - 1)) | (1ull << 52)) << 11;
+  r.e = ex - 1075 - 11;
+  return r;
+}
+__device__ __forceinline__ Ext ext_mul(Ext a, Ext b) {
+  uint64_t lo = a.m * b.m, hi = __umul64hi(a.m, b.m);
+  uint64_t keep, rem, half = 1ull << 63;
+  Ext r;
+  if (hi >> 63) {
+    keep = hi;
+    rem = lo;
+    r.e = a.e + b.e + 64;
+  } else {
+    keep = (hi << 1) | (lo >> 63);
+    rem = lo << 1;
+    r.e = a.e + b.e + 63;
+  }
+  if (rem > half || (rem == half && (keep & 1))) {
+    keep++;
+    if (keep == 0) {
+      keep = 1ull << 63;
+      r.e++;
+    }
+  }
+  r.m = keep;
+  return r;
+}
+// 2^127 / m for m in (2^63, 2^64): restoring division, 64 quotient bits.
+__device__ __forceinline__ Ext ext_inv(Ext a) {
+  Ext r;
+  if (a.m == (1ull << 63)) {
+    r.m = 1ull << 63;
+    r.e = -126 - a.e;
+    return r;
+  }
+  // remainder arithmetic on 65-bit values: rem < m < 2^64
+  uint64_t q = 0, rem = 1ull << 63;  // 2^127 = 2^63 * 2^64: start with rem = 2^63, shift in 64 zero bits
+  for (int i = 0; i < 64; ++i) {
+    bool top = rem >> 63;
+    rem <<= 1;
+    q <<= 1;
+    if (top || rem >= a.m) {
+      rem -= a.m;
+      q |= 1;
+    }
+  }
+  r.e = -127 - a.e;
+  // round: compare 2*rem with m
+  bool top = rem >> 63;
+  uint64_t rem2 = rem << 1;
+  bool gt = top || rem2 > a.m;
+  bool eq = !top && rem2 == a.m;
+  if (gt || (eq && (q & 1))) {
+    q++;
+    if (q == 0) {
+      q = 1ull << 63;
+      r.e++;
+    }
+  }
+  r.m = q;
+  return r;
+}
+__device__ __forceinline__ double ext_to_double(Ext a) {
+  uint64_t keep = a.m >> 11, rem = a.m & 0x7ff;
+  int e = a.e + 11;
+  if (rem > 0x400 || (rem == 0x400 && (keep & 1))) {
+    keep++;
+    if (keep == (1ull << 53)) {
+      keep >>= 1;
+      e++;
+    }
+  }
+  return scalbn(u2d(keep), e);
+}
+
+// ---- Triangle: applications/Triangle.cpp:48-73 -----------------------------------------
+template <bool DBG>
+__device__ void prog_triangle(const ZgDevGraph& g, Ctx& c, Res& r) {
+  if (g.m == 0) {
+    r.fail = true;
+    return;
+  }
+  uint64_t e0 = c.draw(0, g.m - 1);
+  uint4 q = ZG_LDG(&g.rec[e0]);
+  uint64_t S = (uint64_t)q.z + q.w;
+  if (S == 0) {
+    r.fail = true;
+    return;
+  }
+  uint64_t r1 = c.draw(0, S - 1);
+  uint32_t anchor = q.x, other = q.y, suf = q.z;
+  if (r1 >= q.z) {
+    r1 -= q.z;
+    anchor = q.y;
+    other = q.x;
+    suf = q.w;
+  }
+  // closing-edge endpoint `other` offsets do not depend on the second edge: issue early
+  int64_t bo = ZG_LDG(&g.off[other]), eo = ZG_LDG(&g.off[other + 1]);
+  int64_t idx = ZG_LDG(&g.off[anchor + 1]) - (int64_t)suf + (int64_t)r1;
+  uint2 e1 = ZG_LDG(&g.adj_e[idx]);
+  uint32_t a1 = 1 + (e1.x == q.x || e1.x == q.y);
+  res_mul(r, g.m);
+  res_mul(r, S);
+  if (a1 == 2) r.shift = 1;
+  int64_t bc = ZG_LDG(&g.off[e1.x]), ec = ZG_LDG(&g.off[e1.x + 1]);
+  bool closed = (a1 == 1) && edge_after(bo, eo, bc, ec, other, e1.x, e1.y + 1, g.adj_n);
+  r.hit = closed;
+  if (DBG && closed) {
+    double p = 1.0;
+    p = dmul(p, ddiv(1.0, u2d(g.m)));
+    p = dmul(p, ddiv(1.0 * a1, u2d(S)));
+    r.w = ddiv(1.0, p);
+  }
+}
+
+// ---- ThreeChain: applications/ThreeChain.cpp:315-330 -------------------------------------
+template <bool DBG>
+__device__ void prog_three_chain(const ZgDevGraph& g, Ctx& c, Res& r) {
+  if (g.m == 0) {
+    r.fail = true;
+    return;
+  }
+  uint64_t e0 = c.draw(0, g.m - 1);
+  uint4 q = ZG_LDG(&g.rec[e0]);
+  uint64_t S = (uint64_t)q.z + q.w;
+  if (S == 0) {
+    r.fail = true;
+    return;
+  }
+  uint64_t r1 = c.draw(0, S - 1);
+  // The chosen edge only sets the appearance count a, which is 1 on a simple graph
+  // (zg_graph_create rejects duplicate edges); the debug variant reads it and checks.
+  uint32_t a1 = 1;
+  if (DBG) {
+    uint32_t anchor = q.x, suf = q.z;
+    if (r1 >= q.z) {
+      r1 -= q.z;
+      anchor = q.y;
+      suf = q.w;
+    }
+    uint2 e1 = ZG_LDG(&g.adj_e[ZG_LDG(&g.off[anchor + 1]) - (int64_t)suf + (int64_t)r1]);
+    a1 = 1 + (e1.x == q.x || e1.x == q.y);
+  }
+  res_mul(r, g.m);
+  res_mul(r, S);
+  if (a1 == 2) r.shift = 1;
+  r.hit = true;
+  if (DBG) {
+    double p = 1.0;
+    p = dmul(p, ddiv(1.0, u2d(g.m)));
+    p = dmul(p, ddiv(1.0 * a1, u2d(S)));
+    r.w = ddiv(1.0, p);
+  }
+}
+
+// ---- FourClique: applications/FourClique.cpp:176-234 -------------------------------------
+template <bool DBG>
+__device__ void prog_four_clique(const ZgDevGraph& g, Ctx& c, Res& r) {
+  if (g.m == 0) {
+    r.fail = true;
+    return;
+  }
+  uint64_t e0 = c.draw(0, g.m - 1);
+  uint4 q = ZG_LDG(&g.rec[e0]);
+  uint64_t S1 = (uint64_t)q.z + q.w;
+  if (S1 == 0) {
+    r.fail = true;
+    return;
+  }
+  uint64_t r1 = c.draw(0, S1 - 1);
+  // vertex slots in insertion order: 0 = a (e0.src), 1 = b (e0.dst), 2 = c, 3 = d
+  uint32_t v[4];
+  int64_t beg[4], end[4], lb[3];
+  v[0] = q.x;
+  v[1] = q.y;
+  end[0] = ZG_LDG(&g.off[q.x + 1]);
+  end[1] = ZG_LDG(&g.off[q.y + 1]);
+  int s1 = 0;  // slot of the first conditional edge's anchor
+  uint64_t rr = r1;
+  if (rr >= q.z) {
+    rr -= q.z;
+    s1 = 1;
+  }
+  uint32_t suf1 = s1 ? q.w : q.z;
+  int64_t idx1 = end[s1] - (int64_t)suf1 + (int64_t)rr;
+  uint2 e1 = ZG_LDG(&g.adj_e[idx1]);
+  v[2] = e1.x;
+  uint32_t a1 = 1 + (e1.x == v[0] || e1.x == v[1]);
+  res_mul(r, g.m);
+  res_mul(r, S1);
+  if (a1 == 2) r.shift++;
+  // second conditional step: anchors [a, b, c], min_valid = id1 + 1
+  uint32_t mv = e1.y + 1;
+  uint4 q1 = ZG_LDG(&g.rec[e1.y]);
+  uint32_t sufc = (q1.x == v[2]) ? q1.z : q1.w;
+  end[2] = ZG_LDG(&g.off[v[2] + 1]);
+  lb[s1] = idx1 + 1;
+  int so = 1 - s1;
+  uint32_t sufo = so ? q.w : q.z;
+  lb[so] = lb_eid(g.adj_e, end[so] - (int64_t)sufo, end[so], mv);
+  lb[2] = end[2] - (int64_t)sufc;
+  uint64_t S2 = 0;
+  if (a1 == 1) {
+    S2 = (uint64_t)(end[0] - lb[0]) + (uint64_t)(end[1] - lb[1]) + (uint64_t)(end[2] - lb[2]);
+  } else {
+    // c coincides with a or b (duplicate edges): the reference lists only two vertices
+    S2 = (uint64_t)(end[0] - lb[0]) + (uint64_t)(end[1] - lb[1]);
+  }
+  if (S2 == 0) {
+    r.fail = true;
+    return;
+  }
+  uint64_t r2 = c.draw(0, S2 - 1);
+  int s2 = 0;
+  int nslots = a1 == 1 ? 3 : 2;
+  for (; s2 < nslots - 1; ++s2) {
+    uint64_t len = (uint64_t)(end[s2] - lb[s2]);
+    if (r2 < len) break;
+    r2 -= len;
+  }
+  uint2 e2 = ZG_LDG(&g.adj_e[lb[s2] + (int64_t)r2]);
+  v[3] = e2.x;
+  bool dup = false;
+  for (int i = 0; i < nslots; ++i) dup |= (e2.x == v[i]);
+  uint32_t a2 = 1 + (dup ? 1 : 0);
+  res_mul(r, S2);
+  if (a2 == 2) r.shift++;
+  if (a1 != 1 || dup) return;  // three vertices: a triangle was sampled (FourClique.cpp:224-226)
+  // closure: the 3 pairs of the 4-clique not sampled, all with edge id >= id2 + 1
+  uint32_t mv2 = e2.y + 1;
+  beg[0] = ZG_LDG(&g.off[v[0]]);
+  beg[1] = ZG_LDG(&g.off[v[1]]);
+  beg[2] = ZG_LDG(&g.off[v[2]]);
+  beg[3] = ZG_LDG(&g.off[v[3]]);
+  end[3] = ZG_LDG(&g.off[v[3] + 1]);
+  // sampled pairs: (0,1), (s1,2), (s2,3)
+  bool ok = true;
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = i + 1; j < 4; ++j) {
+      bool sampled = (i == 0 && j == 1) || (i == s1 && j == 2) || (i == s2 && j == 3);
+      if (!sampled && ok) ok = edge_after(beg[i], end[i], beg[j], end[j], v[i], v[j], mv2, g.adj_n);
+    }
+  r.hit = ok;
+  if (DBG && ok) {
+    double p = 1.0;
+    p = dmul(p, ddiv(1.0, u2d(g.m)));
+    p = dmul(p, ddiv(1.0 * a1, u2d(S1)));
+    p = dmul(p, ddiv(1.0 * a2, u2d(S2)));
+    r.w = ddiv(1.0, p);
+  }
+}
+
+// ---- FourChain: applications/FourChain.cpp:24-124 ----------------------------------------
+template <bool DBG>
+__device__ void prog_four_chain(const ZgDevGraph& g, Ctx& c, Res& r) {
+  uint64_t sel = c.draw(1, 3);
+  res_mul(r, 3);
+  if (g.m == 0) {
+    r.fail = true;
+    return;
+  }
+  uint64_t e0 = c.draw(0, g.m - 1);
+  res_mul(r, g.m);
+  uint4 q = ZG_LDG(&g.rec[e0]);
+  uint32_t a = q.x, b = q.y;
+  uint64_t S1, S2;
+  uint32_t a1 = 1, a2 = 1;
+  bool ok;
+  if (sel != 3) {
+    // edges [e0], vertices [a, b]
+    S1 = (uint64_t)q.z + q.w;
+    if (S1 == 0) {
+      r.fail = true;
+      return;
+    }
+    uint64_t r1 = c.draw(0, S1 - 1);
+    uint32_t anchor = a, suf = q.z;
+    if (r1 >= q.z) {
+      r1 -= q.z;
+      anchor = b;
+      suf = q.w;
+    }
+    int64_t idx1 = ZG_LDG(&g.off[anchor + 1]) - (int64_t)suf + (int64_t)r1;
+    uint2 e1 = ZG_LDG(&g.adj_e[idx1]);
+    a1 = 1 + (e1.x == a || e1.x == b);
+    res_mul(r, S1);
+    if (a1 == 2) r.shift++;
+    // the vertex of e1 not shared with e0 (FourChain.cpp:44-54)
+    uint32_t nw;
+    if (a == anchor) nw = e1.x;
+    else if (a == e1.x) nw = anchor;
+    else if (b == anchor) nw = e1.x;
+    else nw = anchor;
+    uint4 q1 = ZG_LDG(&g.rec[e1.y]);
+    uint32_t sufn = (q1.x == nw) ? q1.z : q1.w;  // entries after e1 in nw's list
+    int64_t endn = ZG_LDG(&g.off[nw + 1]);
+    int64_t lbn;
+    if (sel == 1) {
+      // edges [e0, e1]: min_valid = id1 + 1
+      lbn = endn - (int64_t)sufn;
+    } else {
+      // edges [e0]: min_valid = id0 + 1, at or before e1's own slot in nw's list
+      int64_t pos1 = endn - (int64_t)sufn - 1;
+      lbn = lb_eid(g.adj_e, ZG_LDG(&g.off[nw]), pos1 + 1, (uint32_t)e0 + 1);
+    }
+    S2 = (uint64_t)(endn - lbn);
+    if (S2 == 0) {
+      r.fail = true;
+      return;
+    }
+    uint64_t r2 = c.draw(0, S2 - 1);
+    uint2 e2 = ZG_LDG(&g.adj_e[lbn + (int64_t)r2]);
+    a2 = 1 + (e2.x == nw);
+    res_mul(r, S2);
+    if (a2 == 2) r.shift++;
+    ok = !(nw == a || nw == b) && !(e2.x == a || e2.x == b);
+    if (sel == 2) ok = ok && !(e2.y >= e1.y);
+  } else {
+    // vertices [a]: e1 from a's list; then vertices [b]: e2 from b's list; edges [e0]
+    S1 = q.z;
+    if (S1 == 0) {
+      r.fail = true;
+      return;
+    }
+    uint64_t r1 = c.draw(0, S1 - 1);
+    uint2 e1 = ZG_LDG(&g.adj_e[ZG_LDG(&g.off[a + 1]) - (int64_t)q.z + (int64_t)r1]);
+    a1 = 1 + (e1.x == a);
+    res_mul(r, S1);
+    if (a1 == 2) r.shift++;
+    S2 = q.w;
+    if (S2 == 0) {
+      r.fail = true;
+      return;
+    }
+    uint64_t r2 = c.draw(0, S2 - 1);
+    uint2 e2 = ZG_LDG(&g.adj_e[ZG_LDG(&g.off[b + 1]) - (int64_t)q.w + (int64_t)r2]);
+    a2 = 1 + (e2.x == b);
+    res_mul(r, S2);
+    if (a2 == 2) r.shift++;
+    ok = !(b == a || b == e1.x) && !(e2.x == a || e2.x == e1.x);
+  }
+  r.hit = ok;
+  if (DBG && ok) {
+    double p = 1. / 3;
+    p = dmul(p, ddiv(1.0, u2d(g.m)));
+    p = dmul(p, ddiv(1.0 * a1, u2d(S1)));
+    p = dmul(p, ddiv(1.0 * a2, u2d(S2)));
+    r.w = ddiv(1.0, p);
+  }
+}
+
+// canonicality_check (applications/ChainMining.cpp:218-235, src/SamplerGenerator.cpp:368-385)
+__device__ __forceinline__ bool canonical(const uint32_t* es, const uint32_t* ed, const uint32_t* ei, int ne,
+                                          uint32_t s, uint32_t d, uint32_t id) {
+  if (ne <= 1) return true;
+  bool found = false;
+  for (int i = 0; i < ne; ++i) {
+    if (!found) {
+      if (s == es[i] || s == ed[i] || d == es[i] || d == ed[i]) found = true;
+    } else if (ei[i] >= id) {
+      return false;
+    }
+  }
+  return true;
+}
+
+// ---- ChainMining: applications/ChainMining.cpp:240-84 ------------------------------------
+template <bool DBG>
+__device__ void prog_chain(const ZgDevGraph& g, int order, Ctx& c, Res& r) {
+  if (g.m == 0) {
+    r.fail = true;
+    return;
+  }
+  uint64_t e0 = c.draw(0, g.m - 1);
+  res_mul(r, g.m);
+  uint4 q = ZG_LDG(&g.rec[e0]);
+  uint32_t es[ZG_MAX_LIST], ed[ZG_MAX_LIST], ei[ZG_MAX_LIST];
+  uint32_t vs[ZG_MAX_LIST];
+  int ne = 1, nvtx = 2;
+  es[0] = q.x;
+  ed[0] = q.y;
+  ei[0] = (uint32_t)e0;
+  vs[0] = q.x;
+  vs[1] = q.y;
+  uint32_t f[2] = {q.x, q.y};
+  int64_t fe[2], fl[2];
+  fe[0] = ZG_LDG(&g.off[q.x + 1]);
+  fe[1] = ZG_LDG(&g.off[q.y + 1]);
+  fl[0] = fe[0] - q.z;
+  fl[1] = fe[1] - q.w;
+  Ext p;
+  if (DBG) p = ext_from_double(ddiv(1.0, u2d(g.m)));
+  uint32_t mv = (uint32_t)e0 + 1;
+  for (int i = 0; i < order - 2; ++i) {
+    uint64_t l0 = (uint64_t)(fe[0] - fl[0]), l1 = (uint64_t)(fe[1] - fl[1]);
+    uint64_t S = l0 + l1;
+    if (S == 0) {
+      r.fail = true;
+      return;
+    }
+    uint64_t rr = c.draw(0, S - 1);
+    int side = 0;
+    if (rr >= l0) {
+      rr -= l0;
+      side = 1;
+    }
+    uint2 e = ZG_LDG(&g.adj_e[fl[side] + (int64_t)rr]);
+    uint32_t src = f[side];
+    uint32_t av = (f[0] == src) + (f[1] == src) + (f[0] == e.x) + (f[1] == e.x);
+    res_mul(r, S);
+    if (av == 2) r.shift++;
+    if (DBG) p = ext_mul(p, ext_from_double(ddiv(1.0 * av, u2d(S))));
+    if (!canonical(es, ed, ei, ne, src, e.x, e.y)) return;
+    es[ne] = src;
+    ed[ne] = e.x;
+    ei[ne] = e.y;
+    ++ne;
+    bool seen = false;
+    for (int k = 0; k < nvtx; ++k) seen |= (vs[k] == e.x);
+    if (!seen) vs[nvtx++] = e.x;
+    if (nvtx != i + 3) return;
+    // frontier update (ChainMining.cpp:265-80); here src is a frontier vertex and e.x is new
+    int upd = (f[0] == src) ? 0 : 1;
+    f[upd] = e.x;
+    uint4 qe = ZG_LDG(&g.rec[e.y]);
+    uint32_t sufe = (qe.x == e.x) ? qe.z : qe.w;
+    fe[upd] = ZG_LDG(&g.off[e.x + 1]);
+    int64_t pos = fe[upd] - (int64_t)sufe - 1;  // e's own slot in the new frontier's list
+    fl[upd] = lb_eid(g.adj_e, ZG_LDG(&g.off[e.x]), pos + 1, mv);
+  }
+  r.hit = true;
+  if (DBG) r.w = ext_to_double(ext_inv(p));
+}
+
+// ---- SamplerGenerator<Empty>::estimate: src/SamplerGenerator.cpp:461-546 ----------------
+__device__ __forceinline__ uint32_t pair_bit(uint32_t i, uint32_t j, uint32_t pv) {
+  if (i > j) {
+    uint32_t t = i;
+    i = j;
+    j = t;
+  }
+  return i * (2 * pv - i - 1) / 2 + (j - i - 1);
+}
+
+template <bool DBG>
+__device__ void prog_pattern(const ZgDevGraph& g, const ZgProgParams& pp, Ctx& c, Res& r) {
+  if (g.m == 0) {
+    r.fail = true;
+    return;
+  }
+  uint64_t e0 = c.draw(0, g.m - 1);
+  res_mul(r, g.m);
+  uint4 q = ZG_LDG(&g.rec[e0]);
+  const int MV = ZG_MAX_PATTERN_V + 1;
+  uint32_t vs[MV];
+  int64_t vl[MV], ve[MV];
+  uint32_t es[ZG_MAX_LIST], ed[ZG_MAX_LIST], ei[ZG_MAX_LIST];
+  int nvtx = 2, ne = 1;
+  vs[0] = q.x;
+  vs[1] = q.y;
+  ve[0] = ZG_LDG(&g.off[q.x + 1]);
+  ve[1] = ZG_LDG(&g.off[q.y + 1]);
+  vl[0] = ve[0] - q.z;
+  vl[1] = ve[1] - q.w;
+  es[0] = q.x;
+  ed[0] = q.y;
+  ei[0] = (uint32_t)e0;
+  uint32_t mv = (uint32_t)e0 + 1;
+  double p = 1.0;
+  if (DBG) p = dmul(p, ddiv(1.0, u2d(g.m)));
+  for (uint32_t k = 1; k < pp.pe; ++k) {
+    uint64_t S = 0;
+    for (int i = 0; i < nvtx; ++i) S += (uint64_t)(ve[i] - vl[i]);
+    if (S == 0) {
+      r.fail = true;
+      return;
+    }
+    uint64_t rr = c.draw(0, S - 1);
+    int side = 0;
+    for (; side < nvtx - 1; ++side) {
+      uint64_t len = (uint64_t)(ve[side] - vl[side]);
+      if (rr < len) break;
+      rr -= len;
+    }
+    uint2 e = ZG_LDG(&g.adj_e[vl[side] + (int64_t)rr]);
+    uint32_t src = vs[side];
+    int nbr_slot = -1;
+    for (int i = 0; i < nvtx; ++i)
+      if (vs[i] == e.x) nbr_slot = i;
+    uint32_t av = 1 + (nbr_slot >= 0);
+    res_mul(r, S);
+    if (av == 2) r.shift++;
+    if (DBG) p = dmul(p, ddiv(1.0 * av, u2d(S)));
+    if (!canonical(es, ed, ei, ne, src, e.x, e.y)) return;
+    es[ne] = src;
+    ed[ne] = e.x;
+    ei[ne] = e.y;
+    ++ne;
+    if (nbr_slot < 0) {
+      vs[nvtx] = e.x;
+      uint4 qe = ZG_LDG(&g.rec[e.y]);
+      uint32_t sufe = (qe.x == e.x) ? qe.z : qe.w;
+      ve[nvtx] = ZG_LDG(&g.off[e.x + 1]);
+      int64_t pos = ve[nvtx] - (int64_t)sufe - 1;
+      vl[nvtx] = lb_eid(g.adj_e, ZG_LDG(&g.off[e.x]), pos + 1, mv);
+      ++nvtx;
+      if ((uint32_t)nvtx > pp.pv) return;
+    }
+  }
+  if ((uint32_t)nvtx != pp.pv) return;
+  // relabel by ascending vertex id (SamplerGenerator.cpp:493-527) and test the edge set
+  uint32_t rank[MV];
+  for (int i = 0; i < nvtx; ++i) {
+    uint32_t rk = 0;
+    for (int j = 0; j < nvtx; ++j) rk += vs[j] < vs[i];
+    rank[i] = rk;
+  }
+  uint32_t mask = 0;
+  for (int k = 0; k < ne; ++k) {
+    uint32_t ri = 0, rj = 0;
+    for (int i = 0; i < nvtx; ++i) {
+      if (vs[i] == es[k]) ri = rank[i];
+      if (vs[i] == ed[k]) rj = rank[i];
+    }
+    mask |= 1u << pair_bit(ri, rj, pp.pv);
+  }
+  int lo = 0, hi = (int)pp.num_unique;
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (ZG_LDG(&pp.masks[mid]) < mask)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  bool ok = lo < (int)pp.num_unique && ZG_LDG(&pp.masks[lo]) == mask;
+  r.hit = ok;
+  if (DBG && ok) r.w = ddiv(1.0, p);
+}
+
+// ---- per-thread exact accumulation and block reduction ----------------------------------
+struct Acc {
+  unsigned long long samples, hits, fails, ovf;
+  uint64_t s[4];
+  double sw, sw2;
+};
+
+__device__ __forceinline__ void acc_init(Acc& a) {
+  a.samples = a.hits = a.fails = a.ovf = 0;
+  a.s[0] = a.s[1] = a.s[2] = a.s[3] = 0;
+  a.sw = a.sw2 = 0.0;
+}
+
+__device__ __forceinline__ double u192_to_double(const ZgU192& n) {
+  // exact enough for the variance sum: top two non-zero limbs
+  if (n.l[2]) return fma(u2d(n.l[2]), 0x1p128, u2d(n.l[1]) * 0x1p64);
+  return fma(u2d(n.l[1]), 0x1p64, u2d(n.l[0]));
+}
+
+__device__ __forceinline__ void acc_add(Acc& a, const Res& r, uint32_t den) {
+  a.samples++;
+  a.fails += r.fail;
+  if (!r.hit) return;
+  a.hits++;
+  a.ovf += r.ovf;
+  uint32_t sh = den - r.shift;  // < 64
+  uint64_t v0 = r.num.l[0] << sh;
+  uint64_t v1 = sh ? (r.num.l[1] << sh) | (r.num.l[0] >> (64 - sh)) : r.num.l[1];
+  uint64_t v2 = sh ? (r.num.l[2] << sh) | (r.num.l[1] >> (64 - sh)) : r.num.l[2];
+  uint64_t v3 = sh ? (r.num.l[2] >> (64 - sh)) : 0;
+  asm("add.cc.u64 %0, %0, %4;\n\t"
+      "addc.cc.u64 %1, %1, %5;\n\t"
+      "addc.cc.u64 %2, %2, %6;\n\t"
+      "addc.u64 %3, %3, %7;"
+      : "+l"(a.s[0]), "+l"(a.s[1]), "+l"(a.s[2]), "+l"(a.s[3])
+      : "l"(v0), "l"(v1), "l"(v2), "l"(v3));
+  double w = ldexp(u192_to_double(r.num), -(int)r.shift);
+  a.sw += w;
+  a.sw2 = fma(w, w, a.sw2);
+}
+
+template <int BLOCK>
+__device__ void block_reduce_store(Acc& a, ZgPartial* out) {
+  unsigned long long v[14];
+  v[0] = a.samples;
+  v[1] = a.hits;
+  v[2] = a.fails;
+  v[3] = a.ovf;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    v[4 + 2 * i] = (uint32_t)a.s[i];
+    v[5 + 2 * i] = a.s[i] >> 32;
+  }
+  double d0 = a.sw, d1 = a.sw2;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+    for (int i = 0; i < 12; ++i) v[i] += __shfl_xor_sync(0xffffffffu, v[i], o);
+    d0 += __shfl_xor_sync(0xffffffffu, d0, o);
+    d1 += __shfl_xor_sync(0xffffffffu, d1, o);
+  }
+  __shared__ unsigned long long sv[BLOCK / 32][12];
+  __shared__ double sd[BLOCK / 32][2];
+  int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) {
+#pragma unroll
+    for (int i = 0; i < 12; ++i) sv[warp][i] = v[i];
+    sd[warp][0] = d0;
+    sd[warp][1] = d1;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    ZgPartial p;
+    unsigned long long t[12] = {0};
+    double s0 = 0, s1 = 0;
+    for (int w = 0; w < BLOCK / 32; ++w) {
+      for (int i = 0; i < 12; ++i) t[i] += sv[w][i];
+      s0 += sd[w][0];
+      s1 += sd[w][1];
+    }
+    p.samples = t[0];
+    p.hits = t[1];
+    p.fails = t[2];
+    p.overflow = t[3];
+    for (int i = 0; i < 8; ++i) p.lane[i] = t[4 + i];
+    p.sum_w = s0;
+    p.sum_w2 = s1;
+    *out = p;
+  }
+}
+
+constexpr int kBlock = 256;
+
+template <bool DBG>
+__device__ __forceinline__ void run_program(const ZgDevGraph& g, const ZgProgParams& pp, Ctx& c, Res& r) {
+  switch (pp.kind) {
+    case ZG_PROG_TRIANGLE: prog_triangle<DBG>(g, c, r); break;
+    case ZG_PROG_FOUR_CLIQUE: prog_four_clique<DBG>(g, c, r); break;
+    case ZG_PROG_THREE_CHAIN: prog_three_chain<DBG>(g, c, r); break;
+    case ZG_PROG_FOUR_CHAIN: prog_four_chain<DBG>(g, c, r); break;
+    case ZG_PROG_CHAIN: prog_chain<DBG>(g, (int)pp.param, c, r); break;
+    default: prog_pattern<DBG>(g, pp, c, r); break;
+  }
+}
+
+// Production kernels: one specialisation per program so each has its own register budget.
+template <int KIND>
+__global__ void __launch_bounds__(kBlock) k_sample(ZgDevGraph g, ZgProgParams pp, uint64_t n, uint64_t first,
+                                                   uint64_t seed, uint32_t stream, ZgPartial* __restrict__ partials) {
+  Acc a;
+  acc_init(a);
+  uint64_t stride = (uint64_t)gridDim.x * kBlock;
+  for (uint64_t i = blockIdx.x * (uint64_t)kBlock + threadIdx.x; i < n; i += stride) {
+    Ctx c{seed, first + i, stream, 0, nullptr};
+    Res r;
+    res_init(r);
+    if (KIND == ZG_PROG_TRIANGLE) prog_triangle<false>(g, c, r);
+    else if (KIND == ZG_PROG_FOUR_CLIQUE) prog_four_clique<false>(g, c, r);
+    else if (KIND == ZG_PROG_THREE_CHAIN) prog_three_chain<false>(g, c, r);
+    else if (KIND == ZG_PROG_FOUR_CHAIN) prog_four_chain<false>(g, c, r);
+    else if (KIND == ZG_PROG_CHAIN) prog_chain<false>(g, (int)pp.param, c, r);
+    else prog_pattern<false>(g, pp, c, r);
+    acc_add(a, r, pp.den_log2);
+  }
+  block_reduce_store<kBlock>(a, &partials[blockIdx.x]);
+}
+
+__global__ void __launch_bounds__(kBlock) k_sample_debug(ZgDevGraph g, ZgProgParams pp, uint64_t n, uint64_t first,
+                                                         uint64_t seed, uint32_t stream, ZgPartial* __restrict__ partials,
+                                                         zg_sample_trace* __restrict__ traces) {
+  Acc a;
+  acc_init(a);
+  uint64_t stride = (uint64_t)gridDim.x * kBlock;
+  for (uint64_t i = blockIdx.x * (uint64_t)kBlock + threadIdx.x; i < n; i += stride) {
+    zg_sample_trace* t = &traces[i];
+    Ctx c{seed, first + i, stream, 0, t};
+    Res r;
+    res_init(r);
+    run_program<true>(g, pp, c, r);
+    acc_add(a, r, pp.den_log2);
+    t->ndraws = c.nd;
+    t->hit = r.hit;
+    t->fail = r.fail;
+    t->shift = r.hit ? r.shift : 0;
+    t->w = r.hit ? r.w : 0.0;
+    t->num[0] = r.hit ? r.num.l[0] : 0;
+    t->num[1] = r.hit ? r.num.l[1] : 0;
+    t->num[2] = r.hit ? (r.ovf ? ~0ull : r.num.l[2]) : 0;
+  }
+  block_reduce_store<kBlock>(a, &partials[blockIdx.x]);
+}
+
+// ---- ThreeMotif: applications/ThreeMotif.cpp:48-121 with the sub-pattern cache ---------
+template <bool DBG>
+__global__ void __launch_bounds__(kBlock) k_three_motif(ZgDevGraph g, uint64_t n_chain, uint64_t n_tri, uint64_t seed,
+                                                        uint32_t stream_chain, uint32_t stream_tri,
+                                                        ZgPartial* __restrict__ pc, ZgPartial* __restrict__ pt,
+                                                        zg_sample_trace* __restrict__ tc,
+                                                        zg_sample_trace* __restrict__ tt) {
+  Acc ac, at;
+  acc_init(ac);
+  acc_init(at);
+  uint64_t n = n_chain > n_tri ? n_chain : n_tri;
+  uint64_t stride = (uint64_t)gridDim.x * kBlock;
+  for (uint64_t i = blockIdx.x * (uint64_t)kBlock + threadIdx.x; i < n; i += stride) {
+    if (i < n_chain) {
+      // ThreeChainCountingInstance: keep the wedge; the triangle instance closes it (:54-62)
+      Ctx c{seed, i, stream_chain, 0, DBG ? &tc[i] : nullptr};
+      Res r;
+      res_init(r);
+      Res rt;
+      res_init(rt);
+      if (g.m == 0) {
+        r.fail = true;
+      } else {
+        uint64_t e0 = c.draw(0, g.m - 1);
+        uint4 q = ZG_LDG(&g.rec[e0]);
+        uint64_t S = (uint64_t)q.z + q.w;
+        if (S == 0) {
+          r.fail = true;
+        } else {
+          uint64_t r1 = c.draw(0, S - 1);
+          uint32_t anchor = q.x, other = q.y, suf = q.z;
+          if (r1 >= q.z) {
+            r1 -= q.z;
+            anchor = q.y;
+            other = q.x;
+            suf = q.w;
+          }
+          res_mul(r, g.m);
+          res_mul(r, S);
+          r.hit = true;
+          if (i < n_tri) {
+            int64_t bo = ZG_LDG(&g.off[other]), eo = ZG_LDG(&g.off[other + 1]);
+            uint2 e1 = ZG_LDG(&g.adj_e[ZG_LDG(&g.off[anchor + 1]) - (int64_t)suf + (int64_t)r1]);
+            uint32_t a1 = 1 + (e1.x == q.x || e1.x == q.y);
+            if (a1 == 2) r.shift = 1;
+            int64_t bc = ZG_LDG(&g.off[e1.x]), ec = ZG_LDG(&g.off[e1.x + 1]);
+            rt.hit = a1 == 1 && edge_after(bo, eo, bc, ec, other, e1.x, e1.y + 1, g.adj_n);
+            rt.num = r.num;
+            rt.shift = r.shift;
+          }
+          if (DBG) {
+            double p = 1.0;
+            p = dmul(p, ddiv(1.0, u2d(g.m)));
+            p = dmul(p, ddiv(1.0, u2d(S)));
+            r.w = ddiv(1.0, p);
+            rt.w = rt.hit ? r.w : 0.0;
+          }
+        }
+      }
+      acc_add(ac, r, 1);
+      if (DBG) {
+        zg_sample_trace* t = &tc[i];
+        t->ndraws = c.nd;
+        t->hit = r.hit;
+        t->fail = r.fail;
+        t->shift = r.hit ? r.shift : 0;
+        t->w = r.hit ? r.w : 0.0;
+        t->num[0] = r.hit ? r.num.l[0] : 0;
+        t->num[1] = r.hit ? r.num.l[1] : 0;
+        t->num[2] = r.hit ? r.num.l[2] : 0;
+      }
+      if (i < n_tri) {
+        acc_add(at, rt, 1);
+        if (DBG) {
+          zg_sample_trace* t = &tt[i];
+          t->ndraws = 0;
+          t->hit = rt.hit;
+          t->fail = 0;
+          t->shift = rt.hit ? rt.shift : 0;
+          t->w = rt.w;
+          t->num[0] = rt.hit ? rt.num.l[0] : 0;
+          t->num[1] = rt.hit ? rt.num.l[1] : 0;
+          t->num[2] = rt.hit ? rt.num.l[2] : 0;
+        }
+      }
+    } else {
+      Ctx c{seed, i, stream_tri, 0, DBG ? &tt[i] : nullptr};
+      Res r;
+      res_init(r);
+      prog_triangle<DBG>(g, c, r);
+      acc_add(at, r, 1);
+      if (DBG) {
+        zg_sample_trace* t = &tt[i];
+        t->ndraws = c.nd;
+        t->hit = r.hit;
+        t->fail = r.fail;
+        t->shift = r.hit ? r.shift : 0;
+        t->w = r.hit ? r.w : 0.0;
+        t->num[0] = r.hit ? r.num.l[0] : 0;
+        t->num[1] = r.hit ? r.num.l[1] : 0;
+        t->num[2] = r.hit ? r.num.l[2] : 0;
+      }
+    }
+  }
+  block_reduce_store<kBlock>(ac, &pc[blockIdx.x]);
+  __syncthreads();
+  block_reduce_store<kBlock>(at, &pt[blockIdx.x]);
+}
+
+// Single-block reduction of the per-block partials, fixed order.
+__global__ void __launch_bounds__(kBlock) k_finalize(const ZgPartial* __restrict__ parts, int nparts,
+                                                     ZgPartial* __restrict__ out) {
+  Acc dummy;
+  (void)dummy;
+  unsigned long long v[12] = {0};
+  double d0 = 0, d1 = 0;
+  for (int b = threadIdx.x; b < nparts; b += kBlock) {
+    const ZgPartial& p = parts[b];
+    v[0] += p.samples;
+    v[1] += p.hits;
+    v[2] += p.fails;
+    v[3] += p.overflow;
+    for (int i = 0; i < 8; ++i) v[4 + i] += p.lane[i];
+    d0 += p.sum_w;
+    d1 += p.sum_w2;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+    for (int i = 0; i < 12; ++i) v[i] += __shfl_xor_sync(0xffffffffu, v[i], o);
+    d0 += __shfl_xor_sync(0xffffffffu, d0, o);
+    d1 += __shfl_xor_sync(0xffffffffu, d1, o);
+  }
+  __shared__ unsigned long long sv[kBlock / 32][12];
+  __shared__ double sd[kBlock / 32][2];
+  int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) {
+    for (int i = 0; i < 12; ++i) sv[warp][i] = v[i];
+    sd[warp][0] = d0;
+    sd[warp][1] = d1;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long t[12] = {0};
+    double s0 = 0, s1 = 0;
+    for (int w = 0; w < kBlock / 32; ++w) {
+      for (int i = 0; i < 12; ++i) t[i] += sv[w][i];
+      s0 += sd[w][0];
+      s1 += sd[w][1];
+    }
+    ZgPartial p;
+    p.samples = t[0];
+    p.hits = t[1];
+    p.fails = t[2];
+    p.overflow = t[3];
+    for (int i = 0; i < 8; ++i) p.lane[i] = t[4 + i];
+    p.sum_w = s0;
+    p.sum_w2 = s1;
+    *out = p;
+  }
+}
+
+// ---- host side ------------------------------------------------------------------------
+typedef unsigned __int128 u128;
+
+// 320-bit value -> correctly rounded double of value / 2^den / n.
+double exact_mean(const uint64_t s[5], uint32_t den, uint64_t n) {
+  if (n == 0) return 0.0;
+  uint64_t q[5];
+  u128 rem = 0;
+  for (int i = 4; i >= 0; --i) {
+    u128 cur = (rem << 64) | s[i];
+    q[i] = (uint64_t)(cur / n);
+    rem = cur % n;
+  }
+  int top = -1;
+  for (int i = 4; i >= 0 && top < 0; --i)
+    if (q[i]) top = i * 64 + 63 - __builtin_clzll(q[i]);
+  if (top < 0) {
+    // quotient < 1: scale the remainder fraction
+    return rem ? ldexp((double)rem / (double)n, -(int)den) : 0.0;
+  }
+  // take 64 bits from the top, sticky from everything below and the remainder
+  auto bit = [&](int k) -> uint64_t { return k < 0 ? 0 : (q[k / 64] >> (k % 64)) & 1ull; };
+  uint64_t mant = 0;
+  for (int k = top; k > top - 64; --k) mant = (mant << 1) | bit(k);
+  bool sticky = rem != 0;
+  for (int k = top - 64; k >= 0 && !sticky; --k) sticky = bit(k);
+  // round 64 -> 53 bits
+  uint64_t keep = mant >> 11, low = mant & 0x7ff;
+  int e = top - 63 + 11;
+  if (low > 0x400 || (low == 0x400 && (sticky || (keep & 1)))) {
+    keep++;
+    if (keep == (1ull << 53)) {
+      keep >>= 1;
+      e++;
+    }
+  }
+  return ldexp((double)keep, e - (int)den);
+}
+
+void partial_to_counters(const ZgPartial& p, uint32_t den, zg_counters* out) {
+  memset(out, 0, sizeof(*out));
+  out->samples = p.samples;
+  out->hits = p.hits;
+  out->fails = p.fails;
+  out->overflow = p.overflow ? 1 : 0;
+  out->den_log2 = den;
+  u128 carry = 0;
+  for (int i = 0; i < 5; ++i) {
+    u128 acc = carry;
+    // lanes are 32-bit digits: digit k has weight 2^(32k); limb i = digits 2i, 2i+1
+    if (2 * i < 8) acc += (u128)p.lane[2 * i];
+    if (2 * i + 1 < 8) acc += (u128)p.lane[2 * i + 1] << 32;
+    out->sum_num[i] = (uint64_t)acc;
+    carry = acc >> 64;
+  }
+  out->sum_w = p.sum_w;
+  out->sum_w2 = p.sum_w2;
+  out->estimate = exact_mean(out->sum_num, den, p.samples);
+}
+
+uint32_t den_for(const zg_program* p) {
+  switch (p->kind) {
+    case ZG_PROG_TRIANGLE: return 1;
+    case ZG_PROG_FOUR_CLIQUE: return 2;
+    case ZG_PROG_THREE_CHAIN: return 1;
+    case ZG_PROG_FOUR_CHAIN: return 2;
+    case ZG_PROG_CHAIN: return p->param - 2;
+    default: return p->pe - 1;
+  }
+}
+
+ZgProgParams params_for(const zg_program* p) {
+  ZgProgParams pp;
+  pp.kind = p->kind;
+  pp.param = p->param;
+  pp.pv = p->pv;
+  pp.pe = p->pe;
+  pp.num_unique = p->num_unique;
+  pp.masks = p->d_masks;
+  pp.den_log2 = den_for(p);
+  return pp;
+}
+
+template <typename K>
+int grid_of(K kernel) {
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kBlock, 0);
+  if (per_sm < 1) per_sm = 1;
+  return per_sm * zg_num_sms();
+}
+
+int grid_for_kind(int kind) {
+  static int cache[8] = {0};
+  static std::mutex mu;
+  std::lock_guard<std::mutex> lk(mu);
+  if (kind < 0 || kind >= 8) kind = ZG_PROG_PATTERN;
+  if (!cache[kind]) {
+    switch (kind) {
+      case ZG_PROG_TRIANGLE: cache[kind] = grid_of(k_sample<ZG_PROG_TRIANGLE>); break;
+      case ZG_PROG_FOUR_CLIQUE: cache[kind] = grid_of(k_sample<ZG_PROG_FOUR_CLIQUE>); break;
+      case ZG_PROG_THREE_CHAIN: cache[kind] = grid_of(k_sample<ZG_PROG_THREE_CHAIN>); break;
+      case ZG_PROG_FOUR_CHAIN: cache[kind] = grid_of(k_sample<ZG_PROG_FOUR_CHAIN>); break;
+      case ZG_PROG_CHAIN: cache[kind] = grid_of(k_sample<ZG_PROG_CHAIN>); break;
+      default: cache[kind] = grid_of(k_sample<ZG_PROG_PATTERN>); break;
+    }
+  }
+  return cache[kind];
+}
+
+int validate_run(const zg_graph* g, const zg_program* p) {
+  if (!g || !p) return zg_set_error(ZG_ERR_INVALID_ARG, "null graph or program"), ZG_ERR_INVALID_ARG;
+  return ZG_OK;
+}
+
+int launch_sample(const zg_graph* g, const zg_program* p, uint64_t n, uint64_t first, uint64_t seed,
+                  uint32_t stream_id, cudaStream_t s, ZgPartial* parts, int grid) {
+  ZgProgParams pp = params_for(p);
+  switch (p->kind) {
+    case ZG_PROG_TRIANGLE:
+      k_sample<ZG_PROG_TRIANGLE><<<grid, kBlock, 0, s>>>(g->d, pp, n, first, seed, stream_id, parts);
+      break;
+    case ZG_PROG_FOUR_CLIQUE:
+      k_sample<ZG_PROG_FOUR_CLIQUE><<<grid, kBlock, 0, s>>>(g->d, pp, n, first, seed, stream_id, parts);
+      break;
+    case ZG_PROG_THREE_CHAIN:
+      k_sample<ZG_PROG_THREE_CHAIN><<<grid, kBlock, 0, s>>>(g->d, pp, n, first, seed, stream_id, parts);
+      break;
+    case ZG_PROG_FOUR_CHAIN:
+      k_sample<ZG_PROG_FOUR_CHAIN><<<grid, kBlock, 0, s>>>(g->d, pp, n, first, seed, stream_id, parts);
+      break;
+    case ZG_PROG_CHAIN:
+      k_sample<ZG_PROG_CHAIN><<<grid, kBlock, 0, s>>>(g->d, pp, n, first, seed, stream_id, parts);
+      break;
+    default:
+      k_sample<ZG_PROG_PATTERN><<<grid, kBlock, 0, s>>>(g->d, pp, n, first, seed, stream_id, parts);
+      break;
+  }
+  return ZG_OK;
+}
+
+}  // namespace
+
+// Shared by the allocation-free entry points of other translation units.
+int zg_sample_grid(int kind) { return grid_for_kind(kind); }
+
+extern "C" int zg_run(const zg_graph* g, const zg_program* p, uint64_t n, uint64_t first_sample, uint64_t seed,
+                      uint32_t stream_id, void* cuda_stream, zg_counters* out) {
+  int rc = validate_run(g, p);
+  if (rc) return rc;
+  if (!out) return zg_set_error(ZG_ERR_INVALID_ARG, "null output"), ZG_ERR_INVALID_ARG;
+  cudaStream_t s = (cudaStream_t)cuda_stream;
+  uint64_t maxg = (n + kBlock - 1) / kBlock;
+  int grid = grid_for_kind(p->kind);
+  if ((uint64_t)grid > maxg) grid = (int)(maxg ? maxg : 1);
+  ZgPartial* parts = nullptr;
+  ZG_CUDA(cudaMallocAsync((void**)&parts, sizeof(ZgPartial) * (grid + 1), s));
+  launch_sample(g, p, n, first_sample, seed, stream_id, s, parts, grid);
+  k_finalize<<<1, kBlock, 0, s>>>(parts, grid, parts + grid);
+  ZgPartial h;
+  cudaError_t ce = cudaMemcpyAsync(&h, parts + grid, sizeof(h), cudaMemcpyDeviceToHost, s);
+  cudaFreeAsync(parts, s);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
+  if (ce == cudaSuccess) ce = cudaGetLastError();
+  if (ce != cudaSuccess) return zg_check_cuda(ce, "zg_run");
+  partial_to_counters(h, den_for(p), out);
+  return ZG_OK;
+}
+
+extern "C" int zg_run_debug(const zg_graph* g, const zg_program* p, uint64_t n, uint64_t first_sample,
+                            uint64_t seed, uint32_t stream_id, zg_sample_trace* traces) {
+  int rc = validate_run(g, p);
+  if (rc) return rc;
+  if (!traces && n) return zg_set_error(ZG_ERR_INVALID_ARG, "null traces"), ZG_ERR_INVALID_ARG;
+  if (n > (1ull << 22)) return zg_set_error(ZG_ERR_TOO_LARGE, "debug runs take at most 2^22 samples"), ZG_ERR_TOO_LARGE;
+  int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>((n + kBlock - 1) / kBlock, 4096));
+  ZgPartial* parts = nullptr;
+  zg_sample_trace* dt = nullptr;
+  ZG_CUDA(cudaMalloc((void**)&parts, sizeof(ZgPartial) * (grid + 1)));
+  cudaError_t ce = cudaMalloc((void**)&dt, sizeof(zg_sample_trace) * (n ? n : 1));
+  if (ce != cudaSuccess) {
+    cudaFree(parts);
+    return zg_check_cuda(ce, "debug traces");
+  }
+  ce = cudaMemset(dt, 0, sizeof(zg_sample_trace) * (n ? n : 1));
+  ZgProgParams pp = params_for(p);
+  k_sample_debug<<<grid, kBlock>>>(g->d, pp, n, first_sample, seed, stream_id, parts, dt);
+  if (ce == cudaSuccess) ce = cudaDeviceSynchronize();
+  if (ce == cudaSuccess) ce = cudaGetLastError();
+  if (ce == cudaSuccess && n) ce = cudaMemcpy(traces, dt, sizeof(zg_sample_trace) * n, cudaMemcpyDeviceToHost);
+  cudaFree(parts);
+  cudaFree(dt);
+  if (ce != cudaSuccess) return zg_check_cuda(ce, "zg_run_debug");
+  return ZG_OK;
+}
+
+static int run_motif(const zg_graph* g, uint64_t n_chain, uint64_t n_tri, uint64_t seed, uint32_t sc, uint32_t st,
+                     cudaStream_t s, zg_counters* oc, zg_counters* ot, zg_sample_trace* tc, zg_sample_trace* tt) {
+  if (!g) return zg_set_error(ZG_ERR_INVALID_ARG, "null graph"), ZG_ERR_INVALID_ARG;
+  bool dbg = tc || tt;
+  uint64_t n = std::max(n_chain, n_tri);
+  if (dbg && n > (1ull << 22)) return zg_set_error(ZG_ERR_TOO_LARGE, "debug runs take at most 2^22 samples"), ZG_ERR_TOO_LARGE;
+  if (dbg && (!tc || !tt)) return zg_set_error(ZG_ERR_INVALID_ARG, "both trace arrays are required"), ZG_ERR_INVALID_ARG;
+  int grid = dbg ? (int)std::max<uint64_t>(1, std::min<uint64_t>((n + kBlock - 1) / kBlock, 4096))
+                 : std::min<int>(grid_of(k_three_motif<false>), (int)std::max<uint64_t>(1, (n + kBlock - 1) / kBlock));
+  ZgPartial* parts = nullptr;
+  zg_sample_trace *dtc = nullptr, *dtt = nullptr;
+  ZG_CUDA(cudaMallocAsync((void**)&parts, sizeof(ZgPartial) * (2 * grid + 2), s));
+  cudaError_t ce = cudaSuccess;
+  if (dbg) {
+    ce = cudaMallocAsync((void**)&dtc, sizeof(zg_sample_trace) * (n_chain ? n_chain : 1), s);
+    if (ce == cudaSuccess) ce = cudaMallocAsync((void**)&dtt, sizeof(zg_sample_trace) * (n_tri ? n_tri : 1), s);
+    if (ce == cudaSuccess) ce = cudaMemsetAsync(dtc, 0, sizeof(zg_sample_trace) * (n_chain ? n_chain : 1), s);
+    if (ce == cudaSuccess) ce = cudaMemsetAsync(dtt, 0, sizeof(zg_sample_trace) * (n_tri ? n_tri : 1), s);
+  }
+  if (ce == cudaSuccess) {
+    if (dbg)
+      k_three_motif<true><<<grid, kBlock, 0, s>>>(g->d, n_chain, n_tri, seed, sc, st, parts, parts + grid, dtc, dtt);
+    else
+      k_three_motif<false><<<grid, kBlock, 0, s>>>(g->d, n_chain, n_tri, seed, sc, st, parts, parts + grid, nullptr,
+                                                   nullptr);
+    k_finalize<<<1, kBlock, 0, s>>>(parts, grid, parts + 2 * grid);
+    k_finalize<<<1, kBlock, 0, s>>>(parts + grid, grid, parts + 2 * grid + 1);
+  }
+  ZgPartial h[2];
+  if (ce == cudaSuccess) ce = cudaMemcpyAsync(h, parts + 2 * grid, sizeof(h), cudaMemcpyDeviceToHost, s);
+  if (ce == cudaSuccess && dbg && n_chain)
+    ce = cudaMemcpyAsync(tc, dtc, sizeof(zg_sample_trace) * n_chain, cudaMemcpyDeviceToHost, s);
+  if (ce == cudaSuccess && dbg && n_tri)
+    ce = cudaMemcpyAsync(tt, dtt, sizeof(zg_sample_trace) * n_tri, cudaMemcpyDeviceToHost, s);
+  cudaFreeAsync(parts, s);
+  if (dtc) cudaFreeAsync(dtc, s);
+  if (dtt) cudaFreeAsync(dtt, s);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
+  if (ce == cudaSuccess) ce = cudaGetLastError();
+  if (ce != cudaSuccess) return zg_check_cuda(ce, "three motif");
+  if (oc) partial_to_counters(h[0], 1, oc);
+  if (ot) partial_to_counters(h[1], 1, ot);
+  return ZG_OK;
+}
+
+extern "C" int zg_run_three_motif(const zg_graph* g, uint64_t n_chain, uint64_t n_tri, uint64_t seed,
+                                  uint32_t stream_chain, uint32_t stream_tri, void* cuda_stream, zg_counters* out_chain,
+                                  zg_counters* out_tri) {
+  return run_motif(g, n_chain, n_tri, seed, stream_chain, stream_tri, (cudaStream_t)cuda_stream, out_chain, out_tri,
+                   nullptr, nullptr);
+}
+
+extern "C" int zg_run_three_motif_debug(const zg_graph* g, uint64_t n_chain, uint64_t n_tri, uint64_t seed,
+                                        uint32_t stream_chain, uint32_t stream_tri, zg_sample_trace* chain_traces,
+                                        zg_sample_trace* tri_traces) {
+  zg_counters a, b;
+  return run_motif(g, n_chain, n_tri, seed, stream_chain, stream_tri, nullptr, &a, &b, chain_traces, tri_traces);
+}

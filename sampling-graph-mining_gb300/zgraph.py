@@ -1,0 +1,527 @@
+"""Python binding of libzgraph_gpu.so (ctypes over include/zgraph_gpu.h) and a host-side mirror of
+the reference's estimator interface (jy-yuan/sampling-graph-mining):
+
+  Graph                     Graph<E> + DistGraphLoader/CSRConstructor (include/Graph.hpp:148-246)
+  Estimation                include/ZGraphInstance.hpp:18-28, src/ZGraphInstance.cpp:15-35
+  ZGraphInstance.calculate  src/ZGraphInstance.cpp:257-297
+  TriangleCountingInstance, FourCliqueCountingInstance, ThreeChainCountingInstance,
+  FourChainCountingInstance, ChainMiningInstance       applications/<App>.cpp estimate() bodies
+  Pattern, SamplerGenerator                            include/SamplerGenerator.hpp:9-80
+  AllPredicateZGraphInstance                           include/ZGraphInstance.hpp:143-157
+  ThreeMotif (ZGraphInstanceWithCache pair)            applications/ThreeMotif.cpp:149-196
+
+Every estimate runs on the GPU through the C ABI; there is no CPU path.  Loading fails loudly
+when the library has not been built.
+"""
+import ctypes as C
+import os
+import threading
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libzgraph_gpu.so")
+
+ZG_OK = 0
+ERRORS = {1: "INVALID_ARG", 2: "OOM", 3: "CUDA", 4: "INVALID_GRAPH", 5: "UNSUPPORTED_ESTIMATOR",
+          6: "TIMEOUT", 7: "BOUND_NOT_MET", 8: "NO_DEVICE", 9: "OVERFLOW", 10: "TOO_LARGE"}
+
+PROG_TRIANGLE, PROG_FOUR_CLIQUE, PROG_THREE_CHAIN, PROG_FOUR_CHAIN, PROG_CHAIN, PROG_PATTERN = 1, 2, 3, 4, 5, 6
+EXACT_TRIANGLE, EXACT_WEDGE, EXACT_THREE_PATH, EXACT_FIVE_STAR, EXACT_FOUR_CLIQUE = 1, 2, 3, 4, 5
+PRED_GE, PRED_LT, PRED_GT, PRED_LE, PRED_EQ, PRED_NE, PRED_RANGE = 1, 2, 3, 4, 5, 6, 7
+NO_SHUFFLE = 0xFFFFFFFFFFFFFFFF
+MAX_DRAWS = 16
+
+
+class ZgError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s (%d): %s" % (ERRORS.get(code, "?"), code, msg))
+        self.code = code
+
+
+class GraphMeta(C.Structure):
+    _fields_ = [("num_vertices", C.c_uint32), ("weighted", C.c_uint32), ("num_local_edges", C.c_uint64),
+                ("num_edges", C.c_uint64), ("max_degree", C.c_uint64), ("device_bytes", C.c_uint64)]
+
+
+class Counters(C.Structure):
+    _fields_ = [("samples", C.c_uint64), ("hits", C.c_uint64), ("fails", C.c_uint64),
+                ("den_log2", C.c_uint32), ("overflow", C.c_uint32), ("sum_num", C.c_uint64 * 5),
+                ("sum_w", C.c_double), ("sum_w2", C.c_double), ("estimate", C.c_double),
+                ("reserved", C.c_double)]
+
+    def exact_sum(self):
+        """Exact sum of 1/p over the samples as a Python Fraction."""
+        from fractions import Fraction
+        v = 0
+        for i in range(5):
+            v |= int(self.sum_num[i]) << (64 * i)
+        return Fraction(v, 1 << self.den_log2)
+
+    def as_dict(self):
+        return {"samples": self.samples, "hits": self.hits, "fails": self.fails,
+                "den_log2": self.den_log2, "overflow": self.overflow,
+                "sum_num": [int(x) for x in self.sum_num], "sum_w": self.sum_w,
+                "sum_w2": self.sum_w2, "estimate": self.estimate}
+
+
+TRACE_DTYPE = np.dtype([("ndraws", "<u4"), ("hit", "<u4"), ("fail", "<u4"), ("shift", "<u4"),
+                        ("w", "<f8"), ("num", "<u8", (3,)), ("lo", "<u8", (MAX_DRAWS,)),
+                        ("hi", "<u8", (MAX_DRAWS,)), ("val", "<u8", (MAX_DRAWS,))])
+
+_lib = None
+_lock = threading.Lock()
+
+
+def lib():
+    """Loads libzgraph_gpu.so (raises if it is missing: no fallback exists)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("libzgraph_gpu.so is not built (%s); run __graft_entry__.build()" % LIB_PATH)
+        L = C.CDLL(LIB_PATH)
+        P, U32, U64, I64, I32, D = C.c_void_p, C.c_uint32, C.c_uint64, C.c_int64, C.c_int, C.c_double
+        sig = {
+            "zg_version": ([], I32), "zg_init": ([I32], I32), "zg_last_error": ([], C.c_char_p),
+            "zg_graph_create": ([P, U64, U32, P, P, C.POINTER(P)], I32),
+            "zg_graph_permuted": ([P, U64, U32, P, U64, P, P, C.POINTER(P)], I32),
+            "zg_graph_free": ([P], I32),
+            "zg_graph_get_meta": ([P, C.POINTER(GraphMeta)], I32),
+            "zg_graph_set_meta": ([P, U64, U64], I32),
+            "zg_graph_download": ([P, P, P, P, P, P, P], I32),
+            "zg_graph_filter": ([P, I32, I64, I64, U64, P, P, C.POINTER(U64), C.POINTER(P)], I32),
+            "zg_graph_subsample": ([P, D, U64, U64, P, P, C.POINTER(U64), C.POINTER(P)], I32),
+            "zg_program_create": ([I32, U32, C.POINTER(P)], I32),
+            "zg_program_create_pattern": ([U32, U32, P, C.POINTER(P)], I32),
+            "zg_program_free": ([P], I32),
+            "zg_program_info": ([P, C.POINTER(U32), C.POINTER(U32), C.POINTER(U32)], I32),
+            "zg_run": ([P, P, U64, U64, U64, U32, P, C.POINTER(Counters)], I32),
+            "zg_run_debug": ([P, P, U64, U64, U64, U32, P], I32),
+            "zg_run_three_motif": ([P, U64, U64, U64, U32, U32, P, C.POINTER(Counters), C.POINTER(Counters)], I32),
+            "zg_run_three_motif_debug": ([P, U64, U64, U64, U32, U32, P, P], I32),
+            "zg_exact_count": ([P, I32, P, P], I32),
+            "zg_gen_rmat": ([U32, U32, D, D, D, U64, U64, P, C.POINTER(U64)], I32),
+            "zg_gen_chung_lu": ([U32, D, D, U64, U64, P, C.POINTER(U64)], I32),
+            "zg_gen_weights": ([U64, U32, U64, P], I32),
+        }
+        for name, (args, res) in sig.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = res
+        _lib = L
+        return _lib
+
+
+def check(rc):
+    if rc != ZG_OK:
+        raise ZgError(rc, lib().zg_last_error().decode(errors="replace"))
+
+
+_init_done = set()
+
+
+def init(device=0):
+    """zg_init: select and check the sm_103 device (NetworkInterface/SharedMemSys set-up)."""
+    if device not in _init_done:
+        check(lib().zg_init(device))
+        _init_done.add(device)
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+# ---- synthetic inputs ---------------------------------------------------------------------
+def gen_rmat(scale, edge_factor, a=0.57, b=0.19, c=0.19, seed=1):
+    """Undirected simplified R-MAT edge list, (m, 2) uint32 in a seeded random order."""
+    L = lib()
+    m = C.c_uint64(0)
+    check(L.zg_gen_rmat(scale, edge_factor, a, b, c, seed, 0, None, C.byref(m)))
+    out = np.empty((m.value, 2), dtype=np.uint32)
+    check(L.zg_gen_rmat(scale, edge_factor, a, b, c, seed, m.value, _ptr(out), C.byref(m)))
+    return out
+
+
+def gen_chung_lu(n, exponent, avg_degree, seed=1):
+    L = lib()
+    m = C.c_uint64(0)
+    check(L.zg_gen_chung_lu(n, exponent, avg_degree, seed, 0, None, C.byref(m)))
+    out = np.empty((m.value, 2), dtype=np.uint32)
+    check(L.zg_gen_chung_lu(n, exponent, avg_degree, seed, m.value, _ptr(out), C.byref(m)))
+    return out
+
+
+def gen_weights(m, max_value=100, seed=1):
+    w = np.empty(m, dtype=np.uint32)
+    check(lib().zg_gen_weights(m, max_value, seed, _ptr(w)))
+    return w
+
+
+# ---- graph --------------------------------------------------------------------------------
+class Graph:
+    """Device-resident Graph<E>: COO in edge-id order + both adjacency orders (zg_graph_create)."""
+
+    def __init__(self, handle, num_vertices, parent_index=None):
+        self._h = handle
+        self.num_vertices = num_vertices
+        self.parent_index = parent_index
+
+    @classmethod
+    def from_edges(cls, edges, num_vertices, weights=None, shuffle_seed=None, stream=None):
+        init()
+        e = np.ascontiguousarray(edges, dtype=np.uint32).reshape(-1, 2)
+        w = None if weights is None else np.ascontiguousarray(weights, dtype=np.uint32)
+        h = C.c_void_p()
+        L = lib()
+        if shuffle_seed is None:
+            check(L.zg_graph_create(_ptr(e), e.shape[0], num_vertices, _ptr(w), stream, C.byref(h)))
+            return cls(h, num_vertices)
+        parent = np.empty(e.shape[0], dtype=np.uint64)
+        check(L.zg_graph_permuted(_ptr(e), e.shape[0], num_vertices, _ptr(w), shuffle_seed, stream,
+                                  _ptr(parent), C.byref(h)))
+        return cls(h, num_vertices, parent)
+
+    @classmethod
+    def load(cls, path, weighted=False, shuffle_seed=None):
+        """Reads the reference's binary .biedgelist (+ .csv vertex count, src/Utilities.cpp:24-35)."""
+        raw = np.fromfile(path + ".biedgelist", dtype=np.uint32)
+        rec = raw.reshape(-1, 3 if weighted else 2)
+        with open(path + ".csv") as f:
+            f.readline()
+            line = f.readline()
+        digits = ""
+        for ch in line:
+            if ch.isdigit():
+                digits += ch
+            elif digits:
+                break
+        nv = int(digits)
+        return cls.from_edges(rec[:, :2], nv, rec[:, 2] if weighted else None, shuffle_seed=shuffle_seed)
+
+    @property
+    def handle(self):
+        if not self._h:
+            raise ValueError("graph was freed")
+        return self._h
+
+    def meta(self):
+        m = GraphMeta()
+        check(lib().zg_graph_get_meta(self.handle, C.byref(m)))
+        return m
+
+    @property
+    def num_local_edges(self):
+        return self.meta().num_local_edges
+
+    @property
+    def num_edges(self):
+        return self.meta().num_edges
+
+    @property
+    def max_degree(self):
+        return self.meta().max_degree
+
+    def set_meta(self, num_edges, max_degree):
+        check(lib().zg_graph_set_meta(self.handle, num_edges, max_degree))
+
+    def download(self):
+        m = self.num_local_edges
+        nv = self.num_vertices
+        out = {"edges": np.empty((m, 2), np.uint32), "offsets": np.empty(nv + 1, np.int64),
+               "adj_e": np.empty((2 * m, 2), np.uint32), "adj_n": np.empty((2 * m, 2), np.uint32),
+               "suffix": np.empty((m, 2), np.uint32)}
+        w = np.empty(m, np.uint32) if self.meta().weighted else None
+        check(lib().zg_graph_download(self.handle, _ptr(out["edges"]), _ptr(w), _ptr(out["offsets"]),
+                                      _ptr(out["adj_e"]), _ptr(out["adj_n"]), _ptr(out["suffix"])))
+        out["weights"] = w
+        return out
+
+    def filter(self, op, t0, t1=0, shuffle_seed=NO_SHUFFLE):
+        """GraphFilter::generate_graph (src/GraphFilters.cpp:17-177)."""
+        parent = np.empty(max(1, self.num_local_edges), np.uint64)
+        mo = C.c_uint64(0)
+        h = C.c_void_p()
+        check(lib().zg_graph_filter(self.handle, op, t0, t1, shuffle_seed, None, _ptr(parent), C.byref(mo),
+                                    C.byref(h)))
+        return Graph(h, self.num_vertices, parent[:mo.value].copy())
+
+    def subsample(self, rate, keep_seed, shuffle_seed=NO_SHUFFLE):
+        """GraphSampler::sample_graph (src/Graph.cpp:629-780)."""
+        parent = np.empty(max(1, self.num_local_edges), np.uint64)
+        mo = C.c_uint64(0)
+        h = C.c_void_p()
+        check(lib().zg_graph_subsample(self.handle, rate, keep_seed, shuffle_seed, None, _ptr(parent),
+                                       C.byref(mo), C.byref(h)))
+        return Graph(h, self.num_vertices, parent[:mo.value].copy())
+
+    def exact_count(self, kind, stream=None):
+        out = (C.c_uint64 * 2)()
+        check(lib().zg_exact_count(self.handle, kind, stream, out))
+        return int(out[0]) | (int(out[1]) << 64)
+
+    def free(self):
+        if self._h:
+            lib().zg_graph_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+# ---- programs -----------------------------------------------------------------------------
+class Program:
+    def __init__(self, kind, param=0, pattern=None):
+        h = C.c_void_p()
+        if kind == PROG_PATTERN:
+            nv, edges = pattern
+            e = np.ascontiguousarray(edges, dtype=np.uint32).reshape(-1, 2)
+            check(lib().zg_program_create_pattern(nv, e.shape[0], _ptr(e), C.byref(h)))
+        else:
+            check(lib().zg_program_create(kind, param, C.byref(h)))
+        self._h = h
+        self.kind = kind
+        self.param = param
+
+    @property
+    def handle(self):
+        return self._h
+
+    def info(self):
+        u, c, v = C.c_uint32(), C.c_uint32(), C.c_uint32()
+        check(lib().zg_program_info(self._h, C.byref(u), C.byref(c), C.byref(v)))
+        return {"num_unique": u.value, "cond_calls": c.value, "vertices": v.value}
+
+    def run(self, graph, n, seed, stream_id=0, first_sample=0, cuda_stream=None):
+        out = Counters()
+        check(lib().zg_run(graph.handle, self._h, n, first_sample, seed, stream_id, cuda_stream, C.byref(out)))
+        return out
+
+    def run_debug(self, graph, n, seed, stream_id=0, first_sample=0):
+        tr = np.zeros(n, dtype=TRACE_DTYPE)
+        check(lib().zg_run_debug(graph.handle, self._h, n, first_sample, seed, stream_id, _ptr(tr)))
+        return tr
+
+    def __del__(self):
+        try:
+            if self._h:
+                lib().zg_program_free(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+
+def run_three_motif(graph, n_chain, n_tri, seed, stream_chain=0, stream_tri=1, cuda_stream=None):
+    a, b = Counters(), Counters()
+    check(lib().zg_run_three_motif(graph.handle, n_chain, n_tri, seed, stream_chain, stream_tri, cuda_stream,
+                                   C.byref(a), C.byref(b)))
+    return a, b
+
+
+def run_three_motif_debug(graph, n_chain, n_tri, seed, stream_chain=0, stream_tri=1):
+    tc = np.zeros(max(1, n_chain), dtype=TRACE_DTYPE)
+    tt = np.zeros(max(1, n_tri), dtype=TRACE_DTYPE)
+    check(lib().zg_run_three_motif_debug(graph.handle, n_chain, n_tri, seed, stream_chain, stream_tri,
+                                         _ptr(tc), _ptr(tt)))
+    return tc[:n_chain], tt[:n_tri]
+
+
+# ---- the reference's estimator interface --------------------------------------------------
+class Estimation:
+    """Running mean of finished estimators (src/ZGraphInstance.cpp:15-35)."""
+
+    def __init__(self):
+        self.reset()
+
+    def reset(self):
+        self.num_finished_estimators = 0
+        self.current_estimation = 0.0
+
+    def update(self, new_num_estimators, new_estimation):
+        n, k = self.num_finished_estimators, new_num_estimators
+        self.current_estimation = (1.0 * n / (n + k)) * self.current_estimation + (1.0 * k / (n + k)) * new_estimation
+        self.num_finished_estimators = n + k
+
+    def get_num_finished_estimators(self):
+        return self.num_finished_estimators
+
+    def get_currnet_estimation(self):
+        return self.current_estimation
+
+
+class ZGraphInstance:
+    """ZGraphInstance<E> (include/ZGraphInstance.hpp:107-140) bound to one device program.
+
+    calculate(n, k, init) runs n estimators on the GPU and folds their mean into init exactly as
+    src/ZGraphInstance.cpp:257-297 does (one partition, one socket: scaling factor 1).  Each call
+    consumes fresh sample indices of this instance's Philox stream.
+    """
+
+    program_kind = None
+    program_param = 0
+
+    def __init__(self, graph, seed=None, stream_id=0):
+        init()
+        self._graph = graph
+        self.seed = int.from_bytes(os.urandom(8), "little") if seed is None else int(seed)
+        self.stream_id = stream_id
+        self.next_sample = 0
+        self.program = self._make_program()
+        self.last_counters = None
+
+    def _make_program(self):
+        return Program(self.program_kind, self.program_param)
+
+    def get_graph(self):
+        return self._graph
+
+    def set_graph(self, graph):
+        self._graph = graph
+
+    def _sampling_graph(self):
+        return self._graph
+
+    def run(self, n, cuda_stream=None):
+        """n estimators -> Counters (exact sums); advances the sample cursor."""
+        c = self.program.run(self._sampling_graph(), n, self.seed, self.stream_id, self.next_sample, cuda_stream)
+        self.next_sample += n
+        self.last_counters = c
+        return c
+
+    def calculate(self, num_estimators, num_vertices_in_pattern, init_estimation):
+        if init_estimation.get_num_finished_estimators() >= num_estimators:
+            return init_estimation.get_currnet_estimation()
+        n = num_estimators - init_estimation.get_num_finished_estimators()
+        c = self.run(n)
+        init_estimation.update(n, c.estimate)
+        return init_estimation.get_currnet_estimation()
+
+    def get_num_sample_edge_calls(self):
+        return 1.0  # src/ZGraphInstance.cpp:450-452 returns 1 before measuring
+
+    def get_num_conditional_sample_edge_calls(self):
+        return float(self.program.info()["cond_calls"])
+
+
+class TriangleCountingInstance(ZGraphInstance):
+    """applications/Triangle.cpp:42-74."""
+    program_kind = PROG_TRIANGLE
+
+
+class FourCliqueCountingInstance(ZGraphInstance):
+    """applications/FourClique.cpp:193-235."""
+    program_kind = PROG_FOUR_CLIQUE
+
+
+class ThreeChainCountingInstance(ZGraphInstance):
+    """applications/ThreeChain.cpp:309-331."""
+    program_kind = PROG_THREE_CHAIN
+
+
+class FourChainCountingInstance(ZGraphInstance):
+    """applications/FourChain.cpp:18-125."""
+    program_kind = PROG_FOUR_CHAIN
+
+
+class ChainMiningInstance(ZGraphInstance):
+    """applications/ChainMining.cpp:213-85 (order k)."""
+    program_kind = PROG_CHAIN
+
+    def __init__(self, graph, order, seed=None, stream_id=0):
+        self.program_param = int(order)
+        super().__init__(graph, seed, stream_id)
+
+
+class Pattern:
+    """Pattern (include/SamplerGenerator.hpp:9-49): num_vertices, edges as (src, dst) pairs."""
+
+    def __init__(self, num_vertices, num_edges, edges):
+        self.num_vertices = int(num_vertices)
+        self.edges = [(int(s), int(d)) for s, d in edges][:num_edges]
+        if len(self.edges) != num_edges:
+            raise ValueError("pattern lists %d edges, expected %d" % (len(self.edges), num_edges))
+
+    def get_num_vertices(self):
+        return self.num_vertices
+
+    def get_num_edges(self):
+        return len(self.edges)
+
+    def is_in_edges_list(self, e):
+        return any((a, b) == (e[0], e[1]) or (a, b) == (e[1], e[0]) for a, b in self.edges)
+
+    def is_automorphic(self, other):
+        """Pattern::is_automorphic (src/SamplerGenerator.cpp:307-324)."""
+        if other.num_vertices != self.num_vertices or len(other.edges) != len(self.edges):
+            return False
+        return all(self.is_in_edges_list(e) for e in other.edges)
+
+    def relabelled(self, mapping):
+        return Pattern(self.num_vertices, len(self.edges), [(mapping[s], mapping[d]) for s, d in self.edges])
+
+
+class SamplerGenerator(ZGraphInstance):
+    """SamplerGenerator<Empty>(graph, pattern) (src/SamplerGenerator.cpp:393-546)."""
+    program_kind = PROG_PATTERN
+
+    def __init__(self, graph, pattern, seed=None, stream_id=0):
+        self.pattern = pattern
+        super().__init__(graph, seed, stream_id)
+        self.num_unique_patterns = self.program.info()["num_unique"]
+
+    def _make_program(self):
+        return Program(PROG_PATTERN, pattern=(self.pattern.num_vertices, self.pattern.edges))
+
+    def get_num_sample_edge_calls(self):
+        return 1.0
+
+    def get_num_conditional_sample_edge_calls(self):
+        return float(self.pattern.get_num_edges() - 1)
+
+
+class AllPredicateZGraphInstance(ZGraphInstance):
+    """AllPredicateZGraphInstance<VertexId> (src/ZGraphInstance.cpp:492-525) running the triangle
+    estimator of applications/AllPredicateWeightedTriangle.cpp:42-72 on the filtered graph.
+    predicate = (op, t0[, t1]) with op one of PRED_*.
+    """
+    program_kind = PROG_TRIANGLE
+
+    def __init__(self, graph, predicate, seed=None, stream_id=0, shuffle_seed=None):
+        self.predicate = tuple(predicate)
+        self.shuffle_seed = shuffle_seed
+        self._filtered = None
+        super().__init__(graph, seed, stream_id)
+        self.set_graph(graph)
+
+    def set_graph(self, graph):
+        self._graph = graph
+        op, t0 = self.predicate[0], self.predicate[1]
+        t1 = self.predicate[2] if len(self.predicate) > 2 else 0
+        sh = self.seed ^ 0x5A5A5A5A if self.shuffle_seed is None else self.shuffle_seed
+        if self._filtered is not None:
+            self._filtered.free()
+        self._filtered = graph.filter(op, t0, t1, sh)
+
+    def get_filtered_graph(self):
+        return self._filtered
+
+    def _sampling_graph(self):
+        return self._filtered
+
+
+class ThreeMotif:
+    """applications/ThreeMotif.cpp:149-196: a 3-chain run whose wedges a triangle run re-closes
+    (ZGraphInstanceWithCache), fused into one kernel."""
+
+    def __init__(self, graph, seed=None):
+        init()
+        self.graph = graph
+        self.seed = int.from_bytes(os.urandom(8), "little") if seed is None else int(seed)
+
+    def calculate(self, n_chain, n_tri):
+        a, b = run_three_motif(self.graph, n_chain, n_tri, self.seed)
+        return a.estimate, b.estimate, a, b
