@@ -1,0 +1,326 @@
+#!/usr/bin/env python
+"""Benchmark of the neighbour-sampling estimator hot path on GB300.
+
+Workload (default "rmat20"): undirected R-MAT scale 20, edge factor 3, a/b/c/d = .57/.19/.19/.05,
+self-loops and duplicates removed (~3.1M edges, seeded synthetic input); one step = the
+triangle, 4-clique, 3-chain and 4-chain estimators with 2^26 samples each (2^28 estimators).
+
+  value : samples/s over the timed steps, device time from CUDA events on the launching stream
+          (graph resident in HBM; L2 flushed between steps by writing a 512 MiB buffer).
+  e2e   : samples/s through the public API (ZGraphInstance.calculate -> zg_run): host wall time
+          per query including the device->host read of each result.
+  roofline: dominant kernel, algorithmic bytes = access-model sectors x 32 B per sample (measured
+          per program by the debug kernel on 2^16 samples) x samples / kernel time.
+  cpu_baseline: the CPU restatement of the reference path (oracle, all host threads) on a
+          bounded sample of the same workload.
+
+--impl reference runs that CPU restatement as the measured arm (the reference is CPU code and
+does not build on this host without its MPI/NUMA stack).  Under torchrun each rank runs its
+own shard of sample indices (weak scaling); rank 0 prints one JSON line.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "sampling-graph-mining_gb300"))
+
+METRIC = "time-to-1%-error@95% and samples/s, learned vs plain ELP, 1 GB300"
+WORKLOADS = {
+    "rmat20": {"scale": 20, "edge_factor": 3, "a": 0.57, "b": 0.19, "c": 0.19, "seed": 1, "samples": 1 << 26,
+               "programs": ["triangle", "four_clique", "three_chain", "four_chain"]},
+    "rmat13": {"scale": 13, "edge_factor": 12, "a": 0.57, "b": 0.19, "c": 0.19, "seed": 1, "samples": 1 << 20,
+               "programs": ["triangle"]},
+}
+PROG_IDS = {"triangle": 1, "four_clique": 2, "three_chain": 3, "four_chain": 4}
+EXACT_IDS = {"triangle": 1, "three_chain": 2, "four_chain": 3, "four_clique": 5}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="rmat20", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        sm = [float(r[1]) for r in self.rows if len(r) > 8 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 8 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows if len(r) > 8 for i in range(4) if r[5 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """Per-launch DRAM bytes of the dominant kernels from the committed ncu summary, if any."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def make_graph(Z, wl):
+    e = Z.gen_rmat(wl["scale"], wl["edge_factor"], wl["a"], wl["b"], wl["c"], wl["seed"])
+    return e, 1 << wl["scale"]
+
+
+def cpu_baseline(wl, edges, nv, threads, target_s=12.0):
+    """The oracle (CPU restatement of the reference path) on a bounded sample of the workload."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    og = O.OracleGraph(edges, nv)
+    rates, total_samples, total_s = {}, 0, 0.0
+    budget = target_s / len(wl["programs"])
+    for name in wl["programs"]:
+        prog = O.OracleProgram(PROG_IDS[name])
+        n = 1 << 14
+        while True:
+            t0 = time.perf_counter()
+            O.run(og, prog, n, 0, 17, PROG_IDS[name], threads)
+            dt = time.perf_counter() - t0
+            if dt > budget / 4 or n >= (1 << 26):
+                break
+            n *= 4
+        rates[name] = n / dt
+        total_samples += n
+        total_s += dt
+    return {"value": total_samples / total_s, "unit": "samples/s", "cores": threads, "kind": "port",
+            "sample": "%s: %d samples per pattern class (bounded), oracle/zg_oracle.c with %d threads; per pattern %s"
+                      % (",".join(wl["programs"]), total_samples // len(wl["programs"]), threads,
+                         {k: round(v) for k, v in rates.items()})}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    wl = WORKLOADS[args.workload]
+    import zgraph as Z
+    edges, nv = make_graph(Z, wl)
+    threads = os.cpu_count() or 1
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    og = O.OracleGraph(edges, nv)
+    progs = [(PROG_IDS[p], O.OracleProgram(PROG_IDS[p])) for p in wl["programs"]]
+    # calibrate a bounded per-step sample (about 1-2 s of CPU per step)
+    n = 1 << 12
+    while True:
+        t0 = time.perf_counter()
+        for pid, p in progs:
+            O.run(og, p, n, 0, 5, pid, threads)
+        dt = time.perf_counter() - t0
+        if dt > 0.5 or n >= wl["samples"]:
+            break
+        n *= 2
+    for i in range(args.warmup):
+        for pid, p in progs:
+            O.run(og, p, n, i * n, 5, pid, threads)
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        for pid, p in progs:
+            O.run(og, p, n, (args.warmup + i) * n, 5, pid, threads)
+    dt = time.perf_counter() - t0
+    value = len(progs) * n * args.steps / dt
+    line = {"metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dt * 1000 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int64/f64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": "%s: R-MAT scale %d ef %d (%d edges), %s; bounded sample %d per pattern per step"
+                       % (args.workload, wl["scale"], wl["edge_factor"], len(edges), "+".join(wl["programs"]), n)},
+            "cpu_baseline": {"value": value, "unit": "samples/s", "cores": threads, "kind": "port",
+                             "sample": "%d samples x %d patterns per step, oracle/zg_oracle.c" % (n, len(progs))},
+            "e2e": {"value": value, "unit": "samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300(args):
+    import torch
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    import zgraph as Z
+    Z.init(local)
+    wl = WORKLOADS[args.workload]
+    n = wl["samples"]
+    edges, nv = make_graph(Z, wl)
+    t0 = time.perf_counter()
+    g = Z.Graph.from_edges(edges, nv)
+    torch.cuda.synchronize()
+    build_s = time.perf_counter() - t0
+    names = wl["programs"]
+    progs = [Z.Program(PROG_IDS[p]) for p in names]
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    d_res = torch.zeros((len(progs), Z.ZG_RESULT_BYTES if hasattr(Z, "ZG_RESULT_BYTES") else 112),
+                        dtype=torch.uint8, device="cuda")
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    seed = 20250101
+
+    def enqueue(step, evs=None):
+        for j, p in enumerate(progs):
+            if evs is not None:
+                evs[j].record(stream)
+            p.run_async(g, n, seed, d_res[j].data_ptr(), stream_id=j + 1,
+                        first_sample=(step * world + rank) * n, cuda_stream=sp)
+        if evs is not None:
+            evs[len(progs)].record(stream)
+
+    for i in range(args.warmup):
+        enqueue(i)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    per_prog = [0.0] * len(progs)
+    step_ms = []
+    for i in range(args.steps):
+        flush.zero_()
+        evs = [torch.cuda.Event(enable_timing=True) for _ in range(len(progs) + 1)]
+        enqueue(args.warmup + i, evs)
+        torch.cuda.synchronize()
+        for j in range(len(progs)):
+            per_prog[j] += evs[j].elapsed_time(evs[j + 1])
+        step_ms.append(evs[0].elapsed_time(evs[-1]))
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    total_ms = sum(step_ms)
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * len(progs) * n * args.steps / (total_ms / 1000.0)
+    res = [p.result_to_counters(bytes(d_res[j].cpu().numpy())) for j, p in enumerate(progs)]
+
+    # end to end through the public API: calculate() per program, results read back each query
+    insts = [getattr(Z, c)(g, seed=seed + 7, stream_id=j + 11) for j, c in
+             enumerate({"triangle": "TriangleCountingInstance", "four_clique": "FourCliqueCountingInstance",
+                        "three_chain": "ThreeChainCountingInstance",
+                        "four_chain": "FourChainCountingInstance"}[p] for p in names)]
+    for inst in insts:
+        inst.calculate(n, 3, Z.Estimation())
+    torch.cuda.synchronize()
+    e2e_steps = max(1, min(args.steps, 5))
+    t0 = time.perf_counter()
+    for i in range(e2e_steps):
+        for inst in insts:
+            inst.calculate(n, 3, Z.Estimation())
+    e2e_s = time.perf_counter() - t0
+    e2e = {"value": world * len(insts) * n * e2e_steps / e2e_s, "unit": "samples/s", "h2d_bytes_per_step": 0,
+           "d2h_bytes_per_step": len(insts) * 112}
+
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
+    # algorithmic bytes per sample: access model from the debug kernel (2^16 samples)
+    model = {}
+    for j, p in enumerate(progs):
+        tr = p.run_debug(g, 1 << 16, seed, stream_id=j + 1)
+        model[names[j]] = float(tr["sectors"].mean()) * 32.0
+    peak, peak_kind = peaks()
+    kern = []
+    for j, name in enumerate(names):
+        t = per_prog[j] / args.steps / 1000.0
+        ach = model[name] * n / t / 1e9
+        kern.append({"kernel": "k_sample<%s>" % name, "ms": per_prog[j] / args.steps, "bytes_per_sample": model[name],
+                     "achieved_gbs": ach, "samples_per_s": n / t, "hits": int(res[j].hits),
+                     "estimate": res[j].estimate})
+    dom = max(kern, key=lambda k: k["ms"])
+    traffic = profile_traffic().get(dom["kernel"])
+    roofline = {"bound": "hbm", "achieved": dom["achieved_gbs"], "peak": peak, "unit": "GB/s",
+                "frac": dom["achieved_gbs"] / peak, "traffic": traffic, "kernel": dom["kernel"],
+                "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
+                "per_kernel": kern}
+    # accuracy against the GPU exact counts
+    acc = {}
+    for j, name in enumerate(names):
+        ex = g.exact_count(EXACT_IDS[name])
+        acc[name] = {"exact": ex, "estimate": res[j].estimate,
+                     "rel_err": abs(res[j].estimate - ex) / ex if ex else None}
+    line = {"metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int64/u192 exact (f64 reference 1/p)",
+            "data": "synthetic (seeded R-MAT, zg_gen_rmat)",
+            "config": {"workload": "%s: R-MAT scale %d, edge factor %d, a/b/c=.57/.19/.19, %d undirected edges; "
+                                   "%s x 2^%d samples per step" % (args.workload, wl["scale"], wl["edge_factor"],
+                                                                   len(edges), "+".join(names),
+                                                                   n.bit_length() - 1),
+                       "l2": "flushed between steps (512 MiB write)", "graph_build_s": round(build_s, 3),
+                       "graph_device_bytes": int(g.meta().device_bytes)},
+            "e2e": e2e, "gpu_launches": 2 * len(progs) * args.steps, "clocks": clk, "roofline": roofline,
+            "accuracy": acc}
+    if not args.no_cpu_baseline and world == 1:
+        line["cpu_baseline"] = cpu_baseline(wl, edges, nv, os.cpu_count() or 1)
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

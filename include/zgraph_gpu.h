@@ -108,6 +108,8 @@ typedef struct zg_sample_trace {
   uint32_t hit;
   uint32_t fail;
   uint32_t shift;
+  uint32_t sectors;        /* 32-byte sectors of the access model (algorithmic bytes / 32) */
+  uint32_t reserved;
   double   w;              /* bit-exact reference value of estimate()               */
   uint64_t num[3];         /* 192-bit exact numerator                               */
   uint64_t lo[ZG_MAX_DRAWS];
@@ -182,6 +184,14 @@ int zg_program_info(const zg_program* p, uint32_t* num_unique, uint32_t* cond_ca
  * (src/ZGraphInstance.cpp:257-297) without the Estimation fold, which the host does. */
 int zg_run(const zg_graph* g, const zg_program* p, uint64_t n, uint64_t first_sample,
            uint64_t seed, uint32_t stream_id, void* cuda_stream, zg_counters* out);
+/* Asynchronous zg_run: enqueues the sampling and reduction kernels on cuda_stream and returns.
+ * The reduced result (ZG_RESULT_BYTES bytes) lands in device memory at d_result; copy it to the
+ * host after the stream completes and convert it with zg_result_to_counters.  Stream-ordered,
+ * so several runs can be queued back to back. */
+#define ZG_RESULT_BYTES 112
+int zg_run_async(const zg_graph* g, const zg_program* p, uint64_t n, uint64_t first_sample,
+                 uint64_t seed, uint32_t stream_id, void* cuda_stream, void* d_result);
+int zg_result_to_counters(const void* h_result, const zg_program* p, zg_counters* out);
 /* As zg_run, one trace per sample (n <= 2^22). */
 int zg_run_debug(const zg_graph* g, const zg_program* p, uint64_t n, uint64_t first_sample,
                  uint64_t seed, uint32_t stream_id, zg_sample_trace* traces);

@@ -155,7 +155,22 @@ typedef struct {
   int shift;
   u128 num_lo; uint64_t num_hi; /* 192-bit exact numerator */
   int overflow;
+  uint32_t sectors; /* 32-byte sector access model (see zgo_model_*) */
 } zgo_ctx;
+
+/* Access model of the rebuilt kernels, in 32-byte sectors (the roofline's algorithmic bytes):
+ * sample_edge 1; a conditional step sum over anchors v with d_v > 0 of 1 + max(1, ceil(log2 d_v) - 2),
+ * plus 1 for the chosen entry; a closure edge (x,y) 1 + max(1, ceil(log2 min(d_x,d_y)) - 2) + 1,
+ * counted for each edge checked up to the first miss. */
+static uint32_t zgo_clog2(uint64_t d) {
+  uint32_t b = 0;
+  while (((uint64_t)1 << b) < d) ++b;
+  return b;
+}
+static uint32_t zgo_model_search(uint64_t d) {
+  uint32_t l = zgo_clog2(d);
+  return l > 3 ? l - 2 : 1;
+}
 
 static uint64_t ctx_rand(zgo_ctx* c, uint64_t lo, uint64_t hi) {
   uint64_t v = zgo_draw(c->seed, c->stream, c->sample, c->nd, lo, hi);
@@ -182,6 +197,7 @@ static double prim_sample_edge(zgo_ctx* c, zgo_edge* out) {
   uint64_t id = ctx_rand(c, 0, g->m - 1);
   out->eid = id; out->src = g->src[id]; out->dst = g->dst[id];
   num_mul(c, g->m);
+  c->sectors += 1;
   return 1. / (double)g->m;
 }
 
@@ -198,6 +214,7 @@ static double prim_cond_sample(zgo_ctx* c, const zgo_edge* edges, int ne, const 
     uint32_t v = verts[i];
     uint64_t b = g->off[v], e = g->off[v + 1];
     if (e == b) continue; /* bitmap bit clear */
+    c->sectors += 1 + zgo_model_search(e - b);
     if (min_valid <= g->adj_eid[b]) { sum += e - b; pos[np++] = b; }
     else if (min_valid > g->adj_eid[e - 1]) { pos[np++] = e; }
     else if (e - b <= ZGO_BS_THRESHOLD) {
@@ -213,6 +230,7 @@ static double prim_cond_sample(zgo_ctx* c, const zgo_edge* edges, int ne, const 
     }
   }
   if (sum == 0) return -1.0;
+  c->sectors += 1;
   uint64_t rr = ctx_rand(c, 0, sum - 1);
   int pi = 0;
   uint64_t chosen = 0;
@@ -242,6 +260,10 @@ static int prim_close(zgo_ctx* c, const zgo_sub* sampled, const zgo_sub* wait) {
   for (int i = 0; i < wait->ne; ++i) {
     uint32_t ws = wait->e[i].src, wd = wait->e[i].dst;
     int found = 0;
+    {
+      uint64_t dx = g->off[ws + 1] - g->off[ws], dy = g->off[wd + 1] - g->off[wd];
+      c->sectors += 2 + zgo_model_search(dx < dy ? dx : dy);
+    }
     for (int j = 0; j < sampled->nv && !found; ++j) {
       uint32_t v = sampled->v[j];
       for (uint64_t idx = g->off[v]; idx < g->off[v + 1]; ++idx) {
@@ -602,13 +624,14 @@ static uint32_t prog_den_log2(const zgo_program* p) {
 static void ctx_init(zgo_ctx* c, const zgo_graph* g, uint64_t seed, uint32_t stream,
                      uint64_t sample, zg_sample_trace* tr) {
   c->g = g; c->seed = seed; c->stream = stream; c->sample = sample; c->nd = 0; c->tr = tr;
-  c->shift = 0; c->num_lo = 1; c->num_hi = 0; c->overflow = 0;
+  c->shift = 0; c->num_lo = 1; c->num_hi = 0; c->overflow = 0; c->sectors = 0;
   memset(tr, 0, sizeof(*tr));
 }
 
 static void ctx_finish(zgo_ctx* c, double r) {
   zg_sample_trace* tr = c->tr;
   tr->ndraws = c->nd;
+  tr->sectors = c->sectors;
   if (r < 0) { tr->fail = 1; r = 0; }
   tr->w = r;
   tr->hit = r != 0;

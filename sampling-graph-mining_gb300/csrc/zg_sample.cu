@@ -29,6 +29,7 @@ struct Ctx {
   uint32_t stream;
   uint32_t nd;
   zg_sample_trace* tr;  // debug only
+  uint32_t sectors;     // debug only: access model, 32-byte sectors
   __device__ __forceinline__ uint64_t draw(uint64_t lo, uint64_t hi) {
     uint64_t v = zg_draw(seed, stream, sample, nd, lo, hi);
     if (tr && nd < ZG_MAX_DRAWS) {
@@ -98,10 +99,24 @@ __device__ __forceinline__ bool edge_after(int64_t bx, int64_t ex, int64_t by, i
   return a.x == t && a.y >= min_valid;
 }
 
-__device__ __forceinline__ bool edge_after_v(const ZgDevGraph& g, uint32_t x, uint32_t y, uint32_t min_valid) {
-  int64_t bx = ZG_LDG(&g.off[x]), ex = ZG_LDG(&g.off[x + 1]);
-  int64_t by = ZG_LDG(&g.off[y]), ey = ZG_LDG(&g.off[y + 1]);
-  return edge_after(bx, ex, by, ey, x, y, min_valid, g.adj_n);
+// ---- access model (debug): algorithmic bytes of a sample in 32-byte sectors ---------------
+// sample_edge 1; a conditional step: per anchor v with d_v > 0, 1 + max(1, ceil(log2 d_v) - 2),
+// plus 1 for the chosen entry; a closure edge: 2 + max(1, ceil(log2 min(d_x, d_y)) - 2),
+// counted for every edge checked up to the first miss.
+__device__ __forceinline__ uint32_t model_search(uint64_t d) {
+  uint32_t l = d <= 1 ? 0u : (uint32_t)(64 - __clzll(d - 1));
+  return l > 3 ? l - 2 : 1u;
+}
+__device__ __forceinline__ uint64_t degree(const ZgDevGraph& g, uint32_t v) {
+  return (uint64_t)(ZG_LDG(&g.off[v + 1]) - ZG_LDG(&g.off[v]));
+}
+__device__ __forceinline__ uint32_t model_anchor(const ZgDevGraph& g, uint32_t v) {
+  uint64_t d = degree(g, v);
+  return d ? 1 + model_search(d) : 0;
+}
+__device__ __forceinline__ uint32_t model_close(const ZgDevGraph& g, uint32_t x, uint32_t y) {
+  uint64_t dx = degree(g, x), dy = degree(g, y);
+  return 2 + model_search(dx < dy ? dx : dy);
 }
 
 // ---- reference doubles (debug) ---------------------------------------------------------
@@ -203,10 +218,12 @@ __device__ void prog_triangle(const ZgDevGraph& g, Ctx& c, Res& r) {
   uint64_t e0 = c.draw(0, g.m - 1);
   uint4 q = ZG_LDG(&g.rec[e0]);
   uint64_t S = (uint64_t)q.z + q.w;
+  if (DBG) c.sectors += 1 + model_anchor(g, q.x) + model_anchor(g, q.y);
   if (S == 0) {
     r.fail = true;
     return;
   }
+  if (DBG) c.sectors += 1;
   uint64_t r1 = c.draw(0, S - 1);
   uint32_t anchor = q.x, other = q.y, suf = q.z;
   if (r1 >= q.z) {
@@ -225,6 +242,7 @@ __device__ void prog_triangle(const ZgDevGraph& g, Ctx& c, Res& r) {
   if (a1 == 2) r.shift = 1;
   int64_t bc = ZG_LDG(&g.off[e1.x]), ec = ZG_LDG(&g.off[e1.x + 1]);
   bool closed = (a1 == 1) && edge_after(bo, eo, bc, ec, other, e1.x, e1.y + 1, g.adj_n);
+  if (DBG) c.sectors += model_close(g, other, e1.x);
   r.hit = closed;
   if (DBG && closed) {
     double p = 1.0;
@@ -244,10 +262,12 @@ __device__ void prog_three_chain(const ZgDevGraph& g, Ctx& c, Res& r) {
   uint64_t e0 = c.draw(0, g.m - 1);
   uint4 q = ZG_LDG(&g.rec[e0]);
   uint64_t S = (uint64_t)q.z + q.w;
+  if (DBG) c.sectors += 1 + model_anchor(g, q.x) + model_anchor(g, q.y);
   if (S == 0) {
     r.fail = true;
     return;
   }
+  if (DBG) c.sectors += 1;
   uint64_t r1 = c.draw(0, S - 1);
   // The chosen edge only sets the appearance count a, which is 1 on a simple graph
   // (zg_graph_create rejects duplicate edges); the debug variant reads it and checks.
@@ -284,10 +304,12 @@ __device__ void prog_four_clique(const ZgDevGraph& g, Ctx& c, Res& r) {
   uint64_t e0 = c.draw(0, g.m - 1);
   uint4 q = ZG_LDG(&g.rec[e0]);
   uint64_t S1 = (uint64_t)q.z + q.w;
+  if (DBG) c.sectors += 1 + model_anchor(g, q.x) + model_anchor(g, q.y);
   if (S1 == 0) {
     r.fail = true;
     return;
   }
+  if (DBG) c.sectors += 1;
   uint64_t r1 = c.draw(0, S1 - 1);
   // vertex slots in insertion order: 0 = a (e0.src), 1 = b (e0.dst), 2 = c, 3 = d
   uint32_t v[4];
@@ -327,10 +349,12 @@ __device__ void prog_four_clique(const ZgDevGraph& g, Ctx& c, Res& r) {
     // c coincides with a or b (duplicate edges): the reference lists only two vertices
     S2 = (uint64_t)(end[0] - lb[0]) + (uint64_t)(end[1] - lb[1]);
   }
+  if (DBG) c.sectors += model_anchor(g, v[0]) + model_anchor(g, v[1]) + (a1 == 1 ? model_anchor(g, v[2]) : 0);
   if (S2 == 0) {
     r.fail = true;
     return;
   }
+  if (DBG) c.sectors += 1;
   uint64_t r2 = c.draw(0, S2 - 1);
   int s2 = 0;
   int nslots = a1 == 1 ? 3 : 2;
@@ -361,7 +385,10 @@ __device__ void prog_four_clique(const ZgDevGraph& g, Ctx& c, Res& r) {
 #pragma unroll
     for (int j = i + 1; j < 4; ++j) {
       bool sampled = (i == 0 && j == 1) || (i == s1 && j == 2) || (i == s2 && j == 3);
-      if (!sampled && ok) ok = edge_after(beg[i], end[i], beg[j], end[j], v[i], v[j], mv2, g.adj_n);
+      if (!sampled && ok) {
+        ok = edge_after(beg[i], end[i], beg[j], end[j], v[i], v[j], mv2, g.adj_n);
+        if (DBG) c.sectors += model_close(g, v[i], v[j]);
+      }
     }
   r.hit = ok;
   if (DBG && ok) {
@@ -389,13 +416,16 @@ __device__ void prog_four_chain(const ZgDevGraph& g, Ctx& c, Res& r) {
   uint64_t S1, S2;
   uint32_t a1 = 1, a2 = 1;
   bool ok;
+  if (DBG) c.sectors += 1;
   if (sel != 3) {
     // edges [e0], vertices [a, b]
     S1 = (uint64_t)q.z + q.w;
+    if (DBG) c.sectors += model_anchor(g, a) + model_anchor(g, b);
     if (S1 == 0) {
       r.fail = true;
       return;
     }
+    if (DBG) c.sectors += 1;
     uint64_t r1 = c.draw(0, S1 - 1);
     uint32_t anchor = a, suf = q.z;
     if (r1 >= q.z) {
@@ -427,10 +457,12 @@ __device__ void prog_four_chain(const ZgDevGraph& g, Ctx& c, Res& r) {
       lbn = lb_eid(g.adj_e, ZG_LDG(&g.off[nw]), pos1 + 1, (uint32_t)e0 + 1);
     }
     S2 = (uint64_t)(endn - lbn);
+    if (DBG) c.sectors += model_anchor(g, nw);
     if (S2 == 0) {
       r.fail = true;
       return;
     }
+    if (DBG) c.sectors += 1;
     uint64_t r2 = c.draw(0, S2 - 1);
     uint2 e2 = ZG_LDG(&g.adj_e[lbn + (int64_t)r2]);
     a2 = 1 + (e2.x == nw);
@@ -441,20 +473,24 @@ __device__ void prog_four_chain(const ZgDevGraph& g, Ctx& c, Res& r) {
   } else {
     // vertices [a]: e1 from a's list; then vertices [b]: e2 from b's list; edges [e0]
     S1 = q.z;
+    if (DBG) c.sectors += model_anchor(g, a);
     if (S1 == 0) {
       r.fail = true;
       return;
     }
+    if (DBG) c.sectors += 1;
     uint64_t r1 = c.draw(0, S1 - 1);
     uint2 e1 = ZG_LDG(&g.adj_e[ZG_LDG(&g.off[a + 1]) - (int64_t)q.z + (int64_t)r1]);
     a1 = 1 + (e1.x == a);
     res_mul(r, S1);
     if (a1 == 2) r.shift++;
     S2 = q.w;
+    if (DBG) c.sectors += model_anchor(g, b);
     if (S2 == 0) {
       r.fail = true;
       return;
     }
+    if (DBG) c.sectors += 1;
     uint64_t r2 = c.draw(0, S2 - 1);
     uint2 e2 = ZG_LDG(&g.adj_e[ZG_LDG(&g.off[b + 1]) - (int64_t)q.w + (int64_t)r2]);
     a2 = 1 + (e2.x == b);
@@ -513,14 +549,17 @@ __device__ void prog_chain(const ZgDevGraph& g, int order, Ctx& c, Res& r) {
   fl[1] = fe[1] - q.w;
   Ext p;
   if (DBG) p = ext_from_double(ddiv(1.0, u2d(g.m)));
+  if (DBG) c.sectors += 1;
   uint32_t mv = (uint32_t)e0 + 1;
   for (int i = 0; i < order - 2; ++i) {
     uint64_t l0 = (uint64_t)(fe[0] - fl[0]), l1 = (uint64_t)(fe[1] - fl[1]);
     uint64_t S = l0 + l1;
+    if (DBG) c.sectors += model_anchor(g, f[0]) + model_anchor(g, f[1]);
     if (S == 0) {
       r.fail = true;
       return;
     }
+    if (DBG) c.sectors += 1;
     uint64_t rr = c.draw(0, S - 1);
     int side = 0;
     if (rr >= l0) {
@@ -591,13 +630,17 @@ __device__ void prog_pattern(const ZgDevGraph& g, const ZgProgParams& pp, Ctx& c
   uint32_t mv = (uint32_t)e0 + 1;
   double p = 1.0;
   if (DBG) p = dmul(p, ddiv(1.0, u2d(g.m)));
+  if (DBG) c.sectors += 1;
   for (uint32_t k = 1; k < pp.pe; ++k) {
     uint64_t S = 0;
     for (int i = 0; i < nvtx; ++i) S += (uint64_t)(ve[i] - vl[i]);
+    if (DBG)
+      for (int i = 0; i < nvtx; ++i) c.sectors += model_anchor(g, vs[i]);
     if (S == 0) {
       r.fail = true;
       return;
     }
+    if (DBG) c.sectors += 1;
     uint64_t rr = c.draw(0, S - 1);
     int side = 0;
     for (; side < nvtx - 1; ++side) {
@@ -773,7 +816,7 @@ __global__ void __launch_bounds__(kBlock) k_sample(ZgDevGraph g, ZgProgParams pp
   acc_init(a);
   uint64_t stride = (uint64_t)gridDim.x * kBlock;
   for (uint64_t i = blockIdx.x * (uint64_t)kBlock + threadIdx.x; i < n; i += stride) {
-    Ctx c{seed, first + i, stream, 0, nullptr};
+    Ctx c{seed, first + i, stream, 0, nullptr, 0};
     Res r;
     res_init(r);
     if (KIND == ZG_PROG_TRIANGLE) prog_triangle<false>(g, c, r);
@@ -795,7 +838,7 @@ __global__ void __launch_bounds__(kBlock) k_sample_debug(ZgDevGraph g, ZgProgPar
   uint64_t stride = (uint64_t)gridDim.x * kBlock;
   for (uint64_t i = blockIdx.x * (uint64_t)kBlock + threadIdx.x; i < n; i += stride) {
     zg_sample_trace* t = &traces[i];
-    Ctx c{seed, first + i, stream, 0, t};
+    Ctx c{seed, first + i, stream, 0, t, 0};
     Res r;
     res_init(r);
     run_program<true>(g, pp, c, r);
@@ -804,6 +847,7 @@ __global__ void __launch_bounds__(kBlock) k_sample_debug(ZgDevGraph g, ZgProgPar
     t->hit = r.hit;
     t->fail = r.fail;
     t->shift = r.hit ? r.shift : 0;
+    t->sectors = c.sectors;
     t->w = r.hit ? r.w : 0.0;
     t->num[0] = r.hit ? r.num.l[0] : 0;
     t->num[1] = r.hit ? r.num.l[1] : 0;
@@ -827,7 +871,8 @@ __global__ void __launch_bounds__(kBlock) k_three_motif(ZgDevGraph g, uint64_t n
   for (uint64_t i = blockIdx.x * (uint64_t)kBlock + threadIdx.x; i < n; i += stride) {
     if (i < n_chain) {
       // ThreeChainCountingInstance: keep the wedge; the triangle instance closes it (:54-62)
-      Ctx c{seed, i, stream_chain, 0, DBG ? &tc[i] : nullptr};
+      Ctx c{seed, i, stream_chain, 0, DBG ? &tc[i] : nullptr, 0};
+      uint32_t tri_sectors = 0;
       Res r;
       res_init(r);
       Res rt;
@@ -838,9 +883,11 @@ __global__ void __launch_bounds__(kBlock) k_three_motif(ZgDevGraph g, uint64_t n
         uint64_t e0 = c.draw(0, g.m - 1);
         uint4 q = ZG_LDG(&g.rec[e0]);
         uint64_t S = (uint64_t)q.z + q.w;
+        if (DBG) c.sectors += 1 + model_anchor(g, q.x) + model_anchor(g, q.y);
         if (S == 0) {
           r.fail = true;
         } else {
+          if (DBG) c.sectors += 1;
           uint64_t r1 = c.draw(0, S - 1);
           uint32_t anchor = q.x, other = q.y, suf = q.z;
           if (r1 >= q.z) {
@@ -859,6 +906,7 @@ __global__ void __launch_bounds__(kBlock) k_three_motif(ZgDevGraph g, uint64_t n
             if (a1 == 2) r.shift = 1;
             int64_t bc = ZG_LDG(&g.off[e1.x]), ec = ZG_LDG(&g.off[e1.x + 1]);
             rt.hit = a1 == 1 && edge_after(bo, eo, bc, ec, other, e1.x, e1.y + 1, g.adj_n);
+            if (DBG) tri_sectors = model_close(g, other, e1.x);
             rt.num = r.num;
             rt.shift = r.shift;
           }
@@ -878,6 +926,7 @@ __global__ void __launch_bounds__(kBlock) k_three_motif(ZgDevGraph g, uint64_t n
         t->hit = r.hit;
         t->fail = r.fail;
         t->shift = r.hit ? r.shift : 0;
+        t->sectors = c.sectors;
         t->w = r.hit ? r.w : 0.0;
         t->num[0] = r.hit ? r.num.l[0] : 0;
         t->num[1] = r.hit ? r.num.l[1] : 0;
@@ -891,6 +940,7 @@ __global__ void __launch_bounds__(kBlock) k_three_motif(ZgDevGraph g, uint64_t n
           t->hit = rt.hit;
           t->fail = 0;
           t->shift = rt.hit ? rt.shift : 0;
+          t->sectors = tri_sectors;
           t->w = rt.w;
           t->num[0] = rt.hit ? rt.num.l[0] : 0;
           t->num[1] = rt.hit ? rt.num.l[1] : 0;
@@ -898,7 +948,7 @@ __global__ void __launch_bounds__(kBlock) k_three_motif(ZgDevGraph g, uint64_t n
         }
       }
     } else {
-      Ctx c{seed, i, stream_tri, 0, DBG ? &tt[i] : nullptr};
+      Ctx c{seed, i, stream_tri, 0, DBG ? &tt[i] : nullptr, 0};
       Res r;
       res_init(r);
       prog_triangle<DBG>(g, c, r);
@@ -909,6 +959,7 @@ __global__ void __launch_bounds__(kBlock) k_three_motif(ZgDevGraph g, uint64_t n
         t->hit = r.hit;
         t->fail = r.fail;
         t->shift = r.hit ? r.shift : 0;
+        t->sectors = c.sectors;
         t->w = r.hit ? r.w : 0.0;
         t->num[0] = r.hit ? r.num.l[0] : 0;
         t->num[1] = r.hit ? r.num.l[1] : 0;
@@ -924,8 +975,6 @@ __global__ void __launch_bounds__(kBlock) k_three_motif(ZgDevGraph g, uint64_t n
 // Single-block reduction of the per-block partials, fixed order.
 __global__ void __launch_bounds__(kBlock) k_finalize(const ZgPartial* __restrict__ parts, int nparts,
                                                      ZgPartial* __restrict__ out) {
-  Acc dummy;
-  (void)dummy;
   unsigned long long v[12] = {0};
   double d0 = 0, d1 = 0;
   for (int b = threadIdx.x; b < nparts; b += kBlock) {
@@ -1138,6 +1187,35 @@ extern "C" int zg_run(const zg_graph* g, const zg_program* p, uint64_t n, uint64
   if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
   if (ce == cudaSuccess) ce = cudaGetLastError();
   if (ce != cudaSuccess) return zg_check_cuda(ce, "zg_run");
+  partial_to_counters(h, den_for(p), out);
+  return ZG_OK;
+}
+
+static_assert(sizeof(ZgPartial) == ZG_RESULT_BYTES, "result layout");
+
+extern "C" int zg_run_async(const zg_graph* g, const zg_program* p, uint64_t n, uint64_t first_sample,
+                            uint64_t seed, uint32_t stream_id, void* cuda_stream, void* d_result) {
+  int rc = validate_run(g, p);
+  if (rc) return rc;
+  if (!d_result) return zg_set_error(ZG_ERR_INVALID_ARG, "null device result"), ZG_ERR_INVALID_ARG;
+  cudaStream_t s = (cudaStream_t)cuda_stream;
+  uint64_t maxg = (n + kBlock - 1) / kBlock;
+  int grid = grid_for_kind(p->kind);
+  if ((uint64_t)grid > maxg) grid = (int)(maxg ? maxg : 1);
+  ZgPartial* parts = nullptr;
+  ZG_CUDA(cudaMallocAsync((void**)&parts, sizeof(ZgPartial) * grid, s));
+  launch_sample(g, p, n, first_sample, seed, stream_id, s, parts, grid);
+  k_finalize<<<1, kBlock, 0, s>>>(parts, grid, (ZgPartial*)d_result);
+  cudaFreeAsync(parts, s);
+  cudaError_t ce = cudaGetLastError();
+  if (ce != cudaSuccess) return zg_check_cuda(ce, "zg_run_async");
+  return ZG_OK;
+}
+
+extern "C" int zg_result_to_counters(const void* h_result, const zg_program* p, zg_counters* out) {
+  if (!h_result || !p || !out) return zg_set_error(ZG_ERR_INVALID_ARG, "null argument"), ZG_ERR_INVALID_ARG;
+  ZgPartial h;
+  memcpy(&h, h_result, sizeof(h));
   partial_to_counters(h, den_for(p), out);
   return ZG_OK;
 }

@@ -66,7 +66,7 @@ class Counters(C.Structure):
 
 
 TRACE_DTYPE = np.dtype([("ndraws", "<u4"), ("hit", "<u4"), ("fail", "<u4"), ("shift", "<u4"),
-                        ("w", "<f8"), ("num", "<u8", (3,)), ("lo", "<u8", (MAX_DRAWS,)),
+                        ("sectors", "<u4"), ("reserved", "<u4"), ("w", "<f8"), ("num", "<u8", (3,)), ("lo", "<u8", (MAX_DRAWS,)),
                         ("hi", "<u8", (MAX_DRAWS,)), ("val", "<u8", (MAX_DRAWS,))])
 
 _lib = None
@@ -98,6 +98,8 @@ def lib():
             "zg_program_free": ([P], I32),
             "zg_program_info": ([P, C.POINTER(U32), C.POINTER(U32), C.POINTER(U32)], I32),
             "zg_run": ([P, P, U64, U64, U64, U32, P, C.POINTER(Counters)], I32),
+            "zg_run_async": ([P, P, U64, U64, U64, U32, P, P], I32),
+            "zg_result_to_counters": ([P, P, C.POINTER(Counters)], I32),
             "zg_run_debug": ([P, P, U64, U64, U64, U32, P], I32),
             "zg_run_three_motif": ([P, U64, U64, U64, U32, U32, P, C.POINTER(Counters), C.POINTER(Counters)], I32),
             "zg_run_three_motif_debug": ([P, U64, U64, U64, U32, U32, P, P], I32),
@@ -299,6 +301,17 @@ class Program:
     def run(self, graph, n, seed, stream_id=0, first_sample=0, cuda_stream=None):
         out = Counters()
         check(lib().zg_run(graph.handle, self._h, n, first_sample, seed, stream_id, cuda_stream, C.byref(out)))
+        return out
+
+    def run_async(self, graph, n, seed, d_result, stream_id=0, first_sample=0, cuda_stream=None):
+        """Enqueues the run on cuda_stream; the 112-byte result lands at device address d_result."""
+        check(lib().zg_run_async(graph.handle, self._h, n, first_sample, seed, stream_id, cuda_stream,
+                                 C.c_void_p(d_result)))
+
+    def result_to_counters(self, host_bytes):
+        out = Counters()
+        buf = (C.c_char * len(host_bytes)).from_buffer_copy(host_bytes)
+        check(lib().zg_result_to_counters(buf, self._h, C.byref(out)))
         return out
 
     def run_debug(self, graph, n, seed, stream_id=0, first_sample=0):

@@ -1,0 +1,85 @@
+"""libzgraph_gpu.so against outputs of the reference's own code (tests/golden/): per-sample
+estimate() values, ThreeMotif's cached run and the all-predicate triangle bit for bit, and the
+naive exact counters bit for bit."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import zgraph as Z
+from conftest import GOLDEN
+from test_oracle_golden import golden_graph
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def golden():
+    Z.init(0)
+    meta = json.load(open(os.path.join(GOLDEN, "reference_outputs.json")))
+    arr = np.load(os.path.join(GOLDEN, "reference_outputs.npz"))
+    return meta, arr
+
+
+def test_samples_bit_exact(golden):
+    meta, arr = golden
+    graphs = {}
+    for key, s in meta["samples"].items():
+        gname, label = key.split("__")
+        if label == "three_motif" or label.startswith("pred_"):
+            continue
+        if gname not in graphs:
+            e, nv = golden_graph(meta, arr, gname)
+            graphs[gname] = Z.Graph.from_edges(e, nv)
+        pat = s["pattern"]
+        prog = Z.Program(s["kind"], s["param"], None if pat is None else (pat[0], pat[1]))
+        tr = prog.run_debug(graphs[gname], s["n"], s["seed"], stream_id=s["stream"])
+        assert np.array_equal(tr["w"].view(np.uint64), arr["w__" + key]), key
+        assert np.array_equal(tr["ndraws"], arr["ndraws__" + key]), key
+        c = prog.run(graphs[gname], s["n"], s["seed"], stream_id=s["stream"])
+        assert c.hits == s["hits"], key
+
+
+def test_three_motif(golden):
+    meta, arr = golden
+    for key, s in meta["samples"].items():
+        gname, label = key.split("__")
+        if label != "three_motif":
+            continue
+        e, nv = golden_graph(meta, arr, gname)
+        g = Z.Graph.from_edges(e, nv)
+        tc, tt = Z.run_three_motif_debug(g, s["n_chain"], s["n_tri"], s["seed"], s["stream_chain"], s["stream_tri"])
+        for tr, n, ref in ((tc, s["n_chain"], s["chain"]), (tt, s["n_tri"], s["triangle"])):
+            acc = 0.0
+            for w in tr["w"]:
+                acc += w
+            assert (acc / float(n)).hex() == ref, key
+
+
+def test_all_predicate_triangle(golden):
+    meta, arr = golden
+    e, nv = golden_graph(meta, arr, "wiki_vote")
+    w = arr["wiki_vote_weights"]
+    g = Z.Graph.from_edges(e, nv, weights=w)
+    for key, s in meta["samples"].items():
+        if "__pred_" not in key:
+            continue
+        inst = Z.AllPredicateZGraphInstance(g, (s["op"], s["t"]), seed=s["seed"], stream_id=s["stream"],
+                                           shuffle_seed=s["shuffle_seed"])
+        f = inst.get_filtered_graph()
+        assert f.num_local_edges == s["filtered_m"]
+        tr = inst.program.run_debug(f, s["n"], s["seed"], stream_id=s["stream"])
+        assert np.array_equal(tr["w"].view(np.uint64), arr["w__" + key]), key
+
+
+def test_naive_exact_counts(golden):
+    meta, arr = golden
+    kinds = {"triangle": Z.EXACT_TRIANGLE, "wedge": Z.EXACT_WEDGE, "three_path": Z.EXACT_THREE_PATH,
+             "five_star": Z.EXACT_FIVE_STAR, "four_clique": Z.EXACT_FOUR_CLIQUE}
+    for gname, counts in meta["naive"].items():
+        e, nv = golden_graph(meta, arr, gname)
+        g = Z.Graph.from_edges(e, nv)
+        for k, v in counts.items():
+            if k in kinds:
+                assert g.exact_count(kinds[k]) == v, (gname, k)

@@ -1,0 +1,175 @@
+"""The CPU oracle against outputs the reference's own code produced (tests/golden/, made by
+tests/golden/make_golden.py): per-sample estimate() values bit for bit, calculate()'s reduction,
+ThreeMotif's cached run, the all-predicate triangle on a filtered graph, naive exact counts,
+the reference tests' known answers and the ELP building blocks."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+import zgraph as Z
+from conftest import GOLDEN
+
+STAR = (5, [(0, 1), (0, 2), (0, 3), (0, 4)])
+HOUSE = (5, [(0, 1), (0, 2), (1, 2), (1, 3), (2, 4), (3, 4)])
+TRI = (3, [(0, 1), (0, 2), (1, 2)])
+
+
+@pytest.fixture(scope="module")
+def golden():
+    meta = json.load(open(os.path.join(GOLDEN, "reference_outputs.json")))
+    arr = np.load(os.path.join(GOLDEN, "reference_outputs.npz"))
+    return meta, arr
+
+
+def golden_graph(meta, arr, name):
+    g = meta["graphs"][name]
+    if name + "_edges" in arr:
+        e = arr[name + "_edges"]
+    elif g["generator"] == "rmat":
+        p = g["params"]
+        e = Z.gen_rmat(p["scale"], p["edge_factor"], p["a"], p["b"], p["c"], p["seed"])
+    else:
+        p = g["params"]
+        e = Z.gen_chung_lu(p["n"], p["exponent"], p["avg_degree"], p["seed"])
+    import hashlib
+    assert hashlib.sha256(np.ascontiguousarray(e, dtype=np.uint32).tobytes()).hexdigest() == g["sha256"]
+    return e, g["num_vertices"]
+
+
+def test_samples_bit_exact(golden):
+    meta, arr = golden
+    graphs = {}
+    checked = 0
+    for key, s in meta["samples"].items():
+        gname, label = key.split("__")
+        if label == "three_motif" or label.startswith("pred_"):
+            continue
+        if gname not in graphs:
+            e, nv = golden_graph(meta, arr, gname)
+            graphs[gname] = O.OracleGraph(e, nv)
+        pat = s["pattern"]
+        prog = O.OracleProgram(s["kind"], s["param"], None if pat is None else (pat[0], pat[1]))
+        tr, _ = O.traces(graphs[gname], prog, s["n"], s["seed"], stream=s["stream"])
+        assert np.array_equal(tr["w"].view(np.uint64), arr["w__" + key]), key
+        assert np.array_equal(tr["ndraws"], arr["ndraws__" + key]), key
+        checked += 1
+        if "calculate" in s:
+            # calculate(n): one thread sums estimate() in sample order, divides by n (:273-292)
+            acc = 0.0
+            for w in tr["w"]:
+                acc += w
+            assert (acc / float(s["n"])).hex() == s["calculate"]
+    assert checked >= 50
+
+
+def test_three_motif(golden):
+    meta, arr = golden
+    for key, s in meta["samples"].items():
+        gname, label = key.split("__")
+        if label != "three_motif":
+            continue
+        e, nv = golden_graph(meta, arr, gname)
+        tc, tt, _, _ = O.three_motif(O.OracleGraph(e, nv), s["n_chain"], s["n_tri"], s["seed"], s["stream_chain"],
+                                     s["stream_tri"])
+        for tr, n, ref in ((tc, s["n_chain"], s["chain"]), (tt, s["n_tri"], s["triangle"])):
+            acc = 0.0
+            for w in tr["w"]:
+                acc += w
+            assert (acc / float(n)).hex() == ref, key
+
+
+def test_all_predicate_triangle(golden):
+    meta, arr = golden
+    e, nv = golden_graph(meta, arr, "wiki_vote")
+    w = arr["wiki_vote_weights"]
+    for key, s in meta["samples"].items():
+        if "__pred_" not in key:
+            continue
+        keep = np.array([O.pred(s["op"], s["t"], 0, int(x)) for x in w])
+        idx = np.nonzero(keep)[0]
+        assert len(idx) == s["filtered_m"]
+        fe = e[idx][O.shuffle_perm(len(idx), s["shuffle_seed"]).astype(np.int64)]
+        tr, _ = O.traces(O.OracleGraph(fe, nv), O.OracleProgram(Z.PROG_TRIANGLE), s["n"], s["seed"],
+                         stream=s["stream"])
+        assert np.array_equal(tr["w"].view(np.uint64), arr["w__" + key]), key
+
+
+def test_naive_exact_counts(golden):
+    meta, arr = golden
+    kinds = {"triangle": Z.EXACT_TRIANGLE, "wedge": Z.EXACT_WEDGE, "three_path": Z.EXACT_THREE_PATH,
+             "five_star": Z.EXACT_FIVE_STAR, "four_clique": Z.EXACT_FOUR_CLIQUE}
+    for gname, counts in meta["naive"].items():
+        e, nv = golden_graph(meta, arr, gname)
+        og = O.OracleGraph(e, nv)
+        for k, v in counts.items():
+            if k in kinds:
+                assert og.exact_fast(kinds[k]) == v, (gname, k)
+                if gname != "wiki_vote" or k != "three_path":
+                    if k != "four_clique" or nv <= 4096:
+                        assert og.exact_naive(kinds[k]) == v, (gname, k)
+    e, nv = golden_graph(meta, arr, "wiki_vote")
+    og = O.OracleGraph(e, nv, arr["wiki_vote_weights"])
+    assert og.exact_weighted_triangle(50, False) == meta["naive"]["wiki_vote"]["weighted_triangle_50"]
+    assert og.exact_weighted_triangle(50, True) == meta["naive"]["wiki_vote"]["at_least_one_triangle_50"]
+
+
+def test_known_answers(golden):
+    meta, _ = golden
+    kat = meta["kat"]
+    # tests/TestPattern2.cpp: unique vertex relabelings of the 4-chain, 4-clique and 5-star
+    chain4 = (4, [(0, 1), (1, 2), (2, 3)])
+    clique4 = (4, [(1, 0), (2, 0), (2, 1), (3, 0), (3, 1), (3, 2)])
+    got = []
+    for nv, edges in (chain4, clique4, STAR):
+        p = O.OracleProgram(Z.PROG_PATTERN, 0, (nv, edges))
+        fact = int(np.prod(np.arange(1, nv + 1)))
+        got.append("%d/%d" % (p.num_unique, fact))
+    assert got == kat["TestPattern2"]
+    # tests/TestRegression.cpp: k^2 of the fixed arrays
+    te = np.array([0.09, 0.26, 0.15, 0.42, 0.57, 0.10, 2.62]) / 100.0
+    ee = np.array([1, 2, 4, 8, 16, 32, 64], dtype=np.float64) / 100.0
+    k = O.regression_k(te, ee)
+    assert "%.4f" % (k * k) == kat["TestRegression"]
+    assert kat["TestSubgraph"].endswith("1<->2)")
+
+
+def test_elp_building_blocks(golden):
+    meta, _ = golden
+    for c in meta["elp"]["regression"]:
+        assert O.regression_k(np.array(c["x"]), np.array(c["y"])).hex() == c["k"]
+    for c in meta["elp"]["calculate_bound"]:
+        a = c["args"]
+        assert O.calculate_bound(a[0], a[1], a[2], a[3], a[4], int(a[5]), int(a[6])).hex() == c["bound"]
+    for c in meta["elp"]["estimation_fold"]:
+        e = Z.Estimation()
+        for n, v in zip(c["n"], c["v"]):
+            e.update(n, v)
+        assert e.get_currnet_estimation().hex() == c["r"]
+
+
+def test_philox_known_answers():
+    # Random123 known-answer vectors for philox4x32 with 10 rounds
+    assert O.philox([0, 0, 0, 0], [0, 0]) == [0x6627e8d5, 0xe169c58d, 0xbc57ac4c, 0x9b00dbd8]
+    assert O.philox([0xffffffff] * 4, [0xffffffff] * 2) == [0x408f276d, 0x41c83b0e, 0xa20bc7c6, 0x6d5451fd]
+    assert O.philox([0x243f6a88, 0x85a308d3, 0x13198a2e, 0x03707344], [0xa4093822, 0x299f31d0]) == \
+        [0xd16cfe09, 0x94fdcceb, 0x5001e420, 0x24126ea1]
+
+
+def test_x87_emulation_matches_long_double():
+    import ctypes
+    import platform
+    rng = np.random.default_rng(1)
+    for _ in range(2000):
+        k = int(rng.integers(1, 12))
+        f = rng.integers(1, 1 << 20, size=k).astype(np.float64)
+        f = 1.0 / f * rng.integers(1, 3, size=k)
+        got = O.ext_inv_product(f)
+        if platform.machine() in ("x86_64", "AMD64") and ctypes.sizeof(ctypes.c_longdouble) == 16:
+            p = np.longdouble(1.0)
+            for x in f:
+                p = p * np.longdouble(x)
+            assert got == float(np.longdouble(1.0) / p)
+        assert abs(got * np.prod(f) - 1.0) < 1e-12
