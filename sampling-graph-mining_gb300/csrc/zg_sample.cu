@@ -1026,23 +1026,23 @@ __global__ void __launch_bounds__(kBlock) k_finalize(const ZgPartial* __restrict
 // ---- host side ------------------------------------------------------------------------
 typedef unsigned __int128 u128;
 
-// 320-bit value -> correctly rounded double of value / 2^den / n.
+// 320-bit value -> correctly rounded double of value / 2^den / n: q = floor(value * 2^128 / n)
+// carries 128 fraction bits, the remainder is the sticky bit.
 double exact_mean(const uint64_t s[5], uint32_t den, uint64_t n) {
   if (n == 0) return 0.0;
-  uint64_t q[5];
+  uint64_t q[7];
+  uint64_t x[7] = {0, 0, s[0], s[1], s[2], s[3], s[4]};
   u128 rem = 0;
-  for (int i = 4; i >= 0; --i) {
-    u128 cur = (rem << 64) | s[i];
+  for (int i = 6; i >= 0; --i) {
+    u128 cur = (rem << 64) | x[i];
     q[i] = (uint64_t)(cur / n);
     rem = cur % n;
   }
+  den += 128;
   int top = -1;
-  for (int i = 4; i >= 0 && top < 0; --i)
+  for (int i = 6; i >= 0 && top < 0; --i)
     if (q[i]) top = i * 64 + 63 - __builtin_clzll(q[i]);
-  if (top < 0) {
-    // quotient < 1: scale the remainder fraction
-    return rem ? ldexp((double)rem / (double)n, -(int)den) : 0.0;
-  }
+  if (top < 0) return 0.0;  // below 2^-128 * 2^-den: no estimator weight is that small
   // take 64 bits from the top, sticky from everything below and the remainder
   auto bit = [&](int k) -> uint64_t { return k < 0 ? 0 : (q[k / 64] >> (k % 64)) & 1ull; };
   uint64_t mant = 0;

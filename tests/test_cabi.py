@@ -39,6 +39,26 @@ def test_version_and_errors_without_device():
     assert b"unknown program kind" in L.zg_last_error()
 
 
+def test_result_conversion_is_exact():
+    """zg_result_to_counters: carry-saved 32-bit lanes -> 320-bit sum -> mean rounded once."""
+    from fractions import Fraction
+    import struct
+    rng = np.random.default_rng(3)
+    p = Z.Program(Z.PROG_FOUR_CLIQUE)  # den_log2 = 2; no device memory needed
+    for trial in range(300):
+        n = int(rng.integers(1, 1 << 40))
+        bits = int(rng.integers(1, 50))
+        lanes = [int(x) for x in rng.integers(0, 1 << bits, size=8, dtype=np.uint64)]
+        if trial % 3 == 0:
+            lanes = [0] * 7 + [int(rng.integers(0, 4))]
+        blob = struct.pack("<4Q8Q2d", n, 5, 1, 0, *lanes, 1.5, 2.5)
+        c = p.result_to_counters(blob)
+        total = sum(v << (32 * i) for i, v in enumerate(lanes))
+        assert sum(int(c.sum_num[i]) << (64 * i) for i in range(5)) == total
+        assert c.estimate == float(Fraction(total, 4 * n))
+        assert (c.samples, c.hits, c.fails, c.sum_w, c.sum_w2) == (n, 5, 1, 1.5, 2.5)
+
+
 def test_generators_are_deterministic_and_simple():
     a = Z.gen_rmat(12, 8, seed=1)
     b = Z.gen_rmat(12, 8, seed=1)
