@@ -192,6 +192,20 @@ int zg_run(const zg_graph* g, const zg_program* p, uint64_t n, uint64_t first_sa
 int zg_run_async(const zg_graph* g, const zg_program* p, uint64_t n, uint64_t first_sample,
                  uint64_t seed, uint32_t stream_id, void* cuda_stream, void* d_result);
 int zg_result_to_counters(const void* h_result, const zg_program* p, zg_counters* out);
+
+/* zg_run_async that allocates nothing, for callers that cannot allocate device memory while they
+ * serve queries: a process whose memory manager reserves all device memory up front, or a
+ * latency-critical path where cudaMalloc/cudaFree could synchronise the device.  It has no
+ * counterpart in the reference.  The per-block scratch is one fixed device array of
+ * ZG_NOALLOC_MAX_BLOCKS x ZG_RESULT_BYTES bytes (448 KiB) that every GPU loading the library keeps
+ * until the process exits; a launch that would need more blocks is rejected with ZG_ERR_TOO_LARGE.
+ * The first call on each device looks up the array's device address (cudaGetSymbolAddress), so
+ * make that first call before any stream capture.  All calls share the array: calls whose
+ * executions overlap on the GPU race and must be serialised by the caller.  d_result: device
+ * memory of ZG_RESULT_BYTES bytes provided by the caller; read it as for zg_run_async. */
+#define ZG_NOALLOC_MAX_BLOCKS 4096
+int zg_run_noalloc(const zg_graph* g, const zg_program* p, uint64_t n, uint64_t first_sample,
+                   uint64_t seed, uint32_t stream_id, void* cuda_stream, void* d_result);
 /* As zg_run, one trace per sample (n <= 2^22). */
 int zg_run_debug(const zg_graph* g, const zg_program* p, uint64_t n, uint64_t first_sample,
                  uint64_t seed, uint32_t stream_id, zg_sample_trace* traces);

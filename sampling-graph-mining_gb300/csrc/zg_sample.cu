@@ -1168,6 +1168,17 @@ int launch_sample(const zg_graph* g, const zg_program* p, uint64_t n, uint64_t f
 // Shared by the allocation-free entry points of other translation units.
 int zg_sample_grid(int kind) { return grid_for_kind(kind); }
 
+// Enqueues the sampling and finalize kernels with caller-provided block scratch (grid blocks of
+// ZgPartial) and result slot; allocates nothing.
+int zg_launch_sample_with_scratch(const zg_graph* g, const zg_program* p, uint64_t n, uint64_t first, uint64_t seed,
+                                  uint32_t stream_id, cudaStream_t s, ZgPartial* scratch, int grid, void* d_result) {
+  launch_sample(g, p, n, first, seed, stream_id, s, scratch, grid);
+  k_finalize<<<1, kBlock, 0, s>>>(scratch, grid, (ZgPartial*)d_result);
+  cudaError_t ce = cudaGetLastError();
+  if (ce != cudaSuccess) return zg_check_cuda(ce, "sampling launch");
+  return ZG_OK;
+}
+
 extern "C" int zg_run(const zg_graph* g, const zg_program* p, uint64_t n, uint64_t first_sample, uint64_t seed,
                       uint32_t stream_id, void* cuda_stream, zg_counters* out) {
   int rc = validate_run(g, p);

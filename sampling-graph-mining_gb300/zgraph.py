@@ -100,6 +100,7 @@ def lib():
             "zg_run": ([P, P, U64, U64, U64, U32, P, C.POINTER(Counters)], I32),
             "zg_run_async": ([P, P, U64, U64, U64, U32, P, P], I32),
             "zg_result_to_counters": ([P, P, C.POINTER(Counters)], I32),
+            "zg_run_noalloc": ([P, P, U64, U64, U64, U32, P, P], I32),
             "zg_run_debug": ([P, P, U64, U64, U64, U32, P], I32),
             "zg_run_three_motif": ([P, U64, U64, U64, U32, U32, P, C.POINTER(Counters), C.POINTER(Counters)], I32),
             "zg_run_three_motif_debug": ([P, U64, U64, U64, U32, U32, P, P], I32),
