@@ -206,6 +206,17 @@ int zg_result_to_counters(const void* h_result, const zg_program* p, zg_counters
 #define ZG_NOALLOC_MAX_BLOCKS 4096
 int zg_run_noalloc(const zg_graph* g, const zg_program* p, uint64_t n, uint64_t first_sample,
                    uint64_t seed, uint32_t stream_id, void* cuda_stream, void* d_result);
+/* Autotuner (no counterpart in the reference, whose thread count comes from libnuma).  Each
+ * program kind has ZG_VARIANTS launch shapes: the sampling kernel compiled for
+ * min-blocks-per-SM 1, 2, 3, 4, 6, 8 (register caps 255/128/80/64/40/32) with a grid of
+ * occupancy x SM count.  zg_tune times every variant on g (probe_samples estimators, best of 3)
+ * and keeps the fastest for this device and kind; ms_per_variant (may be NULL) receives
+ * ZG_VARIANTS timings.  zg_set_variant / zg_get_variant fix or read the choice. */
+#define ZG_VARIANTS 6
+int zg_tune(const zg_graph* g, const zg_program* p, uint64_t probe_samples, void* cuda_stream,
+            int* best_variant, float* ms_per_variant);
+int zg_set_variant(int kind, int variant);
+int zg_get_variant(int kind, int* variant, int* min_blocks, int* grid);
 /* As zg_run, one trace per sample (n <= 2^22). */
 int zg_run_debug(const zg_graph* g, const zg_program* p, uint64_t n, uint64_t first_sample,
                  uint64_t seed, uint32_t stream_id, zg_sample_trace* traces);

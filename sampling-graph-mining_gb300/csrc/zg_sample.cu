@@ -704,8 +704,9 @@ __device__ void prog_pattern(const ZgDevGraph& g, const ZgProgParams& pp, Ctx& c
 }
 
 // ---- per-thread exact accumulation and block reduction ----------------------------------
+// Per-thread state kept small: one thread handles < 2^32 estimators, so 32-bit counters.
 struct Acc {
-  unsigned long long samples, hits, fails, ovf;
+  uint32_t samples, hits, fails, ovf;
   uint64_t s[4];
   double sw, sw2;
 };
@@ -808,9 +809,10 @@ __device__ __forceinline__ void run_program(const ZgDevGraph& g, const ZgProgPar
   }
 }
 
-// Production kernels: one specialisation per program so each has its own register budget.
-template <int KIND>
-__global__ void __launch_bounds__(kBlock) k_sample(ZgDevGraph g, ZgProgParams pp, uint64_t n, uint64_t first,
+// Production kernels: one specialisation per program and per register budget (MINB resident
+// blocks of 256 threads requested from the compiler); zg_tune picks the fastest per program.
+template <int KIND, int MINB>
+__global__ void __launch_bounds__(kBlock, MINB) k_sample(ZgDevGraph g, ZgProgParams pp, uint64_t n, uint64_t first,
                                                    uint64_t seed, uint32_t stream, ZgPartial* __restrict__ partials) {
   Acc a;
   acc_init(a);
@@ -1114,53 +1116,87 @@ int grid_of(K kernel) {
   return per_sm * zg_num_sms();
 }
 
-int grid_for_kind(int kind) {
-  static int cache[8] = {0};
-  static std::mutex mu;
-  std::lock_guard<std::mutex> lk(mu);
-  if (kind < 0 || kind >= 8) kind = ZG_PROG_PATTERN;
-  if (!cache[kind]) {
-    switch (kind) {
-      case ZG_PROG_TRIANGLE: cache[kind] = grid_of(k_sample<ZG_PROG_TRIANGLE>); break;
-      case ZG_PROG_FOUR_CLIQUE: cache[kind] = grid_of(k_sample<ZG_PROG_FOUR_CLIQUE>); break;
-      case ZG_PROG_THREE_CHAIN: cache[kind] = grid_of(k_sample<ZG_PROG_THREE_CHAIN>); break;
-      case ZG_PROG_FOUR_CHAIN: cache[kind] = grid_of(k_sample<ZG_PROG_FOUR_CHAIN>); break;
-      case ZG_PROG_CHAIN: cache[kind] = grid_of(k_sample<ZG_PROG_CHAIN>); break;
-      default: cache[kind] = grid_of(k_sample<ZG_PROG_PATTERN>); break;
-    }
+// Launch-shape variants: __launch_bounds__ min-blocks (register caps 255/128/80/64/40/32).
+constexpr int kVariants = 6;
+constexpr int kMinBlocks[kVariants] = {1, 2, 3, 4, 6, 8};
+typedef void (*SampleKernel)(ZgDevGraph, ZgProgParams, uint64_t, uint64_t, uint64_t, uint32_t, ZgPartial*);
+
+template <int KIND>
+SampleKernel kernel_variant(int v) {
+  switch (v) {
+    case 0: return k_sample<KIND, 1>;
+    case 1: return k_sample<KIND, 2>;
+    case 2: return k_sample<KIND, 3>;
+    case 3: return k_sample<KIND, 4>;
+    case 4: return k_sample<KIND, 6>;
+    default: return k_sample<KIND, 8>;
   }
-  return cache[kind];
 }
+
+SampleKernel kernel_for(int kind, int v) {
+  switch (kind) {
+    case ZG_PROG_TRIANGLE: return kernel_variant<ZG_PROG_TRIANGLE>(v);
+    case ZG_PROG_FOUR_CLIQUE: return kernel_variant<ZG_PROG_FOUR_CLIQUE>(v);
+    case ZG_PROG_THREE_CHAIN: return kernel_variant<ZG_PROG_THREE_CHAIN>(v);
+    case ZG_PROG_FOUR_CHAIN: return kernel_variant<ZG_PROG_FOUR_CHAIN>(v);
+    case ZG_PROG_CHAIN: return kernel_variant<ZG_PROG_CHAIN>(v);
+    default: return kernel_variant<ZG_PROG_PATTERN>(v);
+  }
+}
+
+// Per device: the variant each program kind uses and its occupancy grid.
+constexpr int kMaxDev = 64;
+std::mutex g_tune_mu;
+int g_variant[kMaxDev][8];
+int g_grid[kMaxDev][8][kVariants];
+bool g_tune_init[kMaxDev];
+// Defaults before tuning (register footprints measured with -Xptxas -v).
+constexpr int kDefaultVariant[8] = {3, 3, 2, 3, 2, 3, 3, 3};
+
+int current_device() {
+  int d = 0;
+  cudaGetDevice(&d);
+  return (d >= 0 && d < kMaxDev) ? d : 0;
+}
+
+int kind_slot(int kind) { return (kind >= 0 && kind < 8) ? kind : ZG_PROG_PATTERN; }
+
+int variant_for(int kind) {
+  int d = current_device();
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  if (!g_tune_init[d]) {
+    for (int k = 0; k < 8; ++k) g_variant[d][k] = kDefaultVariant[k];
+    g_tune_init[d] = true;
+  }
+  return g_variant[d][kind_slot(kind)];
+}
+
+int grid_for_variant(int kind, int v) {
+  int d = current_device();
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  int& g = g_grid[d][kind_slot(kind)][v];
+  if (!g) g = grid_of(kernel_for(kind, v));
+  return g;
+}
+
+int grid_for_kind(int kind) { return grid_for_variant(kind, variant_for(kind)); }
 
 int validate_run(const zg_graph* g, const zg_program* p) {
   if (!g || !p) return zg_set_error(ZG_ERR_INVALID_ARG, "null graph or program"), ZG_ERR_INVALID_ARG;
   return ZG_OK;
 }
 
+int launch_variant(const zg_graph* g, const zg_program* p, int v, uint64_t n, uint64_t first, uint64_t seed,
+                   uint32_t stream_id, cudaStream_t s, ZgPartial* parts, int grid) {
+  ZgProgParams pp = params_for(p);
+  SampleKernel k = kernel_for(p->kind, v);
+  k<<<grid, kBlock, 0, s>>>(g->d, pp, n, first, seed, stream_id, parts);
+  return ZG_OK;
+}
+
 int launch_sample(const zg_graph* g, const zg_program* p, uint64_t n, uint64_t first, uint64_t seed,
                   uint32_t stream_id, cudaStream_t s, ZgPartial* parts, int grid) {
-  ZgProgParams pp = params_for(p);
-  switch (p->kind) {
-    case ZG_PROG_TRIANGLE:
-      k_sample<ZG_PROG_TRIANGLE><<<grid, kBlock, 0, s>>>(g->d, pp, n, first, seed, stream_id, parts);
-      break;
-    case ZG_PROG_FOUR_CLIQUE:
-      k_sample<ZG_PROG_FOUR_CLIQUE><<<grid, kBlock, 0, s>>>(g->d, pp, n, first, seed, stream_id, parts);
-      break;
-    case ZG_PROG_THREE_CHAIN:
-      k_sample<ZG_PROG_THREE_CHAIN><<<grid, kBlock, 0, s>>>(g->d, pp, n, first, seed, stream_id, parts);
-      break;
-    case ZG_PROG_FOUR_CHAIN:
-      k_sample<ZG_PROG_FOUR_CHAIN><<<grid, kBlock, 0, s>>>(g->d, pp, n, first, seed, stream_id, parts);
-      break;
-    case ZG_PROG_CHAIN:
-      k_sample<ZG_PROG_CHAIN><<<grid, kBlock, 0, s>>>(g->d, pp, n, first, seed, stream_id, parts);
-      break;
-    default:
-      k_sample<ZG_PROG_PATTERN><<<grid, kBlock, 0, s>>>(g->d, pp, n, first, seed, stream_id, parts);
-      break;
-  }
-  return ZG_OK;
+  return launch_variant(g, p, variant_for(p->kind), n, first, seed, stream_id, s, parts, grid);
 }
 
 }  // namespace
@@ -1220,6 +1256,83 @@ extern "C" int zg_run_async(const zg_graph* g, const zg_program* p, uint64_t n, 
   cudaFreeAsync(parts, s);
   cudaError_t ce = cudaGetLastError();
   if (ce != cudaSuccess) return zg_check_cuda(ce, "zg_run_async");
+  return ZG_OK;
+}
+
+extern "C" int zg_set_variant(int kind, int variant) {
+  if (variant < 0 || variant >= kVariants)
+    return zg_set_error(ZG_ERR_INVALID_ARG, "launch variant %d outside [0, %d)", variant, kVariants), ZG_ERR_INVALID_ARG;
+  if (kind < ZG_PROG_TRIANGLE || kind > ZG_PROG_PATTERN)
+    return zg_set_error(ZG_ERR_INVALID_ARG, "unknown program kind %d", kind), ZG_ERR_INVALID_ARG;
+  variant_for(kind);  // initialise the table
+  int d = current_device();
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_variant[d][kind] = variant;
+  return ZG_OK;
+}
+
+extern "C" int zg_get_variant(int kind, int* variant, int* min_blocks, int* grid) {
+  if (kind < ZG_PROG_TRIANGLE || kind > ZG_PROG_PATTERN)
+    return zg_set_error(ZG_ERR_INVALID_ARG, "unknown program kind %d", kind), ZG_ERR_INVALID_ARG;
+  int v = variant_for(kind);
+  if (variant) *variant = v;
+  if (min_blocks) *min_blocks = kMinBlocks[v];
+  if (grid) *grid = grid_for_variant(kind, v);
+  return ZG_OK;
+}
+
+// Autotuner: times every launch variant of p's kernel on g (probe_samples estimators each, best
+// of `reps`, CUDA events on cuda_stream) and keeps the fastest for this device and program kind.
+extern "C" int zg_tune(const zg_graph* g, const zg_program* p, uint64_t probe_samples, void* cuda_stream,
+                       int* best_variant, float* ms_per_variant) {
+  int rc = validate_run(g, p);
+  if (rc) return rc;
+  if (probe_samples == 0) probe_samples = 1ull << 22;
+  cudaStream_t s = (cudaStream_t)cuda_stream;
+  int grid_max = 0;
+  for (int v = 0; v < kVariants; ++v) grid_max = std::max(grid_max, grid_for_variant(p->kind, v));
+  ZgPartial* parts = nullptr;
+  ZG_CUDA(cudaMallocAsync((void**)&parts, sizeof(ZgPartial) * (grid_max + 1), s));
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  int bestv = variant_for(p->kind);
+  const int reps = 3;
+  cudaError_t ce = cudaSuccess;
+  for (int v = 0; v < kVariants && ce == cudaSuccess; ++v) {
+    int grid = grid_for_variant(p->kind, v);
+    uint64_t maxg = (probe_samples + kBlock - 1) / kBlock;
+    if ((uint64_t)grid > maxg) grid = (int)maxg;
+    float vbest = 1e30f;
+    launch_variant(g, p, v, probe_samples, 0, 1, 0, s, parts, grid);  // warm
+    for (int r = 0; r < reps; ++r) {
+      cudaEventRecord(e0, s);
+      launch_variant(g, p, v, probe_samples, (uint64_t)(r + 1) * probe_samples, 1, 0, s, parts, grid);
+      cudaEventRecord(e1, s);
+      ce = cudaEventSynchronize(e1);
+      float ms = 0;
+      cudaEventElapsedTime(&ms, e0, e1);
+      vbest = std::min(vbest, ms);
+    }
+    if (ms_per_variant) ms_per_variant[v] = vbest;
+    if (vbest < best) {
+      best = vbest;
+      bestv = v;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFreeAsync(parts, s);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
+  if (ce == cudaSuccess) ce = cudaGetLastError();
+  if (ce != cudaSuccess) return zg_check_cuda(ce, "zg_tune");
+  {
+    int d = current_device();
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_variant[d][kind_slot(p->kind)] = bestv;
+  }
+  if (best_variant) *best_variant = bestv;
   return ZG_OK;
 }
 

@@ -101,6 +101,9 @@ def lib():
             "zg_run_async": ([P, P, U64, U64, U64, U32, P, P], I32),
             "zg_result_to_counters": ([P, P, C.POINTER(Counters)], I32),
             "zg_run_noalloc": ([P, P, U64, U64, U64, U32, P, P], I32),
+            "zg_tune": ([P, P, U64, P, C.POINTER(I32), P], I32),
+            "zg_set_variant": ([I32, I32], I32),
+            "zg_get_variant": ([I32, C.POINTER(I32), C.POINTER(I32), C.POINTER(I32)], I32),
             "zg_run_debug": ([P, P, U64, U64, U64, U32, P], I32),
             "zg_run_three_motif": ([P, U64, U64, U64, U32, U32, P, C.POINTER(Counters), C.POINTER(Counters)], I32),
             "zg_run_three_motif_debug": ([P, U64, U64, U64, U32, U32, P, P], I32),
@@ -314,6 +317,18 @@ class Program:
         buf = (C.c_char * len(host_bytes)).from_buffer_copy(host_bytes)
         check(lib().zg_result_to_counters(buf, self._h, C.byref(out)))
         return out
+
+    def tune(self, graph, probe_samples=1 << 22, cuda_stream=None):
+        """zg_tune: time every launch variant on graph, keep the fastest; returns (best, ms list)."""
+        best = C.c_int(0)
+        ms = (C.c_float * 8)()
+        check(lib().zg_tune(graph.handle, self._h, probe_samples, cuda_stream, C.byref(best), ms))
+        return best.value, [float(ms[i]) for i in range(6)]
+
+    def variant(self):
+        v, mb, g = C.c_int(), C.c_int(), C.c_int()
+        check(lib().zg_get_variant(self.kind, C.byref(v), C.byref(mb), C.byref(g)))
+        return {"variant": v.value, "min_blocks": mb.value, "grid": g.value}
 
     def run_debug(self, graph, n, seed, stream_id=0, first_sample=0):
         tr = np.zeros(n, dtype=TRACE_DTYPE)

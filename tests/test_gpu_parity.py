@@ -245,3 +245,22 @@ def test_determinism_and_additivity(graphs):
     h2 = p.run(g, (1 << 18) - 100000, 5, first_sample=100000)
     assert h1.exact_sum() + h2.exact_sum() == a.exact_sum()
     assert h1.hits + h2.hits == a.hits
+
+
+@pytest.mark.parametrize("name,kind,param,pattern", PROGRAMS[:9], ids=[p[0] for p in PROGRAMS[:9]])
+def test_launch_variants_agree(graphs, name, kind, param, pattern):
+    """Every launch shape (register cap / grid) gives the same exact sums; zg_tune keeps one."""
+    L = Z.lib()
+    e, nv = graphs["rmat12"]
+    g = Z.Graph.from_edges(e, nv)
+    p = Z.Program(kind, param, pattern)
+    base = None
+    for v in range(6):
+        Z.check(L.zg_set_variant(kind, v))
+        c = p.run(g, 1 << 19, 123)
+        got = (c.samples, c.hits, c.fails, _sums(c))
+        assert base is None or got == base, (name, v)
+        base = got
+    best, ms = p.tune(g, 1 << 18)
+    assert 0 <= best < 6 and all(t > 0 for t in ms)
+    assert p.variant()["variant"] == best
