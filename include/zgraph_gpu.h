@@ -230,6 +230,74 @@ int zg_run_three_motif_debug(const zg_graph* g, uint64_t n_chain, uint64_t n_tri
                              uint64_t seed, uint32_t stream_chain, uint32_t stream_tri,
                              zg_sample_trace* chain_traces, zg_sample_trace* tri_traces);
 
+/* ---- error-latency profiles and bounded queries ------------------------------ */
+/* Draw plan of zg_elp_plain for a given seed: the subsample keeps edge e iff
+ * zg_draw(seed + ZG_ELP_KEEP_OFFSET, subsample stream, e) <= 0.1 * 2^30 and is permuted with
+ * seed + ZG_ELP_SHUFFLE_OFFSET; a predicate filter on it uses seed + ZG_ELP_FILTER_OFFSET; the
+ * 2^14 x 16 grouped estimators take sample indices [0, 2^18) and the 2^23 follow-up estimators
+ * [2^18, 2^18 + 2^23), all on stream ZG_ELP_STREAM. */
+#define ZG_ELP_KEEP_OFFSET    1
+#define ZG_ELP_SHUFFLE_OFFSET 2
+#define ZG_ELP_FILTER_OFFSET  3
+#define ZG_ELP_STREAM         0x454C5000u
+
+typedef struct zg_elp_result {
+  uint64_t n_required;        /* (unsigned long long) of the bound, as get_num_estimators returns */
+  double   n_required_f;
+  double   K;                 /* regression slope (src/Regression.cpp:17-28) */
+  double   estimate_sampled;  /* estimate on the 10 % subsample */
+  double   big_estimate;      /* mean of the 2^23 follow-up estimators */
+  double   rough_estimate;    /* estimate_sampled / 0.1^(nse + ncse) */
+  double   nse, ncse;         /* sample_edge / conditional_sample_edge calls per estimate */
+  uint64_t sampled_edges, sampled_max_degree;
+  double   profile_ms;        /* wall time of the whole profile */
+} zg_elp_result;
+
+/* ErrorProfile<E>::calculate_bound (src/ErrorLatencyProfile.cpp:52-59). */
+double zg_calculate_bound(double epsilon, double delta, double nse, double ncse, double estimation,
+                          uint64_t max_degree, uint64_t num_edges);
+/* Standard normal quantile (Acklam's approximation, one Halley refinement). */
+double zg_normal_quantile(double p);
+/* n_groups consecutive groups of group_size estimators: per-group mean of estimate() summed in
+ * sample order in double, what a one-threaded calculate(group_size) returns
+ * (src/ZGraphInstance.cpp:273-292).  group_estimates: host array of n_groups. */
+int zg_run_groups(const zg_graph* g, const zg_program* p, uint64_t n_groups, uint32_t group_size,
+                  uint64_t first_sample, uint64_t seed, uint32_t stream_id, void* cuda_stream,
+                  double* group_estimates);
+/* The host half of ErrorProfile::get_num_estimators (src/ErrorLatencyProfile.cpp:115-206). */
+int zg_elp_solve(const double* group_estimates, uint64_t n_groups, uint32_t group_size,
+                 double big_estimate, uint64_t big_n, double nse, double ncse, uint64_t sampled_m,
+                 uint64_t sampled_max_degree, uint64_t orig_m, uint64_t orig_max_degree, double eps,
+                 double conf, zg_elp_result* out);
+/* ErrorProfile<E>::get_num_estimators (src/ErrorLatencyProfile.cpp:72-207) on the device.
+ * pred_op != 0 profiles an AllPredicate instance: the predicate filters the subsample, as
+ * AllPredicateZGraphInstance::set_graph does (src/ZGraphInstance.cpp:514-520).
+ * group_estimates (may be NULL) receives the 2^14 group means. */
+int zg_elp_plain(const zg_graph* g, const zg_program* p, int pred_op, int64_t t0, int64_t t1,
+                 double error, double confidence, uint64_t seed, void* cuda_stream,
+                 zg_elp_result* out, double* group_estimates);
+/* TimeProfile<E>::run (src/ErrorLatencyProfile.cpp:25-47): doubling calculate() calls from 64
+ * estimators while the next one fits the budget, then a final call sized to the remaining time. */
+int zg_time_profile(const zg_graph* g, const zg_program* p, uint32_t time_limit_ms, uint64_t seed,
+                    uint32_t stream_id, void* cuda_stream, double* estimate, uint64_t* samples_used);
+
+typedef struct zg_query_result {
+  double   estimate;          /* exact mean over all samples taken */
+  double   half_width;        /* z * sqrt(var / n) at the requested confidence */
+  double   rel_half_width;
+  uint64_t samples, hits;
+  uint32_t bound_met, rounds;
+  uint64_t n_sized;           /* the initial budget */
+  double   ms_total;
+} zg_query_result;
+/* A bounded query (no counterpart in the reference, whose ErrorProfile::run trusts its bound):
+ * run n_initial estimators, judge the answer by its empirical CLT half-width, and keep sampling
+ * fresh estimators until half_width <= error * estimate with at least 30 hits, or max_samples
+ * (0: 2^40) is reached (then bound_met = 0). */
+int zg_query(const zg_graph* g, const zg_program* p, double error, double confidence,
+             uint64_t n_initial, uint64_t max_samples, uint64_t seed, uint32_t stream_id,
+             void* cuda_stream, zg_query_result* out);
+
 /* ---- exact counts ---------------------------------------------------------- */
 /* out[0..1]: 128-bit little-endian count.  kind: ZG_EXACT_*. */
 int zg_exact_count(const zg_graph* g, int kind, void* cuda_stream, uint64_t out[2]);

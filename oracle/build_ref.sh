@@ -27,6 +27,7 @@ for f in Bitmap Debug ErrorLatencyProfile Graph GraphFilters NetworkInterface Re
   $CXX $FLAGS $INC -c "$REF/src/$f.cpp" -o "$OUT/obj/$f.o" &
 done
 $CXX $FLAGS $INC -c "$HERE/ref/replay_random.cpp" -o "$OUT/obj/replay_random.o" &
+${CC:-gcc} -O2 -fopenmp -fPIC -fvisibility=hidden -c "$HERE/zg_oracle.c" -o "$OUT/obj/zg_oracle.o" &
 wait
 
 for app in triangle four_clique three_chain four_chain chain pred_triangle three_motif pattern; do

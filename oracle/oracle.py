@@ -261,6 +261,8 @@ def ref_lib(app):
         if app == "three_motif":
             L.zgref_motif.argtypes = [P, U64, U32, U64, U64, P, P, C.POINTER(D), C.POINTER(D)]
             L.zgref_motif.restype = U64
+        L.zgref_elp.argtypes = [P, U64, U32, C.c_int, U32, P, U32, U32, U64, U32, D, D, C.POINTER(U64)]
+        L.zgref_elp.restype = U64
         if app == "pattern":
             L.zgref_regression_k.argtypes = [P, P, U32]
             L.zgref_regression_k.restype = D
@@ -309,6 +311,22 @@ class RefInstance:
             self.close()
         except Exception:
             pass
+
+
+def ref_elp(app, edges, num_vertices, kind, param=0, pattern=None, seed=1, probe_stream=0x50524F42, eps=0.05,
+            conf=0.95):
+    """The reference's ErrorProfile::get_num_estimators, replaying the zg_elp_plain draw plan."""
+    L = ref_lib(app)
+    e = np.ascontiguousarray(edges, dtype=np.uint32).reshape(-1, 2)
+    pv, pe, pedges = 0, 0, None
+    if pattern is not None:
+        pv, pedges = pattern
+        pedges = np.ascontiguousarray(pedges, dtype=np.uint32).reshape(-1, 2)
+        pe = pedges.shape[0]
+    bad = C.c_uint64(0)
+    n = L.zgref_elp(_p(e), e.shape[0], num_vertices, kind, param, _p(pedges), pv, pe, seed, probe_stream, eps, conf,
+                    C.byref(bad))
+    return int(n), int(bad.value)
 
 
 def ref_motif(edges, num_vertices, n_chain, n_tri, chain_tr, tri_tr):

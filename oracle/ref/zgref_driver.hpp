@@ -21,8 +21,10 @@
 #include "NetworkInterface.hpp"
 #include "SharedMemSys.hpp"
 #include "ZGraphInstance.hpp"
+#include "ErrorLatencyProfile.hpp"
 #include "zgref_replay.hpp"
 #include "../../include/zgraph_gpu.h"
+#include "../zg_oracle.h"
 
 #define ZGREF_API extern "C" __attribute__((visibility("default")))
 
@@ -132,6 +134,94 @@ ZGREF_API double zgref_calculate(void* hv, uint64_t n, uint32_t k, const zg_samp
   *bad = zgref_replay.mismatches + zgref_replay.overruns + zgref_replay.q.size();
   zgref_replay.q.clear();
   return r;
+}
+
+/* ErrorProfile<E>::get_num_estimators run by the reference itself, its Random replaying, in the
+ * order the reference consumes them: 1024 probe estimators on the original graph (oracle stream
+ * probe_stream), one keep draw per edge for GraphSampler, the shuffle of the kept edges, then the
+ * 2^14 x 16 + 2^23 estimators on the subsample (oracle, stream ZG_ELP_STREAM, indices from 0) —
+ * the draw plan of zg_elp_plain.  Returns n_required; *bad counts replay mismatches. */
+ZGREF_API void zgref_close(void* hv);
+
+struct ZgrefElpFeed {
+  const zgo_graph* orig;
+  zgo_graph sub;
+  zgo_program prog;
+  uint64_t seed, m, next_probe, next_keep, next_sample, total_samples;
+  uint32_t probe_stream;
+};
+
+static bool zgref_elp_refill(void* vctx) {
+  ZgrefElpFeed* f = (ZgrefElpFeed*)vctx;
+  zg_sample_trace t;
+  if (f->next_probe < 1024) {
+    for (int k = 0; k < 256 && f->next_probe < 1024; ++k, ++f->next_probe) {
+      zgo_sample(f->orig, &f->prog, f->seed, f->probe_stream, f->next_probe, &t);
+      zgref_queue(t);
+    }
+    return true;
+  }
+  if (f->next_keep < f->m) {
+    for (int k = 0; k < 65536 && f->next_keep < f->m; ++k, ++f->next_keep) {
+      uint64_t v = zgo_draw(f->seed + ZG_ELP_KEEP_OFFSET, 0xFFFFFFF1u, f->next_keep, 0, 1, 1ull << 30);
+      zgref_replay.q.push_back(ZgrefDraw{1, 1ull << 30, v});
+    }
+    return true;
+  }
+  if (f->next_sample < f->total_samples) {
+    for (int k = 0; k < 4096 && f->next_sample < f->total_samples; ++k, ++f->next_sample) {
+      zgo_sample(&f->sub, &f->prog, f->seed, ZG_ELP_STREAM, f->next_sample, &t);
+      zgref_queue(t);
+    }
+    return true;
+  }
+  return false;
+}
+
+ZGREF_API uint64_t zgref_elp(const uint32_t* edges, uint64_t m, uint32_t nv, int kind, uint32_t param,
+                             const uint32_t* pattern, uint32_t pv, uint32_t pe, uint64_t seed, uint32_t probe_stream,
+                             double eps, double conf, uint64_t* bad) {
+  zgref_boot();
+  ZgrefHandle* h = (ZgrefHandle*)zgref_open(edges, m, nv, nullptr, param, nullptr, 0, pattern, pv, pe);
+  ZgrefElpFeed f;
+  zgo_graph orig;
+  zgo_graph_build(&orig, nv, m, edges, nullptr);
+  f.orig = &orig;
+  zgo_program_init(&f.prog, kind, param, pv, pe, pattern);
+  f.seed = seed;
+  f.m = m;
+  f.probe_stream = probe_stream;
+  f.next_probe = f.next_keep = f.next_sample = 0;
+  f.total_samples = (1ull << 18) + (1ull << 23);
+  // the subsample our device builds: kept edges in order, then permuted
+  std::vector<uint64_t> kept;
+  for (uint64_t e = 0; e < m; ++e)
+    if (zgo_subsample_keep(0.1, seed + ZG_ELP_KEEP_OFFSET, e)) kept.push_back(e);
+  std::vector<uint64_t> perm(kept.size() ? kept.size() : 1);
+  zgo_shuffle_perm(kept.size(), seed + ZG_ELP_SHUFFLE_OFFSET, perm.data());
+  std::vector<uint32_t> sub_edges(2 * kept.size());
+  for (size_t i = 0; i < kept.size(); ++i) {
+    sub_edges[2 * i] = edges[2 * kept[perm[i]]];
+    sub_edges[2 * i + 1] = edges[2 * kept[perm[i]] + 1];
+  }
+  zgo_graph_build(&f.sub, nv, kept.size(), sub_edges.data(), nullptr);
+  zgref_replay.q.clear();
+  zgref_replay.reset_counts();
+  zgref_replay.raw_script = zgref_shuffle_script(perm.data(), kept.size());
+  zgref_replay.raw_pos = 0;
+  zgref_replay.refill = zgref_elp_refill;
+  zgref_replay.refill_ctx = &f;
+  ErrorProfile<ZGREF_E> ep;
+  unsigned long long n = ep.get_num_estimators(*h->inst, 3, eps, conf);
+  *bad = zgref_replay.mismatches + zgref_replay.overruns + zgref_replay.q.size() + zgref_replay.raw_overruns +
+         (f.next_sample != f.total_samples);
+  zgref_replay.refill = nullptr;
+  zgref_replay.q.clear();
+  zgo_graph_free(&f.sub);
+  zgo_graph_free(&orig);
+  zgo_program_free(&f.prog);
+  zgref_close(h);
+  return n;
 }
 
 ZGREF_API void zgref_close(void* hv) {

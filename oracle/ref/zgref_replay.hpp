@@ -23,6 +23,10 @@ struct ZgrefReplay {
   uint64_t overruns = 0;   /* a draw was requested beyond the queue */
   uint64_t raw_overruns = 0;
 
+  /* Called when q runs dry; appends the next draws and returns false when there are none. */
+  bool (*refill)(void*) = nullptr;
+  void* refill_ctx = nullptr;
+
   void reset_counts() { consumed = mismatches = overruns = raw_overruns = 0; }
   uint64_t raw() {
     if (raw_pos < raw_script.size()) return raw_script[raw_pos++];
@@ -30,6 +34,7 @@ struct ZgrefReplay {
     return 0;
   }
   uint64_t range(uint64_t lo, uint64_t hi) {
+    if (q.empty() && refill) refill(refill_ctx);
     if (q.empty()) { ++overruns; return lo; }
     ZgrefDraw d = q.front();
     q.pop_front();

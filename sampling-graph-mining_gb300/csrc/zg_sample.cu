@@ -858,6 +858,27 @@ __global__ void __launch_bounds__(kBlock) k_sample_debug(ZgDevGraph g, ZgProgPar
   block_reduce_store<kBlock>(a, &partials[blockIdx.x]);
 }
 
+// ---- grouped runs for the error-latency profile ------------------------------------------
+// Group gi = samples [first + gi*group, first + (gi+1)*group): the mean of estimate() summed in
+// sample order in double and divided by the group size, which is what one-threaded
+// calculate(group) returns (src/ZGraphInstance.cpp:273-292).
+__global__ void __launch_bounds__(kBlock) k_groups(ZgDevGraph g, ZgProgParams pp, uint64_t n_groups, uint32_t group,
+                                                   uint64_t first, uint64_t seed, uint32_t stream,
+                                                   double* __restrict__ out) {
+  for (uint64_t gi = blockIdx.x * (uint64_t)kBlock + threadIdx.x; gi < n_groups;
+       gi += (uint64_t)gridDim.x * kBlock) {
+    double acc = 0.0;
+    for (uint32_t j = 0; j < group; ++j) {
+      Ctx c{seed, first + gi * group + j, stream, 0, nullptr, 0};
+      Res r;
+      res_init(r);
+      run_program<true>(g, pp, c, r);
+      acc = __dadd_rn(acc, r.hit ? r.w : 0.0);
+    }
+    out[gi] = __ddiv_rn(acc, u2d(group));
+  }
+}
+
 // ---- ThreeMotif: applications/ThreeMotif.cpp:48-121 with the sub-pattern cache ---------
 template <bool DBG>
 __global__ void __launch_bounds__(kBlock) k_three_motif(ZgDevGraph g, uint64_t n_chain, uint64_t n_tri, uint64_t seed,
@@ -1201,8 +1222,23 @@ int launch_sample(const zg_graph* g, const zg_program* p, uint64_t n, uint64_t f
 
 }  // namespace
 
+// The exact mean of a 320-bit sum, for other translation units.
+double zg_exact_mean_host(const uint64_t s[5], uint32_t den, uint64_t n) { return exact_mean(s, den, n); }
+
 // Shared by the allocation-free entry points of other translation units.
 int zg_sample_grid(int kind) { return grid_for_kind(kind); }
+
+// Per-group estimates (device array out[n_groups]) on stream s.
+int zg_launch_groups(const zg_graph* g, const zg_program* p, uint64_t n_groups, uint32_t group, uint64_t first,
+                     uint64_t seed, uint32_t stream_id, cudaStream_t s, double* out) {
+  ZgProgParams pp = params_for(p);
+  uint64_t blocks = (n_groups + kBlock - 1) / kBlock;
+  int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(blocks, (uint64_t)zg_num_sms() * 8));
+  k_groups<<<grid, kBlock, 0, s>>>(g->d, pp, n_groups, group, first, seed, stream_id, out);
+  cudaError_t ce = cudaGetLastError();
+  if (ce != cudaSuccess) return zg_check_cuda(ce, "grouped run");
+  return ZG_OK;
+}
 
 // Enqueues the sampling and finalize kernels with caller-provided block scratch (grid blocks of
 // ZgPartial) and result slot; allocates nothing.

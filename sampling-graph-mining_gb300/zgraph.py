@@ -65,6 +65,21 @@ class Counters(C.Structure):
                 "sum_w2": self.sum_w2, "estimate": self.estimate}
 
 
+class ElpResult(C.Structure):
+    _fields_ = [("n_required", C.c_uint64), ("n_required_f", C.c_double), ("K", C.c_double),
+                ("estimate_sampled", C.c_double), ("big_estimate", C.c_double), ("rough_estimate", C.c_double),
+                ("nse", C.c_double), ("ncse", C.c_double), ("sampled_edges", C.c_uint64),
+                ("sampled_max_degree", C.c_uint64), ("profile_ms", C.c_double)]
+
+
+class QueryResult(C.Structure):
+    _fields_ = [("estimate", C.c_double), ("half_width", C.c_double), ("rel_half_width", C.c_double),
+                ("samples", C.c_uint64), ("hits", C.c_uint64), ("bound_met", C.c_uint32), ("rounds", C.c_uint32),
+                ("n_sized", C.c_uint64), ("ms_total", C.c_double)]
+
+
+ELP_KEEP_OFFSET, ELP_SHUFFLE_OFFSET, ELP_FILTER_OFFSET, ELP_STREAM = 1, 2, 3, 0x454C5000
+
 TRACE_DTYPE = np.dtype([("ndraws", "<u4"), ("hit", "<u4"), ("fail", "<u4"), ("shift", "<u4"),
                         ("sectors", "<u4"), ("reserved", "<u4"), ("w", "<f8"), ("num", "<u8", (3,)), ("lo", "<u8", (MAX_DRAWS,)),
                         ("hi", "<u8", (MAX_DRAWS,)), ("val", "<u8", (MAX_DRAWS,))])
@@ -108,6 +123,13 @@ def lib():
             "zg_run_three_motif": ([P, U64, U64, U64, U32, U32, P, C.POINTER(Counters), C.POINTER(Counters)], I32),
             "zg_run_three_motif_debug": ([P, U64, U64, U64, U32, U32, P, P], I32),
             "zg_exact_count": ([P, I32, P, P], I32),
+            "zg_calculate_bound": ([D, D, D, D, D, U64, U64], D),
+            "zg_normal_quantile": ([D], D),
+            "zg_run_groups": ([P, P, U64, U32, U64, U64, U32, P, P], I32),
+            "zg_elp_solve": ([P, U64, U32, D, U64, D, D, U64, U64, U64, U64, D, D, C.POINTER(ElpResult)], I32),
+            "zg_elp_plain": ([P, P, I32, I64, I64, D, D, U64, P, C.POINTER(ElpResult), P], I32),
+            "zg_time_profile": ([P, P, U32, U64, U32, P, C.POINTER(D), C.POINTER(U64)], I32),
+            "zg_query": ([P, P, D, D, U64, U64, U64, U32, P, C.POINTER(QueryResult)], I32),
             "zg_gen_rmat": ([U32, U32, D, D, D, U64, U64, P, C.POINTER(U64)], I32),
             "zg_gen_chung_lu": ([U32, D, D, U64, U64, P, C.POINTER(U64)], I32),
             "zg_gen_weights": ([U64, U32, U64, P], I32),
@@ -342,6 +364,50 @@ class Program:
                 self._h = None
         except Exception:
             pass
+
+
+def elp_solve(groups, group_size, big_estimate, big_n, nse, ncse, sampled_m, sampled_max_degree, orig_m,
+              orig_max_degree, eps, conf):
+    """zg_elp_solve: the host half of ErrorProfile::get_num_estimators (no GPU needed)."""
+    g = np.ascontiguousarray(groups, dtype=np.float64)
+    out = ElpResult()
+    check(lib().zg_elp_solve(_ptr(g), len(g), group_size, big_estimate, big_n, nse, ncse, sampled_m,
+                             sampled_max_degree, orig_m, orig_max_degree, eps, conf, C.byref(out)))
+    return out
+
+
+def elp_plain(graph, program, eps, conf, seed, predicate=None, cuda_stream=None, want_groups=False):
+    """zg_elp_plain: ErrorProfile::get_num_estimators on the device."""
+    out = ElpResult()
+    groups = np.zeros(1 << 14, np.float64) if want_groups else None
+    op, t0, t1 = (0, 0, 0) if predicate is None else (predicate[0], predicate[1],
+                                                      predicate[2] if len(predicate) > 2 else 0)
+    check(lib().zg_elp_plain(graph.handle, program.handle, op, t0, t1, eps, conf, seed, cuda_stream, C.byref(out),
+                             _ptr(groups)))
+    return (out, groups) if want_groups else out
+
+
+def run_groups(graph, program, n_groups, group_size, seed, stream_id=0, first_sample=0):
+    out = np.zeros(n_groups, np.float64)
+    check(lib().zg_run_groups(graph.handle, program.handle, n_groups, group_size, first_sample, seed, stream_id,
+                              None, _ptr(out)))
+    return out
+
+
+def time_profile(graph, program, time_limit_ms, seed, stream_id=0):
+    """zg_time_profile: TimeProfile::run."""
+    est, used = C.c_double(), C.c_uint64()
+    check(lib().zg_time_profile(graph.handle, program.handle, time_limit_ms, seed, stream_id, None, C.byref(est),
+                                C.byref(used)))
+    return est.value, used.value
+
+
+def query(graph, program, eps, conf, n_initial, seed, stream_id=0, max_samples=0, cuda_stream=None):
+    """zg_query: budgeted run judged by its empirical CLT bound, extended until the bound holds."""
+    out = QueryResult()
+    check(lib().zg_query(graph.handle, program.handle, eps, conf, n_initial, max_samples, seed, stream_id,
+                         cuda_stream, C.byref(out)))
+    return out
 
 
 def run_three_motif(graph, n_chain, n_tri, seed, stream_chain=0, stream_tri=1, cuda_stream=None):

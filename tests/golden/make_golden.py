@@ -167,6 +167,18 @@ def main():
         meta["samples"][key] = {"n": n, "seed": seed, "stream": stream, "op": op_code, "t": t, "shuffle_seed": sh,
                                 "filtered_m": int(len(idx)), "hits": int(np.count_nonzero(out))}
 
+    # ErrorProfile::get_num_estimators of the reference, replaying the zg_elp_plain draw plan
+    meta["elp"]["get_num_estimators"] = []
+    for gname, app, kind, param, seed in (("rmat10", "triangle", Z.PROG_TRIANGLE, 0, 77),
+                                          ("rmat10", "three_chain", Z.PROG_THREE_CHAIN, 0, 78),
+                                          ("dense7", "four_chain", Z.PROG_FOUR_CHAIN, 0, 79),
+                                          ("dense7", "chain", Z.PROG_CHAIN, 5, 80)):
+        e, nv = graphs[gname]
+        n_req, bad = O.ref_elp(app, e, nv, kind, param=param, seed=seed, eps=0.05, conf=0.95)
+        assert bad == 0, (gname, app)
+        meta["elp"]["get_num_estimators"].append({"graph": gname, "kind": kind, "param": param, "seed": seed,
+                                                  "eps": 0.05, "conf": 0.95, "n_required": n_req})
+
     # exact counts from naive_implementation/
     for gname in ("small10", "simple30", "rmat10", "dense7", "chunglu3k", "wiki_vote"):
         e, nv = graphs[gname]

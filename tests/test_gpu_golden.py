@@ -83,3 +83,14 @@ def test_naive_exact_counts(golden):
         for k, v in counts.items():
             if k in kinds:
                 assert g.exact_count(kinds[k]) == v, (gname, k)
+
+
+def test_error_profile_matches_reference(golden):
+    """zg_elp_plain (subsample, 2^14 x 16 grouped + 2^23 estimators on the device, regression and
+    bound on the host) returns the reference's get_num_estimators on the same draws."""
+    meta, arr = golden
+    for case in meta["elp"]["get_num_estimators"]:
+        e, nv = golden_graph(meta, arr, case["graph"])
+        g = Z.Graph.from_edges(e, nv)
+        r = Z.elp_plain(g, Z.Program(case["kind"], case["param"]), case["eps"], case["conf"], case["seed"])
+        assert abs(r.n_required - case["n_required"]) <= 1e-9 * case["n_required"] + 1, (case, r.n_required)

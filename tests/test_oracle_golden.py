@@ -173,3 +173,31 @@ def test_x87_emulation_matches_long_double():
                 p = p * np.longdouble(x)
             assert got == float(np.longdouble(1.0) / p)
         assert abs(got * np.prod(f) - 1.0) < 1e-12
+
+
+def test_error_profile_matches_reference(golden):
+    """zg_elp_solve on the oracle's draws of the zg_elp_plain plan reproduces the reference's own
+    ErrorProfile::get_num_estimators (src/ErrorLatencyProfile.cpp:72-207)."""
+    meta, arr = golden
+    for case in meta["elp"]["get_num_estimators"]:
+        e, nv = golden_graph(meta, arr, case["graph"])
+        seed = case["seed"]
+        keep = np.array([O.subsample_keep(0.1, seed + Z.ELP_KEEP_OFFSET, i) for i in range(len(e))])
+        kept = np.nonzero(keep)[0]
+        sub = e[kept[O.shuffle_perm(len(kept), seed + Z.ELP_SHUFFLE_OFFSET).astype(np.int64)]]
+        og = O.OracleGraph(sub, nv)
+        prog = O.OracleProgram(case["kind"], case["param"])
+        tr, _ = O.traces(og, prog, 1 << 18, seed, stream=Z.ELP_STREAM)
+        groups = []
+        for row in tr["w"].reshape(-1, 16):
+            acc = 0.0
+            for x in row:
+                acc += float(x)
+            groups.append(acc / 16.0)
+        big = O.run(og, prog, 1 << 23, seed, Z.ELP_STREAM, 1 << 18)
+        ncse = {Z.PROG_TRIANGLE: 1, Z.PROG_THREE_CHAIN: 1, Z.PROG_FOUR_CHAIN: 2,
+                Z.PROG_CHAIN: case["param"] - 2}[case["kind"]]
+        r = Z.elp_solve(np.array(groups), 16, float(big.exact_sum() / big.samples), 1 << 23, 1.0, float(ncse),
+                        len(sub), int(np.bincount(sub.ravel(), minlength=nv).max()), len(e),
+                        int(np.bincount(e.ravel(), minlength=nv).max()), case["eps"], case["conf"])
+        assert abs(r.n_required - case["n_required"]) <= 1e-9 * case["n_required"] + 1, (case, r.n_required)
