@@ -298,6 +298,37 @@ int zg_query(const zg_graph* g, const zg_program* p, double error, double confid
              uint64_t n_initial, uint64_t max_samples, uint64_t seed, uint32_t stream_id,
              void* cuda_stream, zg_query_result* out);
 
+/* ---- learned error-latency profile (no counterpart in the reference) ------------------- */
+/* A 16 -> 64 -> 64 (GELU) -> 2 MLP predicting, for a (graph, program) query, log2 of the
+ * per-sample relative variance Var(1/p)/E(1/p)^2 and log2 of the per-sample latency in ns.
+ * BF16 weights with FP32 accumulation; FP32 master weights and Adam moments; trained and run by
+ * this library's own CUDA kernels.  Parameters: ZG_MLP_PARAMS floats in the order W1[64][16],
+ * b1[64], W2[64][64], b2[64], W3[2][64], b3[2]; norm: 36 floats (feature mean[16], std[16],
+ * target mean[2], std[2]). */
+#define ZG_MLP_FEATURES 16
+#define ZG_MLP_OUTPUTS  2
+#define ZG_MLP_PARAMS   5378
+typedef struct zg_mlp zg_mlp;
+int zg_mlp_num_params(void);
+int zg_mlp_create(uint64_t seed, zg_mlp** out);
+int zg_mlp_free(zg_mlp* net);
+int zg_mlp_get_params(const zg_mlp* net, float* params, float* norm);
+int zg_mlp_set_params(zg_mlp* net, const float* params, const float* norm);
+/* epochs over n_rows raw rows (normalisation statistics are taken from them), minibatches of
+ * batch <= 64 rows in a seeded order, Adam(lr, 0.9, 0.999, 1e-8); loss_history gets one MSE per
+ * step (epochs * n_rows / batch entries), may be NULL. */
+int zg_mlp_train(zg_mlp* net, const float* X, const float* Y, uint32_t n_rows, uint32_t epochs,
+                 uint32_t batch, float lr, uint64_t seed, float* loss_history);
+/* Gradient of the MSE over n_rows <= 64 already-normalised rows at the current weights. */
+int zg_mlp_grad(const zg_mlp* net, const float* X, const float* Y, uint32_t n_rows, float* grads,
+                float* loss);
+/* Predictions for raw features, de-normalised: Y[n_rows][2]. */
+int zg_mlp_predict(const zg_mlp* net, const float* X, uint32_t n_rows, float* Y);
+/* The 16 features of a query: degree statistics of g (one device pass), the program's pattern
+ * class, and a pilot run of pilot_samples estimators (0: 2^16). */
+int zg_graph_features(const zg_graph* g, const zg_program* p, uint64_t pilot_samples,
+                      uint64_t seed, void* cuda_stream, float* features);
+
 /* ---- exact counts ---------------------------------------------------------- */
 /* out[0..1]: 128-bit little-endian count.  kind: ZG_EXACT_*. */
 int zg_exact_count(const zg_graph* g, int kind, void* cuda_stream, uint64_t out[2]);

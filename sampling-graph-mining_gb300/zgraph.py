@@ -130,6 +130,15 @@ def lib():
             "zg_elp_plain": ([P, P, I32, I64, I64, D, D, U64, P, C.POINTER(ElpResult), P], I32),
             "zg_time_profile": ([P, P, U32, U64, U32, P, C.POINTER(D), C.POINTER(U64)], I32),
             "zg_query": ([P, P, D, D, U64, U64, U64, U32, P, C.POINTER(QueryResult)], I32),
+            "zg_mlp_num_params": ([], I32),
+            "zg_mlp_create": ([U64, C.POINTER(P)], I32),
+            "zg_mlp_free": ([P], I32),
+            "zg_mlp_get_params": ([P, P, P], I32),
+            "zg_mlp_set_params": ([P, P, P], I32),
+            "zg_mlp_train": ([P, P, P, U32, U32, U32, C.c_float, U64, P], I32),
+            "zg_mlp_grad": ([P, P, P, U32, P, P], I32),
+            "zg_mlp_predict": ([P, P, U32, P], I32),
+            "zg_graph_features": ([P, P, U64, U64, P, P], I32),
             "zg_gen_rmat": ([U32, U32, D, D, D, U64, U64, P, C.POINTER(U64)], I32),
             "zg_gen_chung_lu": ([U32, D, D, U64, U64, P, C.POINTER(U64)], I32),
             "zg_gen_weights": ([U64, U32, U64, P], I32),
@@ -408,6 +417,87 @@ def query(graph, program, eps, conf, n_initial, seed, stream_id=0, max_samples=0
     check(lib().zg_query(graph.handle, program.handle, eps, conf, n_initial, max_samples, seed, stream_id,
                          cuda_stream, C.byref(out)))
     return out
+
+
+MLP_FEATURES, MLP_OUTPUTS, MLP_PARAMS = 16, 2, 5378
+
+
+def features(graph, program, pilot_samples=1 << 16, seed=1, cuda_stream=None):
+    """zg_graph_features: 16 features of a (graph, program) query."""
+    f = np.zeros(MLP_FEATURES, np.float32)
+    check(lib().zg_graph_features(graph.handle, program.handle, pilot_samples, seed, cuda_stream, _ptr(f)))
+    return f
+
+
+class Mlp:
+    """The learned ELP's network (zg_mlp_*): trained and evaluated by the library's CUDA kernels."""
+
+    def __init__(self, seed=1):
+        init()
+        h = C.c_void_p()
+        check(lib().zg_mlp_create(seed, C.byref(h)))
+        self._h = h
+
+    def params(self):
+        p = np.zeros(MLP_PARAMS, np.float32)
+        nrm = np.zeros(36, np.float32)
+        check(lib().zg_mlp_get_params(self._h, _ptr(p), _ptr(nrm)))
+        return p, nrm
+
+    def set_params(self, params=None, norm=None):
+        pp = None if params is None else np.ascontiguousarray(params, np.float32)
+        nn = None if norm is None else np.ascontiguousarray(norm, np.float32)
+        check(lib().zg_mlp_set_params(self._h, _ptr(pp), _ptr(nn)))
+
+    def train(self, X, Y, epochs=200, batch=64, lr=3e-3, seed=7):
+        X = np.ascontiguousarray(X, np.float32)
+        Y = np.ascontiguousarray(Y, np.float32)
+        steps = max(1, epochs * len(X) // batch)
+        loss = np.zeros(steps, np.float32)
+        check(lib().zg_mlp_train(self._h, _ptr(X), _ptr(Y), len(X), epochs, batch, lr, seed, _ptr(loss)))
+        return loss
+
+    def grad(self, Xn, Yn):
+        Xn = np.ascontiguousarray(Xn, np.float32)
+        Yn = np.ascontiguousarray(Yn, np.float32)
+        g = np.zeros(MLP_PARAMS, np.float32)
+        loss = np.zeros(1, np.float32)
+        check(lib().zg_mlp_grad(self._h, _ptr(Xn), _ptr(Yn), len(Xn), _ptr(g), _ptr(loss)))
+        return g, float(loss[0])
+
+    def predict(self, X):
+        X = np.ascontiguousarray(X, np.float32).reshape(-1, MLP_FEATURES)
+        Y = np.zeros((len(X), MLP_OUTPUTS), np.float32)
+        check(lib().zg_mlp_predict(self._h, _ptr(X), len(X), _ptr(Y)))
+        return Y
+
+    def save(self, path):
+        p, n = self.params()
+        np.savez(path, params=p, norm=n)
+
+    @classmethod
+    def load(cls, path):
+        d = np.load(path)
+        m = cls()
+        m.set_params(d["params"], d["norm"])
+        return m
+
+    def __del__(self):
+        try:
+            if self._h:
+                lib().zg_mlp_free(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+
+def learned_budget(mlp, graph, program, eps, conf, seed=1, pilot_samples=1 << 16):
+    """Learned ELP sizing: predicted per-sample relative variance -> n = z^2 * cv2 / eps^2."""
+    f = features(graph, program, pilot_samples, seed)
+    y = mlp.predict(f[None, :])[0]
+    z = lib().zg_normal_quantile(1.0 - (1.0 - conf) / 2.0)
+    n = z * z * float(2.0 ** y[0]) / (eps * eps)
+    return max(int(n), 1 << 16), f, y
 
 
 def run_three_motif(graph, n_chain, n_tri, seed, stream_chain=0, stream_tri=1, cuda_stream=None):
