@@ -419,6 +419,57 @@ def query(graph, program, eps, conf, n_initial, seed, stream_id=0, max_samples=0
     return out
 
 
+def merge_counters(parts):
+    """Exact merge of runs over disjoint sample ranges (the multi-GPU shards): 320-bit sums add,
+    hit/fail counts add, the mean is re-rounded once from the exact total."""
+    from fractions import Fraction
+    parts = list(parts)
+    out = Counters()
+    den = max(p.den_log2 for p in parts)
+    total = 0
+    for p in parts:
+        v = sum(int(p.sum_num[i]) << (64 * i) for i in range(5))
+        total += v << (den - p.den_log2)
+        out.samples += p.samples
+        out.hits += p.hits
+        out.fails += p.fails
+        out.overflow |= p.overflow
+        out.sum_w += p.sum_w
+        out.sum_w2 += p.sum_w2
+    out.den_log2 = den
+    for i in range(5):
+        out.sum_num[i] = (total >> (64 * i)) & 0xFFFFFFFFFFFFFFFF
+    out.estimate = float(Fraction(total, (1 << den) * out.samples)) if out.samples else 0.0
+    return out
+
+
+def allgather_counters(c, group=None):
+    """torch.distributed all-gather of one rank's Counters as integer limbs, merged exactly on every
+    rank (no floating-point reduction of the estimate)."""
+    import torch
+    import torch.distributed as dist
+    words = [c.samples, c.hits, c.fails, c.den_log2, c.overflow] + [int(x) for x in c.sum_num]
+    t = torch.tensor([w - (1 << 64) if w >= (1 << 63) else w for w in words], dtype=torch.int64)
+    f = torch.tensor([c.sum_w, c.sum_w2], dtype=torch.float64)
+    backend = dist.get_backend(group)
+    if backend == "nccl":
+        t, f = t.cuda(), f.cuda()
+    ts = [torch.zeros_like(t) for _ in range(dist.get_world_size(group))]
+    fs = [torch.zeros_like(f) for _ in range(dist.get_world_size(group))]
+    dist.all_gather(ts, t, group=group)
+    dist.all_gather(fs, f, group=group)
+    parts = []
+    for tt, ff in zip(ts, fs):
+        w = [int(x) & 0xFFFFFFFFFFFFFFFF for x in tt.cpu().tolist()]
+        p = Counters()
+        p.samples, p.hits, p.fails, p.den_log2, p.overflow = w[0], w[1], w[2], w[3], w[4]
+        for i in range(5):
+            p.sum_num[i] = w[5 + i]
+        p.sum_w, p.sum_w2 = [float(x) for x in ff.cpu().tolist()]
+        parts.append(p)
+    return merge_counters(parts)
+
+
 MLP_FEATURES, MLP_OUTPUTS, MLP_PARAMS = 16, 2, 5378
 
 
