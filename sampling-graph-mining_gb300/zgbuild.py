@@ -68,6 +68,51 @@ def build_library(verbose=False, force=False):
     return LIB
 
 
+CPP = os.path.join(PKG, "cpp")
+HOST_LIB = os.path.join(BUILD, "libzgraph_host.so")
+CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-Wno-unused-function", "-I" + os.path.join(CPP, "include")]
+
+
+def _cxx():
+    return os.environ.get("CXX", "g++")
+
+
+def build_host(verbose=False, force=False):
+    """libzgraph_host.so: the C++ host layer (the reference's class interface over the C ABI)."""
+    lib = build_library(verbose=verbose, force=force)
+    src_dir = os.path.join(CPP, "src")
+    inc_dir = os.path.join(CPP, "include")
+    headers = [os.path.join(inc_dir, f) for f in os.listdir(inc_dir)] + \
+              [os.path.join(src_dir, f) for f in os.listdir(src_dir) if f.endswith(".hpp")] + \
+              [os.path.join(ROOT, "include", "zgraph_gpu.h")]
+    units = sorted(f for f in os.listdir(src_dir) if f.endswith(".cpp"))
+    objs, jobs = [], []
+    for u in units:
+        src = os.path.join(src_dir, u)
+        obj = os.path.join(BUILD, "host_" + u + ".o")
+        objs.append(obj)
+        if force or _stale(obj, [src] + headers):
+            jobs.append([_cxx()] + CXX_FLAGS + ["-c", src, "-o", obj])
+    with cf.ThreadPoolExecutor(max_workers=min(8, max(1, len(jobs)))) as ex:
+        for out in ex.map(_run, jobs):
+            if verbose and out.strip():
+                print(out)
+    if force or _stale(HOST_LIB, objs + [lib]):
+        _run([_cxx(), "-shared", "-o", HOST_LIB] + objs +
+             ["-L" + BUILD, "-lzgraph_gpu", "-Wl,-rpath,$ORIGIN"])
+    return HOST_LIB
+
+
+def build_app(sources, out, include_dirs=(), extra_flags=()):
+    """Compiles an application written against the reference's headers and links it to the host
+    layer; the executable finds both libraries through its rpath."""
+    build_host()
+    cmd = [_cxx()] + CXX_FLAGS + ["-I" + d for d in include_dirs] + list(extra_flags) + list(sources) + \
+          ["-o", out, "-L" + BUILD, "-lzgraph_host", "-lzgraph_gpu", "-Wl,-rpath," + BUILD, "-lpthread"]
+    _run(cmd)
+    return out
+
+
 def build_oracle(verbose=False, force=False):
     os.makedirs(ORACLE_BUILD, exist_ok=True)
     src = os.path.join(ORACLE_DIR, "zg_oracle.c")
