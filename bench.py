@@ -50,6 +50,9 @@ def parse():
     ap.add_argument("--workload", default="rmat20", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-time-to-bound", action="store_true")
+    ap.add_argument("--variants", default=None,
+                    help="fixed launch shapes instead of tuning, e.g. triangle=4,four_clique=3 "
+                         "(profiling runs: no tuner probe launches)")
     return ap.parse_args()
 
 
@@ -245,7 +248,13 @@ def run_gb300(args):
     sp = stream.cuda_stream
     # autotuner: pick each program's launch shape on this graph (setup, untimed)
     tuning = {}
+    fixed = dict(kv.split("=") for kv in args.variants.split(",")) if args.variants else None
     for name, p in zip(names, progs):
+        if fixed is not None:
+            if name in fixed:
+                p.set_variant(int(fixed[name]))
+            tuning[name] = dict(p.variant(), fixed=True)
+            continue
         best, ms = p.tune(g, 1 << 23, cuda_stream=sp)
         tuning[name] = {"variant": best, "min_blocks": p.variant()["min_blocks"], "grid": p.variant()["grid"],
                         "ms_per_variant_2^23": [round(x, 3) for x in ms]}

@@ -121,10 +121,123 @@ __global__ void k_adj_n(const unsigned long long* __restrict__ nkeys, const uint
   }
 }
 
+__global__ void k_off32(const int64_t* __restrict__ off, uint64_t n, uint32_t* __restrict__ off32) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    off32[i] = (uint32_t)off[i];
+}
+
+// Bucketed two-choice cuckoo insertion of every edge's key.  A thread claims an empty slot of
+// either bucket with atomicCAS; when both are full it swaps its key into a slot (atomicExch) and
+// carries the evicted key to that key's other bucket.  After kMaxKicks swaps it gives up and
+// raises *fail: the host rebuilds with new hash seeds (every loop here is bounded).
+constexpr int kMaxKicks = 128;
+
+__device__ __forceinline__ bool cuckoo_try(unsigned long long* keys, uint32_t b, unsigned long long k) {
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    unsigned long long* slot = &keys[4 * (uint64_t)b + j];
+    if (*(volatile unsigned long long*)slot != ZG_HASH_EMPTY) continue;
+    if (atomicCAS(slot, ZG_HASH_EMPTY, k) == ZG_HASH_EMPTY) return true;
+  }
+  return false;
+}
+
+__global__ void k_cuckoo_insert(const uint4* __restrict__ rec, uint64_t m, unsigned long long* keys, uint32_t bits,
+                                uint64_t seed, unsigned int* __restrict__ fail) {
+  for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < m; e += (uint64_t)gridDim.x * blockDim.x) {
+    uint4 r = rec[e];
+    unsigned long long k = zg_edge_key(r.x, r.y);
+    uint32_t from = 0xFFFFFFFFu;  // the bucket the carried key was evicted from
+    bool placed = false;
+    for (int kick = 0; kick < kMaxKicks; ++kick) {
+      uint32_t b1 = zg_bucket1(k, seed, bits), b2 = zg_bucket2(k, seed, bits);
+      if (cuckoo_try(keys, b1, k) || (b2 != b1 && cuckoo_try(keys, b2, k))) {
+        placed = true;
+        break;
+      }
+      uint32_t vb = from == b1 ? b2 : from == b2 ? b1 : (((e + kick) & 1) ? b2 : b1);
+      unsigned long long old = atomicExch(&keys[4 * (uint64_t)vb + ((e + (uint64_t)kick) & 3)], k);
+      if (old == ZG_HASH_EMPTY) {
+        placed = true;
+        break;
+      }
+      k = old;
+      from = vb;
+    }
+    if (!placed) atomicOr(fail, 1u);
+  }
+}
+
+// Edge ids beside the keys; a key not found means the insertion lost it (fail).
+__global__ void k_cuckoo_fill(const uint4* __restrict__ rec, uint64_t m, const unsigned long long* __restrict__ keys,
+                              uint32_t bits, uint64_t seed, uint32_t* __restrict__ eid, unsigned int* __restrict__ fail) {
+  for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < m; e += (uint64_t)gridDim.x * blockDim.x) {
+    uint4 r = rec[e];
+    unsigned long long k = zg_edge_key(r.x, r.y);
+    uint32_t bs[2] = {zg_bucket1(k, seed, bits), zg_bucket2(k, seed, bits)};
+    bool found = false;
+    for (int i = 0; i < 2 && !found; ++i)
+      for (int j = 0; j < 4; ++j)
+        if (keys[4 * (uint64_t)bs[i] + j] == k) {
+          eid[4 * (uint64_t)bs[i] + j] = (uint32_t)e;
+          found = true;
+          break;
+        }
+    if (!found) atomicOr(fail, 1u);
+  }
+}
+
+// The cuckoo table of the graph's edges: buckets for a load of at most 0.8, up to 8 seeds, and the
+// table doubled after every 4 failed seeds.
+int build_hash(zg_graph* g, cudaStream_t s) {
+  const uint64_t m = g->d.m;
+  uint32_t bits = 1;
+  while ((4ull << bits) * 4 < m * 5) ++bits;  // 4 * 2^bits slots >= m / 0.8
+  DevBuf fail;
+  int rc;
+  if ((rc = fail.alloc(sizeof(unsigned int)))) return rc;
+  const int B = 256;
+  for (int attempt = 0; attempt < 8; ++attempt) {
+    if (attempt && attempt % 4 == 0) ++bits;
+    const uint64_t slots = 4ull << bits;
+    if (g->hkeys) cudaFree(g->hkeys);
+    if (g->heid) cudaFree(g->heid);
+    g->hkeys = nullptr;
+    g->heid = nullptr;
+    if ((rc = dev_alloc(&g->hkeys, slots)) || (rc = dev_alloc(&g->heid, slots))) return rc;
+    uint64_t seed = zg_mix64(0x5A4748415348ull + attempt);
+    cudaError_t ce;
+    if ((ce = cudaMemsetAsync(g->hkeys, 0xFF, sizeof(unsigned long long) * slots, s)) ||
+        (ce = cudaMemsetAsync(g->heid, 0xFF, sizeof(uint32_t) * slots, s)) ||
+        (ce = cudaMemsetAsync(fail.p, 0, sizeof(unsigned int), s)))
+      return zg_check_cuda(ce, "hash memset");
+    if (m) {
+      k_cuckoo_insert<<<grid_for(m, B), B, 0, s>>>(g->rec, m, g->hkeys, bits, seed, fail.as<unsigned int>());
+      k_cuckoo_fill<<<grid_for(m, B), B, 0, s>>>(g->rec, m, g->hkeys, bits, seed, g->heid, fail.as<unsigned int>());
+    }
+    unsigned int hf = 0;
+    if ((ce = cudaMemcpyAsync(&hf, fail.p, sizeof(hf), cudaMemcpyDeviceToHost, s)) || (ce = cudaStreamSynchronize(s)))
+      return zg_check_cuda(ce, "hash build");
+    if (!hf) {
+      g->d.hkeys = g->hkeys;
+      g->d.heid = g->heid;
+      g->d.hbits = bits;
+      g->d.hseed = seed;
+      g->bytes += slots * (sizeof(unsigned long long) + sizeof(uint32_t));
+      return ZG_OK;
+    }
+  }
+  zg_set_error(ZG_ERR_CUDA, "cuckoo table of %llu edges did not build", (unsigned long long)m);
+  return ZG_ERR_CUDA;
+}
+
 // Builds a graph from a device COO (consumed: freed by the caller afterwards).
 int build_graph(const uint2* d_coo, const uint32_t* d_w_in, uint64_t m, uint32_t nv,
                 cudaStream_t s, zg_graph** out) {
-  if (m >= 0xFFFFFFFFull) return zg_set_error(ZG_ERR_TOO_LARGE, "edge ids are 32-bit: m=%llu", (unsigned long long)m), ZG_ERR_TOO_LARGE;
+  // edge ids and adjacency positions (< 2m) are 32-bit
+  if (m > 0x7FFFFFFFull)
+    return zg_set_error(ZG_ERR_TOO_LARGE, "at most 2^31-1 edges (32-bit positions): m=%llu", (unsigned long long)m),
+           ZG_ERR_TOO_LARGE;
   if (nv == 0 && m > 0) return zg_set_error(ZG_ERR_INVALID_GRAPH, "edges on a graph with 0 vertices"), ZG_ERR_INVALID_GRAPH;
   zg_graph* g = new zg_graph();
   memset(g, 0, sizeof(*g));
@@ -135,7 +248,8 @@ int build_graph(const uint2* d_coo, const uint32_t* d_w_in, uint64_t m, uint32_t
   };
   uint64_t n2 = 2 * m;
   if ((rc = dev_alloc(&g->rec, m)) || (rc = dev_alloc(&g->off, (size_t)nv + 1)) ||
-      (rc = dev_alloc(&g->adj_e, n2)) || (rc = dev_alloc(&g->adj_n, n2)))
+      (rc = dev_alloc(&g->off32, (size_t)nv + 1)) || (rc = dev_alloc(&g->adj_e, n2)) ||
+      (rc = dev_alloc(&g->adj_n, n2)))
     return fail(rc);
   if (d_w_in) {
     if ((rc = dev_alloc(&g->w, m))) return fail(rc);
@@ -144,7 +258,7 @@ int build_graph(const uint2* d_coo, const uint32_t* d_w_in, uint64_t m, uint32_t
       if (e != cudaSuccess) return fail(zg_check_cuda(e, "copy weights"));
     }
   }
-  g->bytes = sizeof(uint4) * m + sizeof(int64_t) * ((size_t)nv + 1) + 2 * sizeof(uint2) * n2 +
+  g->bytes = sizeof(uint4) * m + (sizeof(int64_t) + sizeof(uint32_t)) * ((size_t)nv + 1) + 2 * sizeof(uint2) * n2 +
              (d_w_in ? sizeof(uint32_t) * m : 0);
   DevBuf deg, keys, keys2, vals, vals2, flags, tmp, nk, nk2, nv1, nv2;
   if ((rc = deg.alloc(sizeof(unsigned long long) * ((size_t)nv + 1))) ||
@@ -229,10 +343,14 @@ int build_graph(const uint2* d_coo, const uint32_t* d_w_in, uint64_t m, uint32_t
     }
     g->max_degree = hmax;
   }
+  k_off32<<<grid_for((uint64_t)nv + 1, B), B, 0, s>>>(g->off, (uint64_t)nv + 1, g->off32);
+  g->d.m = m;
+  g->d.rec = g->rec;
+  if ((rc = build_hash(g, s))) return fail(rc);
   ce = cudaGetLastError();
   if (ce != cudaSuccess) return fail(zg_check_cuda(ce, "graph build kernels"));
   g->d.nv = nv;
-  g->d.m = m;
+  g->d.off32 = g->off32;
   g->d.rec = g->rec;
   g->d.off = g->off;
   g->d.adj_e = g->adj_e;
@@ -471,6 +589,9 @@ extern "C" int zg_graph_free(zg_graph* g) {
   if (!g) return ZG_OK;
   if (g->rec) cudaFree(g->rec);
   if (g->off) cudaFree(g->off);
+  if (g->off32) cudaFree(g->off32);
+  if (g->hkeys) cudaFree(g->hkeys);
+  if (g->heid) cudaFree(g->heid);
   if (g->adj_e) cudaFree(g->adj_e);
   if (g->adj_n) cudaFree(g->adj_n);
   if (g->w) cudaFree(g->w);

@@ -8,8 +8,13 @@
 //   off[V+1]  int64 offsets shared by both adjacency arrays (outgoing_adj_index).
 //   adj_e[2m] uint2 (nbr, edge_id) sorted by edge id per vertex (outgoing_adj_list order,
 //             asserted at src/Graph.cpp:324-334): the sampling order.
-//   adj_n[2m] uint2 (nbr, edge_id) sorted by (nbr, edge_id) per vertex: closure look-ups.
+//   adj_n[2m] uint2 (nbr, edge_id) sorted by (nbr, edge_id) per vertex (exports, exact counts).
 //   w[m]      uint32 edge data (Graph<VertexId>) or null.
+//   off32[V+1] the offsets as uint32 (2m < 2^32): what the sampling kernels read.
+//   hkeys[4B] / heid[4B]: the edge set as a two-choice bucketed cuckoo table, B = 2^hbits buckets
+//             of 4 keys (one 32-byte sector); key = (min(u,v) << 32) | max(u,v), heid = its edge
+//             id.  A closure check ("edge (x,y) exists with id >= min_valid") reads two sectors
+//             issued together instead of a binary search of dependent loads.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -22,14 +27,36 @@
 
 struct ZgDevGraph {
   uint32_t nv;
-  uint32_t pad;
+  uint32_t hbits;  // log2 of the cuckoo table's bucket count
   uint64_t m;
   const uint4* rec;
   const int64_t* off;
   const uint2* adj_e;
   const uint2* adj_n;
   const uint32_t* w;
+  const uint32_t* off32;
+  const unsigned long long* hkeys;
+  const uint32_t* heid;
+  uint64_t hseed;
 };
+
+#define ZG_HASH_EMPTY 0xFFFFFFFFFFFFFFFFull
+
+// splitmix64 finaliser: the cuckoo table's bucket hashes.
+__host__ __device__ __forceinline__ uint64_t zg_mix64(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+__host__ __device__ __forceinline__ uint64_t zg_edge_key(uint32_t x, uint32_t y) {
+  return x < y ? ((uint64_t)x << 32) | y : ((uint64_t)y << 32) | x;
+}
+__host__ __device__ __forceinline__ uint32_t zg_bucket1(uint64_t key, uint64_t seed, uint32_t bits) {
+  return (uint32_t)(zg_mix64(key ^ seed) >> (64 - bits));
+}
+__host__ __device__ __forceinline__ uint32_t zg_bucket2(uint64_t key, uint64_t seed, uint32_t bits) {
+  return (uint32_t)(zg_mix64(key ^ (seed * 0x9E3779B97F4A7C15ull + 0x632BE59BD9B4E019ull)) >> (64 - bits));
+}
 
 struct zg_graph {
   ZgDevGraph d;
@@ -38,6 +65,9 @@ struct zg_graph {
   uint2* adj_e;
   uint2* adj_n;
   uint32_t* w;
+  uint32_t* off32;
+  unsigned long long* hkeys;
+  uint32_t* heid;
   uint64_t num_edges;   // Graph::num_edges metadata
   uint64_t max_degree;  // Graph::max_degree metadata
   uint64_t bytes;

@@ -64,9 +64,9 @@ __device__ __forceinline__ void res_mul(Res& r, uint64_t f) {
 }
 
 // first index in adj_e[lo, hi) whose edge id >= key
-__device__ __forceinline__ int64_t lb_eid(const uint2* __restrict__ adj, int64_t lo, int64_t hi, uint32_t key) {
+__device__ __forceinline__ uint32_t lb_eid(const uint2* __restrict__ adj, uint32_t lo, uint32_t hi, uint32_t key) {
   while (lo < hi) {
-    int64_t mid = (lo + hi) >> 1;
+    uint32_t mid = lo + ((hi - lo) >> 1);
     if (ZG_LDG(&adj[mid]).y < key)
       lo = mid + 1;
     else
@@ -75,28 +75,31 @@ __device__ __forceinline__ int64_t lb_eid(const uint2* __restrict__ adj, int64_t
   return lo;
 }
 
-// Does edge (x,y) exist with edge id >= min_valid?  Searches the shorter neighbour-sorted list
-// for the last entry with nbr == target (duplicates, if any, are ordered by edge id).
-__device__ __forceinline__ bool edge_after(int64_t bx, int64_t ex, int64_t by, int64_t ey, uint32_t x, uint32_t y,
-                                           uint32_t min_valid, const uint2* __restrict__ adj_n) {
-  int64_t lo = bx, hi = ex;
-  uint32_t t = y;
-  if (ex - bx > ey - by) {
-    lo = by;
-    hi = ey;
-    t = x;
-  }
-  int64_t b = lo;
-  while (lo < hi) {
-    int64_t mid = (lo + hi) >> 1;
-    if (ZG_LDG(&adj_n[mid]).x <= t)
-      lo = mid + 1;
-    else
-      hi = mid;
-  }
-  if (lo == b) return false;
-  uint2 a = ZG_LDG(&adj_n[lo - 1]);
-  return a.x == t && a.y >= min_valid;
+// Does edge (x,y) exist with edge id >= min_valid?  conditional_close's question
+// (src/ZGraphInstance.cpp:372-407): the pattern edges still to close join two sampled vertices,
+// so "found in some sampled vertex's list with id >= min_valid" is "edge (x,y) exists with such
+// an id".  Answered by the cuckoo table: both candidate buckets (one 32-byte sector each) are
+// read together, and the edge id only when the key is present.
+__device__ __forceinline__ int64_t edge_slot(const ZgDevGraph& g, uint32_t x, uint32_t y) {
+  unsigned long long k = zg_edge_key(x, y);
+  uint64_t b1 = 4ull * zg_bucket1(k, g.hseed, g.hbits), b2 = 4ull * zg_bucket2(k, g.hseed, g.hbits);
+  const ulonglong2* p1 = reinterpret_cast<const ulonglong2*>(g.hkeys + b1);
+  const ulonglong2* p2 = reinterpret_cast<const ulonglong2*>(g.hkeys + b2);
+  ulonglong2 a0 = __ldg(p1), a1 = __ldg(p1 + 1), c0 = __ldg(p2), c1 = __ldg(p2 + 1);
+  int64_t slot = -1;
+  if (a0.x == k) slot = (int64_t)b1;
+  if (a0.y == k) slot = (int64_t)b1 + 1;
+  if (a1.x == k) slot = (int64_t)b1 + 2;
+  if (a1.y == k) slot = (int64_t)b1 + 3;
+  if (c0.x == k) slot = (int64_t)b2;
+  if (c0.y == k) slot = (int64_t)b2 + 1;
+  if (c1.x == k) slot = (int64_t)b2 + 2;
+  if (c1.y == k) slot = (int64_t)b2 + 3;
+  return slot;
+}
+__device__ __forceinline__ bool edge_after(const ZgDevGraph& g, uint32_t x, uint32_t y, uint32_t min_valid) {
+  int64_t slot = edge_slot(g, x, y);
+  return slot >= 0 && ZG_LDG(&g.heid[slot]) >= min_valid;
 }
 
 // ---- access model (debug): algorithmic bytes of a sample in 32-byte sectors ---------------
@@ -108,7 +111,7 @@ __device__ __forceinline__ uint32_t model_search(uint64_t d) {
   return l > 3 ? l - 2 : 1u;
 }
 __device__ __forceinline__ uint64_t degree(const ZgDevGraph& g, uint32_t v) {
-  return (uint64_t)(ZG_LDG(&g.off[v + 1]) - ZG_LDG(&g.off[v]));
+  return (uint64_t)(ZG_LDG(&g.off32[v + 1]) - ZG_LDG(&g.off32[v]));
 }
 __device__ __forceinline__ uint32_t model_anchor(const ZgDevGraph& g, uint32_t v) {
   uint64_t d = degree(g, v);
@@ -232,16 +235,13 @@ __device__ void prog_triangle(const ZgDevGraph& g, Ctx& c, Res& r) {
     other = q.x;
     suf = q.w;
   }
-  // closing-edge endpoint `other` offsets do not depend on the second edge: issue early
-  int64_t bo = ZG_LDG(&g.off[other]), eo = ZG_LDG(&g.off[other + 1]);
-  int64_t idx = ZG_LDG(&g.off[anchor + 1]) - (int64_t)suf + (int64_t)r1;
+  uint32_t idx = ZG_LDG(&g.off32[anchor + 1]) - (uint32_t)suf + (uint32_t)r1;
   uint2 e1 = ZG_LDG(&g.adj_e[idx]);
   uint32_t a1 = 1 + (e1.x == q.x || e1.x == q.y);
   res_mul(r, g.m);
   res_mul(r, S);
   if (a1 == 2) r.shift = 1;
-  int64_t bc = ZG_LDG(&g.off[e1.x]), ec = ZG_LDG(&g.off[e1.x + 1]);
-  bool closed = (a1 == 1) && edge_after(bo, eo, bc, ec, other, e1.x, e1.y + 1, g.adj_n);
+  bool closed = (a1 == 1) && edge_after(g, other, e1.x, e1.y + 1);
   if (DBG) c.sectors += model_close(g, other, e1.x);
   r.hit = closed;
   if (DBG && closed) {
@@ -279,7 +279,7 @@ __device__ void prog_three_chain(const ZgDevGraph& g, Ctx& c, Res& r) {
       anchor = q.y;
       suf = q.w;
     }
-    uint2 e1 = ZG_LDG(&g.adj_e[ZG_LDG(&g.off[anchor + 1]) - (int64_t)suf + (int64_t)r1]);
+    uint2 e1 = ZG_LDG(&g.adj_e[ZG_LDG(&g.off32[anchor + 1]) - (uint32_t)suf + (uint32_t)r1]);
     a1 = 1 + (e1.x == q.x || e1.x == q.y);
   }
   res_mul(r, g.m);
@@ -295,6 +295,8 @@ __device__ void prog_three_chain(const ZgDevGraph& g, Ctx& c, Res& r) {
 }
 
 // ---- FourClique: applications/FourClique.cpp:176-234 -------------------------------------
+// Vertices in insertion order a (e0.src), b (e0.dst), c (e1's new end), d (e2's new end); all
+// state in scalars (no dynamically indexed arrays, which would live in local memory).
 template <bool DBG>
 __device__ void prog_four_clique(const ZgDevGraph& g, Ctx& c, Res& r) {
   if (g.m == 0) {
@@ -311,85 +313,79 @@ __device__ void prog_four_clique(const ZgDevGraph& g, Ctx& c, Res& r) {
   }
   if (DBG) c.sectors += 1;
   uint64_t r1 = c.draw(0, S1 - 1);
-  // vertex slots in insertion order: 0 = a (e0.src), 1 = b (e0.dst), 2 = c, 3 = d
-  uint32_t v[4];
-  int64_t beg[4], end[4], lb[3];
-  v[0] = q.x;
-  v[1] = q.y;
-  end[0] = ZG_LDG(&g.off[q.x + 1]);
-  end[1] = ZG_LDG(&g.off[q.y + 1]);
-  int s1 = 0;  // slot of the first conditional edge's anchor
-  uint64_t rr = r1;
-  if (rr >= q.z) {
-    rr -= q.z;
-    s1 = 1;
-  }
-  uint32_t suf1 = s1 ? q.w : q.z;
-  int64_t idx1 = end[s1] - (int64_t)suf1 + (int64_t)rr;
+  const uint32_t va = q.x, vb = q.y;
+  uint32_t endA = ZG_LDG(&g.off32[va + 1]), endB = ZG_LDG(&g.off32[vb + 1]);
+  const bool s1b = r1 >= q.z;  // the first conditional edge hangs off b
+  uint32_t idx1 = (s1b ? endB - q.w + (uint32_t)(r1 - q.z) : endA - q.z + (uint32_t)r1);
   uint2 e1 = ZG_LDG(&g.adj_e[idx1]);
-  v[2] = e1.x;
-  uint32_t a1 = 1 + (e1.x == v[0] || e1.x == v[1]);
+  const uint32_t vc = e1.x;
+  uint32_t a1 = 1 + (vc == va || vc == vb);
   res_mul(r, g.m);
   res_mul(r, S1);
   if (a1 == 2) r.shift++;
   // second conditional step: anchors [a, b, c], min_valid = id1 + 1
   uint32_t mv = e1.y + 1;
   uint4 q1 = ZG_LDG(&g.rec[e1.y]);
-  uint32_t sufc = (q1.x == v[2]) ? q1.z : q1.w;
-  end[2] = ZG_LDG(&g.off[v[2] + 1]);
-  lb[s1] = idx1 + 1;
-  int so = 1 - s1;
-  uint32_t sufo = so ? q.w : q.z;
-  lb[so] = lb_eid(g.adj_e, end[so] - (int64_t)sufo, end[so], mv);
-  lb[2] = end[2] - (int64_t)sufc;
-  uint64_t S2 = 0;
-  if (a1 == 1) {
-    S2 = (uint64_t)(end[0] - lb[0]) + (uint64_t)(end[1] - lb[1]) + (uint64_t)(end[2] - lb[2]);
-  } else {
-    // c coincides with a or b (duplicate edges): the reference lists only two vertices
-    S2 = (uint64_t)(end[0] - lb[0]) + (uint64_t)(end[1] - lb[1]);
-  }
-  if (DBG) c.sectors += model_anchor(g, v[0]) + model_anchor(g, v[1]) + (a1 == 1 ? model_anchor(g, v[2]) : 0);
+  uint32_t endC = ZG_LDG(&g.off32[vc + 1]);
+  uint32_t lbC = endC - ((q1.x == vc) ? q1.z : q1.w);
+  // the anchor's own list continues right after e1; the other endpoint's list needs a search
+  uint32_t lo = lb_eid(g.adj_e, s1b ? endA - q.z : endB - q.w, s1b ? endA : endB, mv);
+  uint32_t lbA = s1b ? lo : idx1 + 1, lbB = s1b ? idx1 + 1 : lo;
+  uint64_t lenA = endA - lbA, lenB = endB - lbB;
+  // when c coincides with a or b (duplicate edges) the reference lists only two vertices
+  uint64_t lenC = a1 == 1 ? (uint64_t)(endC - lbC) : 0;
+  uint64_t S2 = lenA + lenB + lenC;
+  if (DBG) c.sectors += model_anchor(g, va) + model_anchor(g, vb) + (a1 == 1 ? model_anchor(g, vc) : 0);
   if (S2 == 0) {
     r.fail = true;
     return;
   }
   if (DBG) c.sectors += 1;
   uint64_t r2 = c.draw(0, S2 - 1);
-  int s2 = 0;
-  int nslots = a1 == 1 ? 3 : 2;
-  for (; s2 < nslots - 1; ++s2) {
-    uint64_t len = (uint64_t)(end[s2] - lb[s2]);
-    if (r2 < len) break;
-    r2 -= len;
+  int s2;
+  uint32_t pos2;
+  if (r2 < lenA) {
+    s2 = 0;
+    pos2 = lbA + (uint32_t)r2;
+  } else if (r2 - lenA < lenB) {
+    s2 = 1;
+    pos2 = lbB + (uint32_t)(r2 - lenA);
+  } else {
+    s2 = 2;
+    pos2 = lbC + (uint32_t)(r2 - lenA - lenB);
   }
-  uint2 e2 = ZG_LDG(&g.adj_e[lb[s2] + (int64_t)r2]);
-  v[3] = e2.x;
-  bool dup = false;
-  for (int i = 0; i < nslots; ++i) dup |= (e2.x == v[i]);
+  uint2 e2 = ZG_LDG(&g.adj_e[pos2]);
+  const uint32_t vd = e2.x;
+  bool dup = vd == va || vd == vb || (a1 == 1 && vd == vc);
   uint32_t a2 = 1 + (dup ? 1 : 0);
   res_mul(r, S2);
   if (a2 == 2) r.shift++;
   if (a1 != 1 || dup) return;  // three vertices: a triangle was sampled (FourClique.cpp:224-226)
-  // closure: the 3 pairs of the 4-clique not sampled, all with edge id >= id2 + 1
+  // closure: the 3 vertex pairs not sampled, all with edge id >= id2 + 1.  Sampled pairs are
+  // (a,b), (anchor of e1, c) and (anchor of e2, d).  The reference checks the pairs in slot order
+  // up to the first miss (the debug access model follows that); production issues all three
+  // look-ups at once.
+  const int s1 = s1b ? 1 : 0;
   uint32_t mv2 = e2.y + 1;
-  beg[0] = ZG_LDG(&g.off[v[0]]);
-  beg[1] = ZG_LDG(&g.off[v[1]]);
-  beg[2] = ZG_LDG(&g.off[v[2]]);
-  beg[3] = ZG_LDG(&g.off[v[3]]);
-  end[3] = ZG_LDG(&g.off[v[3] + 1]);
-  // sampled pairs: (0,1), (s1,2), (s2,3)
+  auto vslot = [&](int i) { return i == 0 ? va : i == 1 ? vb : i == 2 ? vc : vd; };
   bool ok = true;
-#pragma unroll
-  for (int i = 0; i < 4; ++i)
-#pragma unroll
-    for (int j = i + 1; j < 4; ++j) {
-      bool sampled = (i == 0 && j == 1) || (i == s1 && j == 2) || (i == s2 && j == 3);
-      if (!sampled && ok) {
-        ok = edge_after(beg[i], end[i], beg[j], end[j], v[i], v[j], mv2, g.adj_n);
-        if (DBG) c.sectors += model_close(g, v[i], v[j]);
+  if (DBG) {
+    for (int i = 0; i < 4; ++i)
+      for (int j = i + 1; j < 4; ++j) {
+        bool sampled = (i == 0 && j == 1) || (i == s1 && j == 2) || (i == s2 && j == 3);
+        if (!sampled && ok) {
+          ok = edge_after(g, vslot(i), vslot(j), mv2);
+          c.sectors += model_close(g, vslot(i), vslot(j));
+        }
       }
-    }
+  } else {
+    uint32_t x0 = s1b ? va : vb;             // the pair (not-anchor-of-e1, c)
+    uint32_t x1 = vslot(s2 == 0 ? 1 : 0);    // the two pairs (?, d) other than e2's own
+    uint32_t x2 = vslot(s2 == 2 ? 1 : 2);
+    int64_t h0 = edge_slot(g, x0, vc), h1 = edge_slot(g, x1, vd), h2 = edge_slot(g, x2, vd);
+    ok = h0 >= 0 && h1 >= 0 && h2 >= 0;
+    if (ok) ok = ZG_LDG(&g.heid[h0]) >= mv2 && ZG_LDG(&g.heid[h1]) >= mv2 && ZG_LDG(&g.heid[h2]) >= mv2;
+  }
   r.hit = ok;
   if (DBG && ok) {
     double p = 1.0;
@@ -433,7 +429,7 @@ __device__ void prog_four_chain(const ZgDevGraph& g, Ctx& c, Res& r) {
       anchor = b;
       suf = q.w;
     }
-    int64_t idx1 = ZG_LDG(&g.off[anchor + 1]) - (int64_t)suf + (int64_t)r1;
+    uint32_t idx1 = ZG_LDG(&g.off32[anchor + 1]) - (uint32_t)suf + (uint32_t)r1;
     uint2 e1 = ZG_LDG(&g.adj_e[idx1]);
     a1 = 1 + (e1.x == a || e1.x == b);
     res_mul(r, S1);
@@ -446,15 +442,15 @@ __device__ void prog_four_chain(const ZgDevGraph& g, Ctx& c, Res& r) {
     else nw = anchor;
     uint4 q1 = ZG_LDG(&g.rec[e1.y]);
     uint32_t sufn = (q1.x == nw) ? q1.z : q1.w;  // entries after e1 in nw's list
-    int64_t endn = ZG_LDG(&g.off[nw + 1]);
-    int64_t lbn;
+    uint32_t endn = ZG_LDG(&g.off32[nw + 1]);
+    uint32_t lbn;
     if (sel == 1) {
       // edges [e0, e1]: min_valid = id1 + 1
-      lbn = endn - (int64_t)sufn;
+      lbn = endn - (uint32_t)sufn;
     } else {
       // edges [e0]: min_valid = id0 + 1, at or before e1's own slot in nw's list
-      int64_t pos1 = endn - (int64_t)sufn - 1;
-      lbn = lb_eid(g.adj_e, ZG_LDG(&g.off[nw]), pos1 + 1, (uint32_t)e0 + 1);
+      uint32_t pos1 = endn - (uint32_t)sufn - 1;
+      lbn = lb_eid(g.adj_e, ZG_LDG(&g.off32[nw]), pos1 + 1, (uint32_t)e0 + 1);
     }
     S2 = (uint64_t)(endn - lbn);
     if (DBG) c.sectors += model_anchor(g, nw);
@@ -464,7 +460,7 @@ __device__ void prog_four_chain(const ZgDevGraph& g, Ctx& c, Res& r) {
     }
     if (DBG) c.sectors += 1;
     uint64_t r2 = c.draw(0, S2 - 1);
-    uint2 e2 = ZG_LDG(&g.adj_e[lbn + (int64_t)r2]);
+    uint2 e2 = ZG_LDG(&g.adj_e[lbn + (uint32_t)r2]);
     a2 = 1 + (e2.x == nw);
     res_mul(r, S2);
     if (a2 == 2) r.shift++;
@@ -480,7 +476,7 @@ __device__ void prog_four_chain(const ZgDevGraph& g, Ctx& c, Res& r) {
     }
     if (DBG) c.sectors += 1;
     uint64_t r1 = c.draw(0, S1 - 1);
-    uint2 e1 = ZG_LDG(&g.adj_e[ZG_LDG(&g.off[a + 1]) - (int64_t)q.z + (int64_t)r1]);
+    uint2 e1 = ZG_LDG(&g.adj_e[ZG_LDG(&g.off32[a + 1]) - (uint32_t)q.z + (uint32_t)r1]);
     a1 = 1 + (e1.x == a);
     res_mul(r, S1);
     if (a1 == 2) r.shift++;
@@ -492,7 +488,7 @@ __device__ void prog_four_chain(const ZgDevGraph& g, Ctx& c, Res& r) {
     }
     if (DBG) c.sectors += 1;
     uint64_t r2 = c.draw(0, S2 - 1);
-    uint2 e2 = ZG_LDG(&g.adj_e[ZG_LDG(&g.off[b + 1]) - (int64_t)q.w + (int64_t)r2]);
+    uint2 e2 = ZG_LDG(&g.adj_e[ZG_LDG(&g.off32[b + 1]) - (uint32_t)q.w + (uint32_t)r2]);
     a2 = 1 + (e2.x == b);
     res_mul(r, S2);
     if (a2 == 2) r.shift++;
@@ -542,9 +538,9 @@ __device__ void prog_chain(const ZgDevGraph& g, int order, Ctx& c, Res& r) {
   vs[0] = q.x;
   vs[1] = q.y;
   uint32_t f[2] = {q.x, q.y};
-  int64_t fe[2], fl[2];
-  fe[0] = ZG_LDG(&g.off[q.x + 1]);
-  fe[1] = ZG_LDG(&g.off[q.y + 1]);
+  uint32_t fe[2], fl[2];
+  fe[0] = ZG_LDG(&g.off32[q.x + 1]);
+  fe[1] = ZG_LDG(&g.off32[q.y + 1]);
   fl[0] = fe[0] - q.z;
   fl[1] = fe[1] - q.w;
   Ext p;
@@ -566,7 +562,7 @@ __device__ void prog_chain(const ZgDevGraph& g, int order, Ctx& c, Res& r) {
       rr -= l0;
       side = 1;
     }
-    uint2 e = ZG_LDG(&g.adj_e[fl[side] + (int64_t)rr]);
+    uint2 e = ZG_LDG(&g.adj_e[fl[side] + (uint32_t)rr]);
     uint32_t src = f[side];
     uint32_t av = (f[0] == src) + (f[1] == src) + (f[0] == e.x) + (f[1] == e.x);
     res_mul(r, S);
@@ -586,9 +582,9 @@ __device__ void prog_chain(const ZgDevGraph& g, int order, Ctx& c, Res& r) {
     f[upd] = e.x;
     uint4 qe = ZG_LDG(&g.rec[e.y]);
     uint32_t sufe = (qe.x == e.x) ? qe.z : qe.w;
-    fe[upd] = ZG_LDG(&g.off[e.x + 1]);
-    int64_t pos = fe[upd] - (int64_t)sufe - 1;  // e's own slot in the new frontier's list
-    fl[upd] = lb_eid(g.adj_e, ZG_LDG(&g.off[e.x]), pos + 1, mv);
+    fe[upd] = ZG_LDG(&g.off32[e.x + 1]);
+    uint32_t pos = fe[upd] - (uint32_t)sufe - 1;  // e's own slot in the new frontier's list
+    fl[upd] = lb_eid(g.adj_e, ZG_LDG(&g.off32[e.x]), pos + 1, mv);
   }
   r.hit = true;
   if (DBG) r.w = ext_to_double(ext_inv(p));
@@ -615,13 +611,13 @@ __device__ void prog_pattern(const ZgDevGraph& g, const ZgProgParams& pp, Ctx& c
   uint4 q = ZG_LDG(&g.rec[e0]);
   const int MV = ZG_MAX_PATTERN_V + 1;
   uint32_t vs[MV];
-  int64_t vl[MV], ve[MV];
+  uint32_t vl[MV], ve[MV];
   uint32_t es[ZG_MAX_LIST], ed[ZG_MAX_LIST], ei[ZG_MAX_LIST];
   int nvtx = 2, ne = 1;
   vs[0] = q.x;
   vs[1] = q.y;
-  ve[0] = ZG_LDG(&g.off[q.x + 1]);
-  ve[1] = ZG_LDG(&g.off[q.y + 1]);
+  ve[0] = ZG_LDG(&g.off32[q.x + 1]);
+  ve[1] = ZG_LDG(&g.off32[q.y + 1]);
   vl[0] = ve[0] - q.z;
   vl[1] = ve[1] - q.w;
   es[0] = q.x;
@@ -648,7 +644,7 @@ __device__ void prog_pattern(const ZgDevGraph& g, const ZgProgParams& pp, Ctx& c
       if (rr < len) break;
       rr -= len;
     }
-    uint2 e = ZG_LDG(&g.adj_e[vl[side] + (int64_t)rr]);
+    uint2 e = ZG_LDG(&g.adj_e[vl[side] + (uint32_t)rr]);
     uint32_t src = vs[side];
     int nbr_slot = -1;
     for (int i = 0; i < nvtx; ++i)
@@ -666,9 +662,9 @@ __device__ void prog_pattern(const ZgDevGraph& g, const ZgProgParams& pp, Ctx& c
       vs[nvtx] = e.x;
       uint4 qe = ZG_LDG(&g.rec[e.y]);
       uint32_t sufe = (qe.x == e.x) ? qe.z : qe.w;
-      ve[nvtx] = ZG_LDG(&g.off[e.x + 1]);
-      int64_t pos = ve[nvtx] - (int64_t)sufe - 1;
-      vl[nvtx] = lb_eid(g.adj_e, ZG_LDG(&g.off[e.x]), pos + 1, mv);
+      ve[nvtx] = ZG_LDG(&g.off32[e.x + 1]);
+      uint32_t pos = ve[nvtx] - (uint32_t)sufe - 1;
+      vl[nvtx] = lb_eid(g.adj_e, ZG_LDG(&g.off32[e.x]), pos + 1, mv);
       ++nvtx;
       if ((uint32_t)nvtx > pp.pv) return;
     }
@@ -717,10 +713,26 @@ __device__ __forceinline__ void acc_init(Acc& a) {
   a.sw = a.sw2 = 0.0;
 }
 
-__device__ __forceinline__ double u192_to_double(const ZgU192& n) {
-  // exact enough for the variance sum: top two non-zero limbs
-  if (n.l[2]) return fma(u2d(n.l[2]), 0x1p128, u2d(n.l[1]) * 0x1p64);
-  return fma(u2d(n.l[1]), 0x1p64, u2d(n.l[0]));
+// num / 2^shift as a double truncated to 53 bits, built from integer operations only: GB300's
+// FP64 pipe is narrow, and this runs once per hit (the variance terms; the mean is exact).
+__device__ __forceinline__ double u192_scaled_to_double(const ZgU192& n, uint32_t shift) {
+  uint64_t top = n.l[0], next = 0;
+  int base = 0;
+  if (n.l[2]) {
+    top = n.l[2];
+    next = n.l[1];
+    base = 128;
+  } else if (n.l[1]) {
+    top = n.l[1];
+    next = n.l[0];
+    base = 64;
+  }
+  if (top == 0) return 0.0;
+  int lz = __clzll(top);
+  uint64_t mant = (top << lz) | (lz ? next >> (64 - lz) : 0ull);
+  int64_t e = (int64_t)base + 63 - lz - (int64_t)shift;  // value = mant * 2^(e - 63)
+  uint64_t bits = ((uint64_t)(e + 1023) << 52) | ((mant >> 11) & ((1ull << 52) - 1));
+  return __longlong_as_double((long long)bits);
 }
 
 __device__ __forceinline__ void acc_add(Acc& a, const Res& r, uint32_t den) {
@@ -740,7 +752,7 @@ __device__ __forceinline__ void acc_add(Acc& a, const Res& r, uint32_t den) {
       "addc.u64 %3, %3, %7;"
       : "+l"(a.s[0]), "+l"(a.s[1]), "+l"(a.s[2]), "+l"(a.s[3])
       : "l"(v0), "l"(v1), "l"(v2), "l"(v3));
-  double w = ldexp(u192_to_double(r.num), -(int)r.shift);
+  double w = u192_scaled_to_double(r.num, r.shift);
   a.sw += w;
   a.sw2 = fma(w, w, a.sw2);
 }
@@ -923,12 +935,10 @@ __global__ void __launch_bounds__(kBlock) k_three_motif(ZgDevGraph g, uint64_t n
           res_mul(r, S);
           r.hit = true;
           if (i < n_tri) {
-            int64_t bo = ZG_LDG(&g.off[other]), eo = ZG_LDG(&g.off[other + 1]);
-            uint2 e1 = ZG_LDG(&g.adj_e[ZG_LDG(&g.off[anchor + 1]) - (int64_t)suf + (int64_t)r1]);
+            uint2 e1 = ZG_LDG(&g.adj_e[ZG_LDG(&g.off32[anchor + 1]) - (uint32_t)suf + (uint32_t)r1]);
             uint32_t a1 = 1 + (e1.x == q.x || e1.x == q.y);
             if (a1 == 2) r.shift = 1;
-            int64_t bc = ZG_LDG(&g.off[e1.x]), ec = ZG_LDG(&g.off[e1.x + 1]);
-            rt.hit = a1 == 1 && edge_after(bo, eo, bc, ec, other, e1.x, e1.y + 1, g.adj_n);
+            rt.hit = a1 == 1 && edge_after(g, other, e1.x, e1.y + 1);
             if (DBG) tri_sectors = model_close(g, other, e1.x);
             rt.num = r.num;
             rt.shift = r.shift;

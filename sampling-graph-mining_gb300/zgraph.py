@@ -356,6 +356,10 @@ class Program:
         check(lib().zg_tune(graph.handle, self._h, probe_samples, cuda_stream, C.byref(best), ms))
         return best.value, [float(ms[i]) for i in range(6)]
 
+    def set_variant(self, variant):
+        """zg_set_variant: fix this program kind's launch shape (0..ZG_VARIANTS-1)."""
+        check(lib().zg_set_variant(self.kind, int(variant)))
+
     def variant(self):
         v, mb, g = C.c_int(), C.c_int(), C.c_int()
         check(lib().zg_get_variant(self.kind, C.byref(v), C.byref(mb), C.byref(g)))
