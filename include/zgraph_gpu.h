@@ -95,8 +95,9 @@ typedef struct zg_counters {
   uint32_t den_log2;
   uint32_t overflow;       /* non-zero: some numerator exceeded 192 bits            */
   uint64_t sum_num[5];
-  double   sum_w;          /* sum of 1/p as doubles (fixed block order)             */
-  double   sum_w2;         /* sum of (1/p)^2 as doubles                             */
+  double   sum_w;          /* sum of 1/p: the exact sum, rounded once to double     */
+  double   sum_w2;         /* sum of (1/p)^2 in double (fixed block order); each 1/p
+                              truncated to 53 bits first: the variance term          */
   double   estimate;       /* exact mean, rounded once to double                    */
   double   reserved;
 } zg_counters;

@@ -126,63 +126,63 @@ __global__ void k_off32(const int64_t* __restrict__ off, uint64_t n, uint32_t* _
     off32[i] = (uint32_t)off[i];
 }
 
-// Bucketed two-choice cuckoo insertion of every edge's key.  A thread claims an empty slot of
-// either bucket with atomicCAS; when both are full it swaps its key into a slot (atomicExch) and
-// carries the evicted key to that key's other bucket.  After kMaxKicks swaps it gives up and
-// raises *fail: the host rebuilds with new hash seeds (every loop here is bounded).
+// Bucketed two-choice cuckoo insertion of every edge's entry (fingerprint << 32 | edge id).  A
+// thread claims an empty slot of either bucket with atomicCAS; when both are full it swaps its
+// entry into a slot (atomicExch) and carries the evicted entry to that entry's other bucket (its
+// key is rebuilt from rec).  After kMaxKicks swaps it gives up and raises *fail: the host rebuilds
+// with new hash seeds.  Every loop here is bounded.
 constexpr int kMaxKicks = 128;
 
-__device__ __forceinline__ bool cuckoo_try(unsigned long long* keys, uint32_t b, unsigned long long k) {
+__device__ __forceinline__ bool cuckoo_try(unsigned long long* ent, uint32_t b, unsigned long long x) {
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
-    unsigned long long* slot = &keys[4 * (uint64_t)b + j];
+    unsigned long long* slot = &ent[4 * (uint64_t)b + j];
     if (*(volatile unsigned long long*)slot != ZG_HASH_EMPTY) continue;
-    if (atomicCAS(slot, ZG_HASH_EMPTY, k) == ZG_HASH_EMPTY) return true;
+    if (atomicCAS(slot, ZG_HASH_EMPTY, x) == ZG_HASH_EMPTY) return true;
   }
   return false;
 }
 
-__global__ void k_cuckoo_insert(const uint4* __restrict__ rec, uint64_t m, unsigned long long* keys, uint32_t bits,
+__global__ void k_cuckoo_insert(const uint4* __restrict__ rec, uint64_t m, unsigned long long* ent, uint32_t bits,
                                 uint64_t seed, unsigned int* __restrict__ fail) {
   for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < m; e += (uint64_t)gridDim.x * blockDim.x) {
     uint4 r = rec[e];
     unsigned long long k = zg_edge_key(r.x, r.y);
-    uint32_t from = 0xFFFFFFFFu;  // the bucket the carried key was evicted from
+    unsigned long long x = ((unsigned long long)zg_fingerprint(k, seed) << 32) | e;
+    uint32_t from = 0xFFFFFFFFu;  // the bucket the carried entry was evicted from
     bool placed = false;
     for (int kick = 0; kick < kMaxKicks; ++kick) {
       uint32_t b1 = zg_bucket1(k, seed, bits), b2 = zg_bucket2(k, seed, bits);
-      if (cuckoo_try(keys, b1, k) || (b2 != b1 && cuckoo_try(keys, b2, k))) {
+      if (cuckoo_try(ent, b1, x) || (b2 != b1 && cuckoo_try(ent, b2, x))) {
         placed = true;
         break;
       }
       uint32_t vb = from == b1 ? b2 : from == b2 ? b1 : (((e + kick) & 1) ? b2 : b1);
-      unsigned long long old = atomicExch(&keys[4 * (uint64_t)vb + ((e + (uint64_t)kick) & 3)], k);
+      unsigned long long old = atomicExch(&ent[4 * (uint64_t)vb + ((e + (uint64_t)kick) & 3)], x);
       if (old == ZG_HASH_EMPTY) {
         placed = true;
         break;
       }
-      k = old;
+      x = old;
+      uint4 ro = rec[(uint32_t)old];
+      k = zg_edge_key(ro.x, ro.y);
       from = vb;
     }
     if (!placed) atomicOr(fail, 1u);
   }
 }
 
-// Edge ids beside the keys; a key not found means the insertion lost it (fail).
-__global__ void k_cuckoo_fill(const uint4* __restrict__ rec, uint64_t m, const unsigned long long* __restrict__ keys,
-                              uint32_t bits, uint64_t seed, uint32_t* __restrict__ eid, unsigned int* __restrict__ fail) {
+// Every edge must be found in one of its two buckets (an insertion that gave up lost one).
+__global__ void k_cuckoo_check(const uint4* __restrict__ rec, uint64_t m, const unsigned long long* __restrict__ ent,
+                               uint32_t bits, uint64_t seed, unsigned int* __restrict__ fail) {
   for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < m; e += (uint64_t)gridDim.x * blockDim.x) {
     uint4 r = rec[e];
     unsigned long long k = zg_edge_key(r.x, r.y);
+    unsigned long long x = ((unsigned long long)zg_fingerprint(k, seed) << 32) | e;
     uint32_t bs[2] = {zg_bucket1(k, seed, bits), zg_bucket2(k, seed, bits)};
     bool found = false;
-    for (int i = 0; i < 2 && !found; ++i)
-      for (int j = 0; j < 4; ++j)
-        if (keys[4 * (uint64_t)bs[i] + j] == k) {
-          eid[4 * (uint64_t)bs[i] + j] = (uint32_t)e;
-          found = true;
-          break;
-        }
+    for (int i = 0; i < 2; ++i)
+      for (int j = 0; j < 4; ++j) found |= ent[4 * (uint64_t)bs[i] + j] == x;
     if (!found) atomicOr(fail, 1u);
   }
 }
@@ -200,30 +200,26 @@ int build_hash(zg_graph* g, cudaStream_t s) {
   for (int attempt = 0; attempt < 8; ++attempt) {
     if (attempt && attempt % 4 == 0) ++bits;
     const uint64_t slots = 4ull << bits;
-    if (g->hkeys) cudaFree(g->hkeys);
-    if (g->heid) cudaFree(g->heid);
-    g->hkeys = nullptr;
-    g->heid = nullptr;
-    if ((rc = dev_alloc(&g->hkeys, slots)) || (rc = dev_alloc(&g->heid, slots))) return rc;
+    if (g->hent) cudaFree(g->hent);
+    g->hent = nullptr;
+    if ((rc = dev_alloc(&g->hent, slots))) return rc;
     uint64_t seed = zg_mix64(0x5A4748415348ull + attempt);
     cudaError_t ce;
-    if ((ce = cudaMemsetAsync(g->hkeys, 0xFF, sizeof(unsigned long long) * slots, s)) ||
-        (ce = cudaMemsetAsync(g->heid, 0xFF, sizeof(uint32_t) * slots, s)) ||
+    if ((ce = cudaMemsetAsync(g->hent, 0xFF, sizeof(unsigned long long) * slots, s)) ||
         (ce = cudaMemsetAsync(fail.p, 0, sizeof(unsigned int), s)))
       return zg_check_cuda(ce, "hash memset");
     if (m) {
-      k_cuckoo_insert<<<grid_for(m, B), B, 0, s>>>(g->rec, m, g->hkeys, bits, seed, fail.as<unsigned int>());
-      k_cuckoo_fill<<<grid_for(m, B), B, 0, s>>>(g->rec, m, g->hkeys, bits, seed, g->heid, fail.as<unsigned int>());
+      k_cuckoo_insert<<<grid_for(m, B), B, 0, s>>>(g->rec, m, g->hent, bits, seed, fail.as<unsigned int>());
+      k_cuckoo_check<<<grid_for(m, B), B, 0, s>>>(g->rec, m, g->hent, bits, seed, fail.as<unsigned int>());
     }
     unsigned int hf = 0;
     if ((ce = cudaMemcpyAsync(&hf, fail.p, sizeof(hf), cudaMemcpyDeviceToHost, s)) || (ce = cudaStreamSynchronize(s)))
       return zg_check_cuda(ce, "hash build");
     if (!hf) {
-      g->d.hkeys = g->hkeys;
-      g->d.heid = g->heid;
+      g->d.hent = g->hent;
       g->d.hbits = bits;
       g->d.hseed = seed;
-      g->bytes += slots * (sizeof(unsigned long long) + sizeof(uint32_t));
+      g->bytes += slots * sizeof(unsigned long long);
       return ZG_OK;
     }
   }
@@ -590,8 +586,7 @@ extern "C" int zg_graph_free(zg_graph* g) {
   if (g->rec) cudaFree(g->rec);
   if (g->off) cudaFree(g->off);
   if (g->off32) cudaFree(g->off32);
-  if (g->hkeys) cudaFree(g->hkeys);
-  if (g->heid) cudaFree(g->heid);
+  if (g->hent) cudaFree(g->hent);
   if (g->adj_e) cudaFree(g->adj_e);
   if (g->adj_n) cudaFree(g->adj_n);
   if (g->w) cudaFree(g->w);

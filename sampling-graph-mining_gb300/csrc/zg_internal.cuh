@@ -11,10 +11,11 @@
 //   adj_n[2m] uint2 (nbr, edge_id) sorted by (nbr, edge_id) per vertex (exports, exact counts).
 //   w[m]      uint32 edge data (Graph<VertexId>) or null.
 //   off32[V+1] the offsets as uint32 (2m < 2^32): what the sampling kernels read.
-//   hkeys[4B] / heid[4B]: the edge set as a two-choice bucketed cuckoo table, B = 2^hbits buckets
-//             of 4 keys (one 32-byte sector); key = (min(u,v) << 32) | max(u,v), heid = its edge
-//             id.  A closure check ("edge (x,y) exists with id >= min_valid") reads two sectors
-//             issued together instead of a binary search of dependent loads.
+//   hent[4B]  the edge set as a two-choice bucketed cuckoo table, B = 2^hbits buckets of 4
+//             entries (one 32-byte sector); entry = (fingerprint << 32) | edge id for the key
+//             (min(u,v) << 32) | max(u,v).  A closure check ("edge (x,y) exists with id >=
+//             min_valid") reads its two buckets together; a fingerprint match is confirmed
+//             against rec[edge id], so the answer is exact.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -35,8 +36,7 @@ struct ZgDevGraph {
   const uint2* adj_n;
   const uint32_t* w;
   const uint32_t* off32;
-  const unsigned long long* hkeys;
-  const uint32_t* heid;
+  const unsigned long long* hent;
   uint64_t hseed;
 };
 
@@ -57,6 +57,11 @@ __host__ __device__ __forceinline__ uint32_t zg_bucket1(uint64_t key, uint64_t s
 __host__ __device__ __forceinline__ uint32_t zg_bucket2(uint64_t key, uint64_t seed, uint32_t bits) {
   return (uint32_t)(zg_mix64(key ^ (seed * 0x9E3779B97F4A7C15ull + 0x632BE59BD9B4E019ull)) >> (64 - bits));
 }
+// Never 0xFFFFFFFF, the fingerprint field of an empty entry.
+__host__ __device__ __forceinline__ uint32_t zg_fingerprint(uint64_t key, uint64_t seed) {
+  uint32_t f = (uint32_t)(zg_mix64(key + seed + 0xD6E8FEB86659FD93ull) >> 32);
+  return f == 0xFFFFFFFFu ? 0x7FFFFFFFu : f;
+}
 
 struct zg_graph {
   ZgDevGraph d;
@@ -66,8 +71,7 @@ struct zg_graph {
   uint2* adj_n;
   uint32_t* w;
   uint32_t* off32;
-  unsigned long long* hkeys;
-  uint32_t* heid;
+  unsigned long long* hent;
   uint64_t num_edges;   // Graph::num_edges metadata
   uint64_t max_degree;  // Graph::max_degree metadata
   uint64_t bytes;

@@ -63,43 +63,99 @@ __device__ __forceinline__ void res_mul(Res& r, uint64_t f) {
   if (zg_u192_mul(r.num, f)) r.ovf = true;
 }
 
-// first index in adj_e[lo, hi) whose edge id >= key
-__device__ __forceinline__ uint32_t lb_eid(const uint2* __restrict__ adj, uint32_t lo, uint32_t hi, uint32_t key) {
-  while (lo < hi) {
-    uint32_t mid = lo + ((hi - lo) >> 1);
-    if (ZG_LDG(&adj[mid]).y < key)
-      lo = mid + 1;
-    else
-      hi = mid;
+// First index in adj_e[lo, hi) whose edge id >= key, where every edge id in the range is known
+// to lie in [vlo, vhi].  The build shuffles the edge ids (a uniformly random permutation), so an
+// edge-id-ordered list is a sorted uniform sample of [0, m): interpolation finds the bound in
+// O(log log d) expected probes instead of log2 d.  After 8 interpolation probes it bisects, which
+// bounds the worst case (unshuffled input) by 8 + log2 d probes.
+__device__ __forceinline__ uint32_t lb_eid(const uint2* __restrict__ adj, uint32_t lo, uint32_t hi, uint32_t key,
+                                           uint32_t vlo, uint32_t vhi) {
+  for (int it = 0; hi - lo > 4; ++it) {
+    if (key <= vlo) return lo;  // every id in the range is >= key
+    if (key > vhi) return hi;   // every id in the range is < key
+    uint32_t n = hi - lo, p;
+    if (it < 8) {
+      float f = __fdividef((float)(key - vlo), (float)(vhi - vlo) + 1.0f);
+      uint32_t est = (uint32_t)(f * (float)n);
+      p = lo + (est < n ? est : n - 1);
+    } else {
+      p = lo + (n >> 1);
+    }
+    uint32_t v = ZG_LDG(&adj[p]).y;
+    if (v < key) {
+      lo = p + 1;
+      vlo = v + 1;
+    } else {
+      hi = p;
+      vhi = v - 1;  // v >= key > vlo >= 0
+    }
   }
-  return lo;
+  // at most 4 entries left (sorted): load them together and count those below the key
+  uint32_t n = hi - lo, below = 0;
+#pragma unroll
+  for (uint32_t i = 0; i < 4; ++i)
+    if (i < n) below += ZG_LDG(&adj[lo + i]).y < key;
+  return lo + below;
 }
 
 // Does edge (x,y) exist with edge id >= min_valid?  conditional_close's question
 // (src/ZGraphInstance.cpp:372-407): the pattern edges still to close join two sampled vertices,
 // so "found in some sampled vertex's list with id >= min_valid" is "edge (x,y) exists with such
 // an id".  Answered by the cuckoo table: both candidate buckets (one 32-byte sector each) are
-// read together, and the edge id only when the key is present.
-__device__ __forceinline__ int64_t edge_slot(const ZgDevGraph& g, uint32_t x, uint32_t y) {
-  unsigned long long k = zg_edge_key(x, y);
-  uint64_t b1 = 4ull * zg_bucket1(k, g.hseed, g.hbits), b2 = 4ull * zg_bucket2(k, g.hseed, g.hbits);
-  const ulonglong2* p1 = reinterpret_cast<const ulonglong2*>(g.hkeys + b1);
-  const ulonglong2* p2 = reinterpret_cast<const ulonglong2*>(g.hkeys + b2);
+// read together; a fingerprint match is confirmed against rec, so the answer is exact.
+// Two phases, so a caller with several look-ups can stop before any dependent load:
+// edge_candidate() reads the two buckets and returns the first entry whose fingerprint matches
+// (or the empty marker: then the edge does not exist); edge_confirm() checks the candidate
+// against rec and, in the rare case of a second fingerprint match, rescans.  The result is the
+// edge id, or -1 when the edge does not exist.
+struct EdgeProbe {
+  unsigned long long key, cand;
+};
+
+__device__ __forceinline__ EdgeProbe edge_candidate(const ZgDevGraph& g, uint32_t x, uint32_t y) {
+  EdgeProbe pr;
+  pr.key = zg_edge_key(x, y);
+  uint64_t b1 = 4ull * zg_bucket1(pr.key, g.hseed, g.hbits), b2 = 4ull * zg_bucket2(pr.key, g.hseed, g.hbits);
+  const ulonglong2* p1 = reinterpret_cast<const ulonglong2*>(g.hent + b1);
+  const ulonglong2* p2 = reinterpret_cast<const ulonglong2*>(g.hent + b2);
   ulonglong2 a0 = __ldg(p1), a1 = __ldg(p1 + 1), c0 = __ldg(p2), c1 = __ldg(p2 + 1);
-  int64_t slot = -1;
-  if (a0.x == k) slot = (int64_t)b1;
-  if (a0.y == k) slot = (int64_t)b1 + 1;
-  if (a1.x == k) slot = (int64_t)b1 + 2;
-  if (a1.y == k) slot = (int64_t)b1 + 3;
-  if (c0.x == k) slot = (int64_t)b2;
-  if (c0.y == k) slot = (int64_t)b2 + 1;
-  if (c1.x == k) slot = (int64_t)b2 + 2;
-  if (c1.y == k) slot = (int64_t)b2 + 3;
-  return slot;
+  uint32_t fp = zg_fingerprint(pr.key, g.hseed);
+  // an empty entry never matches: no fingerprint is 0xFFFFFFFF
+  unsigned long long e = ZG_HASH_EMPTY;
+  e = (uint32_t)(c1.y >> 32) == fp ? c1.y : e;
+  e = (uint32_t)(c1.x >> 32) == fp ? c1.x : e;
+  e = (uint32_t)(c0.y >> 32) == fp ? c0.y : e;
+  e = (uint32_t)(c0.x >> 32) == fp ? c0.x : e;
+  e = (uint32_t)(a1.y >> 32) == fp ? a1.y : e;
+  e = (uint32_t)(a1.x >> 32) == fp ? a1.x : e;
+  e = (uint32_t)(a0.y >> 32) == fp ? a0.y : e;
+  e = (uint32_t)(a0.x >> 32) == fp ? a0.x : e;
+  pr.cand = e;
+  return pr;
 }
+
+// another entry of the two buckets with the same fingerprint (probability ~ 8 / 2^32 a look-up)
+__device__ __noinline__ int64_t edge_rescan(const ZgDevGraph& g, unsigned long long key, unsigned long long cand) {
+  uint64_t b1 = 4ull * zg_bucket1(key, g.hseed, g.hbits), b2 = 4ull * zg_bucket2(key, g.hseed, g.hbits);
+  uint32_t fp = zg_fingerprint(key, g.hseed);
+  for (int i = 0; i < 8; ++i) {
+    unsigned long long x = ZG_LDG(&g.hent[(i < 4 ? b1 : b2) + (i & 3)]);
+    if (x == cand || (uint32_t)(x >> 32) != fp) continue;
+    uint4 q = ZG_LDG(&g.rec[(uint32_t)x]);
+    if (zg_edge_key(q.x, q.y) == key) return (int64_t)(uint32_t)x;
+  }
+  return -1;
+}
+
+__device__ __forceinline__ int64_t edge_confirm(const ZgDevGraph& g, const EdgeProbe& pr) {
+  if (pr.cand == ZG_HASH_EMPTY) return -1;
+  uint4 r = ZG_LDG(&g.rec[(uint32_t)pr.cand]);
+  if (zg_edge_key(r.x, r.y) == pr.key) return (int64_t)(uint32_t)pr.cand;
+  return edge_rescan(g, pr.key, pr.cand);
+}
+
 __device__ __forceinline__ bool edge_after(const ZgDevGraph& g, uint32_t x, uint32_t y, uint32_t min_valid) {
-  int64_t slot = edge_slot(g, x, y);
-  return slot >= 0 && ZG_LDG(&g.heid[slot]) >= min_valid;
+  return edge_confirm(g, edge_candidate(g, x, y)) >= (int64_t)min_valid;
 }
 
 // ---- access model (debug): algorithmic bytes of a sample in 32-byte sectors ---------------
@@ -329,7 +385,9 @@ __device__ void prog_four_clique(const ZgDevGraph& g, Ctx& c, Res& r) {
   uint32_t endC = ZG_LDG(&g.off32[vc + 1]);
   uint32_t lbC = endC - ((q1.x == vc) ? q1.z : q1.w);
   // the anchor's own list continues right after e1; the other endpoint's list needs a search
-  uint32_t lo = lb_eid(g.adj_e, s1b ? endA - q.z : endB - q.w, s1b ? endA : endB, mv);
+  // (that suffix holds edge ids in [id0 + 1, m - 1])
+  uint32_t lo = lb_eid(g.adj_e, s1b ? endA - q.z : endB - q.w, s1b ? endA : endB, mv, (uint32_t)e0 + 1,
+                       (uint32_t)(g.m - 1));
   uint32_t lbA = s1b ? lo : idx1 + 1, lbB = s1b ? idx1 + 1 : lo;
   uint64_t lenA = endA - lbA, lenB = endB - lbB;
   // when c coincides with a or b (duplicate edges) the reference lists only two vertices
@@ -382,9 +440,11 @@ __device__ void prog_four_clique(const ZgDevGraph& g, Ctx& c, Res& r) {
     uint32_t x0 = s1b ? va : vb;             // the pair (not-anchor-of-e1, c)
     uint32_t x1 = vslot(s2 == 0 ? 1 : 0);    // the two pairs (?, d) other than e2's own
     uint32_t x2 = vslot(s2 == 2 ? 1 : 2);
-    int64_t h0 = edge_slot(g, x0, vc), h1 = edge_slot(g, x1, vd), h2 = edge_slot(g, x2, vd);
-    ok = h0 >= 0 && h1 >= 0 && h2 >= 0;
-    if (ok) ok = ZG_LDG(&g.heid[h0]) >= mv2 && ZG_LDG(&g.heid[h1]) >= mv2 && ZG_LDG(&g.heid[h2]) >= mv2;
+    EdgeProbe p0 = edge_candidate(g, x0, vc), p1 = edge_candidate(g, x1, vd), p2 = edge_candidate(g, x2, vd);
+    ok = p0.cand != ZG_HASH_EMPTY && p1.cand != ZG_HASH_EMPTY && p2.cand != ZG_HASH_EMPTY;
+    if (ok)
+      ok = edge_confirm(g, p0) >= (int64_t)mv2 && edge_confirm(g, p1) >= (int64_t)mv2 &&
+           edge_confirm(g, p2) >= (int64_t)mv2;
   }
   r.hit = ok;
   if (DBG && ok) {
@@ -450,7 +510,7 @@ __device__ void prog_four_chain(const ZgDevGraph& g, Ctx& c, Res& r) {
     } else {
       // edges [e0]: min_valid = id0 + 1, at or before e1's own slot in nw's list
       uint32_t pos1 = endn - (uint32_t)sufn - 1;
-      lbn = lb_eid(g.adj_e, ZG_LDG(&g.off32[nw]), pos1 + 1, (uint32_t)e0 + 1);
+      lbn = lb_eid(g.adj_e, ZG_LDG(&g.off32[nw]), pos1 + 1, (uint32_t)e0 + 1, 0u, e1.y);
     }
     S2 = (uint64_t)(endn - lbn);
     if (DBG) c.sectors += model_anchor(g, nw);
@@ -584,7 +644,7 @@ __device__ void prog_chain(const ZgDevGraph& g, int order, Ctx& c, Res& r) {
     uint32_t sufe = (qe.x == e.x) ? qe.z : qe.w;
     fe[upd] = ZG_LDG(&g.off32[e.x + 1]);
     uint32_t pos = fe[upd] - (uint32_t)sufe - 1;  // e's own slot in the new frontier's list
-    fl[upd] = lb_eid(g.adj_e, ZG_LDG(&g.off32[e.x]), pos + 1, mv);
+    fl[upd] = lb_eid(g.adj_e, ZG_LDG(&g.off32[e.x]), pos + 1, mv, 0u, e.y);
   }
   r.hit = true;
   if (DBG) r.w = ext_to_double(ext_inv(p));
@@ -664,7 +724,7 @@ __device__ void prog_pattern(const ZgDevGraph& g, const ZgProgParams& pp, Ctx& c
       uint32_t sufe = (qe.x == e.x) ? qe.z : qe.w;
       ve[nvtx] = ZG_LDG(&g.off32[e.x + 1]);
       uint32_t pos = ve[nvtx] - (uint32_t)sufe - 1;
-      vl[nvtx] = lb_eid(g.adj_e, ZG_LDG(&g.off32[e.x]), pos + 1, mv);
+      vl[nvtx] = lb_eid(g.adj_e, ZG_LDG(&g.off32[e.x]), pos + 1, mv, 0u, e.y);
       ++nvtx;
       if ((uint32_t)nvtx > pp.pv) return;
     }
@@ -752,8 +812,8 @@ __device__ __forceinline__ void acc_add(Acc& a, const Res& r, uint32_t den) {
       "addc.u64 %3, %3, %7;"
       : "+l"(a.s[0]), "+l"(a.s[1]), "+l"(a.s[2]), "+l"(a.s[3])
       : "l"(v0), "l"(v1), "l"(v2), "l"(v3));
+  // sum_w is taken from the exact integer sum at the end; only the square needs the FP64 pipe
   double w = u192_scaled_to_double(r.num, r.shift);
-  a.sw += w;
   a.sw2 = fma(w, w, a.sw2);
 }
 
@@ -1111,7 +1171,7 @@ void partial_to_counters(const ZgPartial& p, uint32_t den, zg_counters* out) {
     out->sum_num[i] = (uint64_t)acc;
     carry = acc >> 64;
   }
-  out->sum_w = p.sum_w;
+  out->sum_w = exact_mean(out->sum_num, den, 1);  // the exact sum, rounded once
   out->sum_w2 = p.sum_w2;
   out->estimate = exact_mean(out->sum_num, den, p.samples);
 }
