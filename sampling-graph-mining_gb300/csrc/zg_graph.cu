@@ -243,10 +243,13 @@ int build_graph(const uint2* d_coo, const uint32_t* d_w_in, uint64_t m, uint32_t
     return code;
   };
   uint64_t n2 = 2 * m;
-  if ((rc = dev_alloc(&g->rec, m)) || (rc = dev_alloc(&g->off, (size_t)nv + 1)) ||
-      (rc = dev_alloc(&g->off32, (size_t)nv + 1)) || (rc = dev_alloc(&g->adj_e, n2)) ||
-      (rc = dev_alloc(&g->adj_n, n2)))
+  // adj_e and off32 share one allocation
+  g->hot_bytes = sizeof(uint2) * n2 + sizeof(uint32_t) * ((size_t)nv + 1);
+  if ((rc = dev_alloc((char**)&g->hot, g->hot_bytes)) || (rc = dev_alloc(&g->rec, m)) ||
+      (rc = dev_alloc(&g->off, (size_t)nv + 1)) || (rc = dev_alloc(&g->adj_n, n2)))
     return fail(rc);
+  g->adj_e = (uint2*)g->hot;
+  g->off32 = (uint32_t*)((char*)g->hot + sizeof(uint2) * n2);
   if (d_w_in) {
     if ((rc = dev_alloc(&g->w, m))) return fail(rc);
     if (m) {
@@ -585,9 +588,8 @@ extern "C" int zg_graph_free(zg_graph* g) {
   if (!g) return ZG_OK;
   if (g->rec) cudaFree(g->rec);
   if (g->off) cudaFree(g->off);
-  if (g->off32) cudaFree(g->off32);
   if (g->hent) cudaFree(g->hent);
-  if (g->adj_e) cudaFree(g->adj_e);
+  if (g->hot) cudaFree(g->hot);  // adj_e and off32
   if (g->adj_n) cudaFree(g->adj_n);
   if (g->w) cudaFree(g->w);
   delete g;

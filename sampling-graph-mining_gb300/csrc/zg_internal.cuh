@@ -72,6 +72,8 @@ struct zg_graph {
   uint32_t* w;
   uint32_t* off32;
   unsigned long long* hent;
+  void* hot;            // one allocation holding adj_e then off32 (read together by every program)
+  uint64_t hot_bytes;
   uint64_t num_edges;   // Graph::num_edges metadata
   uint64_t max_degree;  // Graph::max_degree metadata
   uint64_t bytes;

@@ -108,6 +108,11 @@ __device__ __forceinline__ uint32_t lb_eid(const uint2* __restrict__ adj, uint32
 // (or the empty marker: then the edge does not exist); edge_confirm() checks the candidate
 // against rec and, in the rare case of a second fingerprint match, rescans.  The result is the
 // edge id, or -1 when the edge does not exist.
+// One bucket = one 32-byte sector, read with a single 256-bit load (sm_100 family).
+__device__ __forceinline__ void ld_bucket(const unsigned long long* p, ulonglong2& lo, ulonglong2& hi) {
+  asm("ld.global.nc.v4.u64 {%0, %1, %2, %3}, [%4];" : "=l"(lo.x), "=l"(lo.y), "=l"(hi.x), "=l"(hi.y) : "l"(p));
+}
+
 struct EdgeProbe {
   unsigned long long key, cand;
 };
@@ -116,9 +121,9 @@ __device__ __forceinline__ EdgeProbe edge_candidate(const ZgDevGraph& g, uint32_
   EdgeProbe pr;
   pr.key = zg_edge_key(x, y);
   uint64_t b1 = 4ull * zg_bucket1(pr.key, g.hseed, g.hbits), b2 = 4ull * zg_bucket2(pr.key, g.hseed, g.hbits);
-  const ulonglong2* p1 = reinterpret_cast<const ulonglong2*>(g.hent + b1);
-  const ulonglong2* p2 = reinterpret_cast<const ulonglong2*>(g.hent + b2);
-  ulonglong2 a0 = __ldg(p1), a1 = __ldg(p1 + 1), c0 = __ldg(p2), c1 = __ldg(p2 + 1);
+  ulonglong2 a0, a1, c0, c1;
+  ld_bucket(g.hent + b1, a0, a1);
+  ld_bucket(g.hent + b2, c0, c1);
   uint32_t fp = zg_fingerprint(pr.key, g.hseed);
   // an empty entry never matches: no fingerprint is 0xFFFFFFFF
   unsigned long long e = ZG_HASH_EMPTY;
