@@ -231,6 +231,49 @@ int zg_run_three_motif_debug(const zg_graph* g, uint64_t n_chain, uint64_t n_tri
                              uint64_t seed, uint32_t stream_chain, uint32_t stream_tri,
                              zg_sample_trace* chain_traces, zg_sample_trace* tri_traces);
 
+/* ---- batched mixed queries ----------------------------------------------------- */
+/* Many estimator queries of uneven program, predicate and budget in one persistent launch (no
+ * counterpart in the reference, whose applications run one calculate() at a time).  A query runs
+ * n estimators of `kind` (ZG_PROG_TRIANGLE .. ZG_PROG_CHAIN, param = chain order) with sample
+ * indices [0, n) on Philox stream (seed, stream_id), on the batch's base graph or, when pred_op
+ * != 0, on the base graph filtered by (pred_op, t0, t1) as AllPredicateZGraphInstance does
+ * (src/ZGraphInstance.cpp:492-525).  ZG_QUERY_THREE_MOTIF runs ThreeMotif's pair: n 3-chain
+ * estimators and the triangle estimators that close their wedges (zg_run_three_motif with
+ * n_chain = n_tri = n).  Results equal zg_run's (zg_run_three_motif's) on the same draws, exactly,
+ * except sum_w2, which is summed in a different (fixed) order. */
+#define ZG_QUERY_THREE_MOTIF   16
+#define ZG_BATCH_MAX_QUERIES   65536
+#define ZG_BATCH_MAX_CHUNKS    65536   /* work items of 2^k samples, k >= 12 chosen per batch */
+typedef struct zg_batch_query {
+  int32_t  kind;
+  uint32_t param;
+  int32_t  pred_op;        /* 0: base graph; else ZG_PRED_* */
+  uint32_t stream_id;
+  int64_t  t0, t1;
+  uint64_t n;
+  uint64_t seed;
+} zg_batch_query;
+typedef struct zg_batch zg_batch;
+/* A batch engine over base (which must outlive it): capacity max_queries per submit; filtered
+ * graphs are cached up to cache_bytes of device memory (least recently used first out), each
+ * shuffled with a seed derived from filter_seed and its predicate. */
+int zg_batch_create(const zg_graph* base, uint32_t max_queries, uint64_t cache_bytes, uint64_t filter_seed,
+                    zg_batch** out);
+int zg_batch_free(zg_batch* b);
+/* Enqueues the batch on cuda_stream (one CUDA graph launch after any filtered graphs it needs
+ * are built) and returns; a second submit first waits for the previous batch. */
+int zg_batch_submit(zg_batch* b, const zg_batch_query* queries, uint32_t nq, void* cuda_stream);
+/* Waits for the submitted batch; out[2i] receives query i's counters (ZG_QUERY_THREE_MOTIF:
+ * out[2i] the 3-chain, out[2i+1] the triangle). */
+int zg_batch_wait(zg_batch* b, zg_counters* out);
+/* The cached filtered graph of a predicate (built if missing): what a filtered query samples. */
+int zg_batch_filtered_graph(zg_batch* b, int pred_op, int64_t t0, int64_t t1, void* cuda_stream,
+                            const zg_graph** out);
+/* Autotuner of the batch kernel's launch shape (resident blocks 2, 3 or 4 of 256 threads): runs
+ * the batch three times per shape and keeps the fastest; ms_per_variant (may be NULL) gets 3. */
+int zg_batch_tune(zg_batch* b, const zg_batch_query* queries, uint32_t nq, void* cuda_stream, int* best_variant,
+                  float* ms_per_variant);
+
 /* ---- error-latency profiles and bounded queries ------------------------------ */
 /* Draw plan of zg_elp_plain for a given seed: the subsample keeps edge e iff
  * zg_draw(seed + ZG_ELP_KEEP_OFFSET, subsample stream, e) <= 0.1 * 2^30 and is permuted with

@@ -1,0 +1,876 @@
+// zg_programs.cuh — the estimator programs on the device, shared by the sampling kernels
+// (zg_sample.cu) and the batched-query kernel (zg_batch.cu).
+//
+// One estimator (sample) per thread.  Every estimator draws from its own Philox4x32-10 counter
+// stream (seed, stream_id, sample index, draw index), so results do not depend on the launch
+// shape.  Each program restates one application estimate() (cited) on the device layout of
+// zg_internal.cuh:
+//   * the first conditional step reads its suffix sizes S from rec[] (no search);
+//   * later steps find lower bounds by interpolation search inside ranges the per-edge suffix
+//     counts already narrow;
+//   * closure checks (conditional_close, src/ZGraphInstance.cpp:372-407) look the edge up in the
+//     cuckoo table.
+// Weights are exact: numerator m*prod(S_i) (192-bit) over 2^shift.  The debug variant (DBG)
+// additionally records every draw, the access-model sector count and the reference's double 1/p
+// computed with the same IEEE operation sequence as the application (x87 extended arithmetic
+// restated in integers for ChainMining).
+#pragma once
+
+#include "zg_internal.cuh"
+
+// Internal linkage: every translation unit that includes this header gets its own copy.
+namespace {
+
+#define ZG_LDG(p) __ldg(p)
+
+struct Ctx {
+  uint64_t seed;
+  uint64_t sample;
+  uint32_t stream;
+  uint32_t nd;
+  zg_sample_trace* tr;  // debug only
+  uint32_t sectors;     // debug only: access model, 32-byte sectors
+  __device__ __forceinline__ uint64_t draw(uint64_t lo, uint64_t hi) {
+    uint64_t v = zg_draw(seed, stream, sample, nd, lo, hi);
+    if (tr && nd < ZG_MAX_DRAWS) {
+      tr->lo[nd] = lo;
+      tr->hi[nd] = hi;
+      tr->val[nd] = v;
+    }
+    ++nd;
+    return v;
+  }
+};
+
+struct Res {
+  bool hit;
+  bool fail;
+  bool ovf;
+  uint32_t shift;
+  ZgU192 num;
+  double w;  // debug: reference double
+};
+
+__device__ __forceinline__ void res_init(Res& r) {
+  r.hit = false;
+  r.fail = false;
+  r.ovf = false;
+  r.shift = 0;
+  zg_u192_set(r.num, 1);
+  r.w = 0.0;
+}
+__device__ __forceinline__ void res_mul(Res& r, uint64_t f) {
+  if (zg_u192_mul(r.num, f)) r.ovf = true;
+}
+
+// First index in adj_e[lo, hi) whose edge id >= key, where every edge id in the range is known
+// to lie in [vlo, vhi].  The build shuffles the edge ids (a uniformly random permutation), so an
+// edge-id-ordered list is a sorted uniform sample of [0, m): interpolation finds the bound in
+// O(log log d) expected probes instead of log2 d.  After 8 interpolation probes it bisects, which
+// bounds the worst case (unshuffled input) by 8 + log2 d probes.
+__device__ __forceinline__ uint32_t lb_eid(const uint2* __restrict__ adj, uint32_t lo, uint32_t hi, uint32_t key,
+                                           uint32_t vlo, uint32_t vhi) {
+  for (int it = 0; hi - lo > 4; ++it) {
+    if (key <= vlo) return lo;  // every id in the range is >= key
+    if (key > vhi) return hi;   // every id in the range is < key
+    uint32_t n = hi - lo, p;
+    if (it < 8) {
+      float f = __fdividef((float)(key - vlo), (float)(vhi - vlo) + 1.0f);
+      uint32_t est = (uint32_t)(f * (float)n);
+      p = lo + (est < n ? est : n - 1);
+    } else {
+      p = lo + (n >> 1);
+    }
+    uint32_t v = ZG_LDG(&adj[p]).y;
+    if (v < key) {
+      lo = p + 1;
+      vlo = v + 1;
+    } else {
+      hi = p;
+      vhi = v - 1;  // v >= key > vlo >= 0
+    }
+  }
+  // at most 4 entries left (sorted): load them together and count those below the key
+  uint32_t n = hi - lo, below = 0;
+#pragma unroll
+  for (uint32_t i = 0; i < 4; ++i)
+    if (i < n) below += ZG_LDG(&adj[lo + i]).y < key;
+  return lo + below;
+}
+
+// Does edge (x,y) exist with edge id >= min_valid?  conditional_close's question
+// (src/ZGraphInstance.cpp:372-407): the pattern edges still to close join two sampled vertices,
+// so "found in some sampled vertex's list with id >= min_valid" is "edge (x,y) exists with such
+// an id".  Answered by the cuckoo table: both candidate buckets (one 32-byte sector each) are
+// read together; a fingerprint match is confirmed against rec, so the answer is exact.
+// Two phases, so a caller with several look-ups can stop before any dependent load:
+// edge_candidate() reads the two buckets and returns the first entry whose fingerprint matches
+// (or the empty marker: then the edge does not exist); edge_confirm() checks the candidate
+// against rec and, in the rare case of a second fingerprint match, rescans.  The result is the
+// edge id, or -1 when the edge does not exist.
+// One bucket = one 32-byte sector, read with a single 256-bit load (sm_100 family).
+__device__ __forceinline__ void ld_bucket(const unsigned long long* p, ulonglong2& lo, ulonglong2& hi) {
+  asm("ld.global.nc.v4.u64 {%0, %1, %2, %3}, [%4];" : "=l"(lo.x), "=l"(lo.y), "=l"(hi.x), "=l"(hi.y) : "l"(p));
+}
+
+struct EdgeProbe {
+  unsigned long long key, cand;
+};
+
+__device__ __forceinline__ EdgeProbe edge_candidate(const ZgDevGraph& g, uint32_t x, uint32_t y) {
+  EdgeProbe pr;
+  pr.key = zg_edge_key(x, y);
+  uint64_t b1 = 4ull * zg_bucket1(pr.key, g.hseed, g.hbits), b2 = 4ull * zg_bucket2(pr.key, g.hseed, g.hbits);
+  ulonglong2 a0, a1, c0, c1;
+  ld_bucket(g.hent + b1, a0, a1);
+  ld_bucket(g.hent + b2, c0, c1);
+  uint32_t fp = zg_fingerprint(pr.key, g.hseed);
+  // an empty entry never matches: no fingerprint is 0xFFFFFFFF
+  unsigned long long e = ZG_HASH_EMPTY;
+  e = (uint32_t)(c1.y >> 32) == fp ? c1.y : e;
+  e = (uint32_t)(c1.x >> 32) == fp ? c1.x : e;
+  e = (uint32_t)(c0.y >> 32) == fp ? c0.y : e;
+  e = (uint32_t)(c0.x >> 32) == fp ? c0.x : e;
+  e = (uint32_t)(a1.y >> 32) == fp ? a1.y : e;
+  e = (uint32_t)(a1.x >> 32) == fp ? a1.x : e;
+  e = (uint32_t)(a0.y >> 32) == fp ? a0.y : e;
+  e = (uint32_t)(a0.x >> 32) == fp ? a0.x : e;
+  pr.cand = e;
+  return pr;
+}
+
+// another entry of the two buckets with the same fingerprint (probability ~ 8 / 2^32 a look-up)
+__device__ __noinline__ int64_t edge_rescan(const ZgDevGraph& g, unsigned long long key, unsigned long long cand) {
+  uint64_t b1 = 4ull * zg_bucket1(key, g.hseed, g.hbits), b2 = 4ull * zg_bucket2(key, g.hseed, g.hbits);
+  uint32_t fp = zg_fingerprint(key, g.hseed);
+  for (int i = 0; i < 8; ++i) {
+    unsigned long long x = ZG_LDG(&g.hent[(i < 4 ? b1 : b2) + (i & 3)]);
+    if (x == cand || (uint32_t)(x >> 32) != fp) continue;
+    uint4 q = ZG_LDG(&g.rec[(uint32_t)x]);
+    if (zg_edge_key(q.x, q.y) == key) return (int64_t)(uint32_t)x;
+  }
+  return -1;
+}
+
+__device__ __forceinline__ int64_t edge_confirm(const ZgDevGraph& g, const EdgeProbe& pr) {
+  if (pr.cand == ZG_HASH_EMPTY) return -1;
+  uint4 r = ZG_LDG(&g.rec[(uint32_t)pr.cand]);
+  if (zg_edge_key(r.x, r.y) == pr.key) return (int64_t)(uint32_t)pr.cand;
+  return edge_rescan(g, pr.key, pr.cand);
+}
+
+__device__ __forceinline__ bool edge_after(const ZgDevGraph& g, uint32_t x, uint32_t y, uint32_t min_valid) {
+  return edge_confirm(g, edge_candidate(g, x, y)) >= (int64_t)min_valid;
+}
+
+// ---- access model (debug): algorithmic bytes of a sample in 32-byte sectors ---------------
+// sample_edge 1; a conditional step: per anchor v with d_v > 0, 1 + max(1, ceil(log2 d_v) - 2),
+// plus 1 for the chosen entry; a closure edge: 2 + max(1, ceil(log2 min(d_x, d_y)) - 2),
+// counted for every edge checked up to the first miss.
+__device__ __forceinline__ uint32_t model_search(uint64_t d) {
+  uint32_t l = d <= 1 ? 0u : (uint32_t)(64 - __clzll(d - 1));
+  return l > 3 ? l - 2 : 1u;
+}
+__device__ __forceinline__ uint64_t degree(const ZgDevGraph& g, uint32_t v) {
+  return (uint64_t)(ZG_LDG(&g.off32[v + 1]) - ZG_LDG(&g.off32[v]));
+}
+__device__ __forceinline__ uint32_t model_anchor(const ZgDevGraph& g, uint32_t v) {
+  uint64_t d = degree(g, v);
+  return d ? 1 + model_search(d) : 0;
+}
+__device__ __forceinline__ uint32_t model_close(const ZgDevGraph& g, uint32_t x, uint32_t y) {
+  uint64_t dx = degree(g, x), dy = degree(g, y);
+  return 2 + model_search(dx < dy ? dx : dy);
+}
+
+// ---- reference doubles (debug) ---------------------------------------------------------
+__device__ __forceinline__ double ddiv(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double u2d(uint64_t v) { return __ull2double_rn(v); }
+
+// x87 extended (64-bit mantissa, round-to-nearest-even), restated in integers.
+struct Ext {
+  uint64_t m;
+  int32_t e;
+};
+__device__ __forceinline__ Ext ext_from_double(double d) {
+  uint64_t b = (uint64_t)__double_as_longlong(d);
+  int ex = (int)((b >> 52) & 0x7ff);
+  Ext r;
+  r.m = ((b & ((1ull << 52) - 1)) | (1ull << 52)) << 11;
+  r.e = ex - 1075 - 11;
+  return r;
+}
+__device__ __forceinline__ Ext ext_mul(Ext a, Ext b) {
+  uint64_t lo = a.m * b.m, hi = __umul64hi(a.m, b.m);
+  uint64_t keep, rem, half = 1ull << 63;
+  Ext r;
+  if (hi >> 63) {
+    keep = hi;
+    rem = lo;
+    r.e = a.e + b.e + 64;
+  } else {
+    keep = (hi << 1) | (lo >> 63);
+    rem = lo << 1;
+    r.e = a.e + b.e + 63;
+  }
+  if (rem > half || (rem == half && (keep & 1))) {
+    keep++;
+    if (keep == 0) {
+      keep = 1ull << 63;
+      r.e++;
+    }
+  }
+  r.m = keep;
+  return r;
+}
+// 2^127 / m for m in (2^63, 2^64): restoring division, 64 quotient bits.
+__device__ __forceinline__ Ext ext_inv(Ext a) {
+  Ext r;
+  if (a.m == (1ull << 63)) {
+    r.m = 1ull << 63;
+    r.e = -126 - a.e;
+    return r;
+  }
+  // remainder arithmetic on 65-bit values: rem < m < 2^64
+  uint64_t q = 0, rem = 1ull << 63;  // 2^127 = 2^63 * 2^64: start with rem = 2^63, shift in 64 zero bits
+  for (int i = 0; i < 64; ++i) {
+    bool top = rem >> 63;
+    rem <<= 1;
+    q <<= 1;
+    if (top || rem >= a.m) {
+      rem -= a.m;
+      q |= 1;
+    }
+  }
+  r.e = -127 - a.e;
+  // round: compare 2*rem with m
+  bool top = rem >> 63;
+  uint64_t rem2 = rem << 1;
+  bool gt = top || rem2 > a.m;
+  bool eq = !top && rem2 == a.m;
+  if (gt || (eq && (q & 1))) {
+    q++;
+    if (q == 0) {
+      q = 1ull << 63;
+      r.e++;
+    }
+  }
+  r.m = q;
+  return r;
+}
+__device__ __forceinline__ double ext_to_double(Ext a) {
+  uint64_t keep = a.m >> 11, rem = a.m & 0x7ff;
+  int e = a.e + 11;
+  if (rem > 0x400 || (rem == 0x400 && (keep & 1))) {
+    keep++;
+    if (keep == (1ull << 53)) {
+      keep >>= 1;
+      e++;
+    }
+  }
+  return scalbn(u2d(keep), e);
+}
+
+// ---- Triangle: applications/Triangle.cpp:48-73 -----------------------------------------
+template <bool DBG>
+__device__ void prog_triangle(const ZgDevGraph& g, Ctx& c, Res& r) {
+  if (g.m == 0) {
+    r.fail = true;
+    return;
+  }
+  uint64_t e0 = c.draw(0, g.m - 1);
+  uint4 q = ZG_LDG(&g.rec[e0]);
+  uint64_t S = (uint64_t)q.z + q.w;
+  if (DBG) c.sectors += 1 + model_anchor(g, q.x) + model_anchor(g, q.y);
+  if (S == 0) {
+    r.fail = true;
+    return;
+  }
+  if (DBG) c.sectors += 1;
+  uint64_t r1 = c.draw(0, S - 1);
+  uint32_t anchor = q.x, other = q.y, suf = q.z;
+  if (r1 >= q.z) {
+    r1 -= q.z;
+    anchor = q.y;
+    other = q.x;
+    suf = q.w;
+  }
+  uint32_t idx = ZG_LDG(&g.off32[anchor + 1]) - (uint32_t)suf + (uint32_t)r1;
+  uint2 e1 = ZG_LDG(&g.adj_e[idx]);
+  uint32_t a1 = 1 + (e1.x == q.x || e1.x == q.y);
+  res_mul(r, g.m);
+  res_mul(r, S);
+  if (a1 == 2) r.shift = 1;
+  bool closed = (a1 == 1) && edge_after(g, other, e1.x, e1.y + 1);
+  if (DBG) c.sectors += model_close(g, other, e1.x);
+  r.hit = closed;
+  if (DBG && closed) {
+    double p = 1.0;
+    p = dmul(p, ddiv(1.0, u2d(g.m)));
+    p = dmul(p, ddiv(1.0 * a1, u2d(S)));
+    r.w = ddiv(1.0, p);
+  }
+}
+
+// ---- ThreeChain: applications/ThreeChain.cpp:315-330 -------------------------------------
+template <bool DBG>
+__device__ void prog_three_chain(const ZgDevGraph& g, Ctx& c, Res& r) {
+  if (g.m == 0) {
+    r.fail = true;
+    return;
+  }
+  uint64_t e0 = c.draw(0, g.m - 1);
+  uint4 q = ZG_LDG(&g.rec[e0]);
+  uint64_t S = (uint64_t)q.z + q.w;
+  if (DBG) c.sectors += 1 + model_anchor(g, q.x) + model_anchor(g, q.y);
+  if (S == 0) {
+    r.fail = true;
+    return;
+  }
+  if (DBG) c.sectors += 1;
+  uint64_t r1 = c.draw(0, S - 1);
+  // The chosen edge only sets the appearance count a, which is 1 on a simple graph
+  // (zg_graph_create rejects duplicate edges); the debug variant reads it and checks.
+  uint32_t a1 = 1;
+  if (DBG) {
+    uint32_t anchor = q.x, suf = q.z;
+    if (r1 >= q.z) {
+      r1 -= q.z;
+      anchor = q.y;
+      suf = q.w;
+    }
+    uint2 e1 = ZG_LDG(&g.adj_e[ZG_LDG(&g.off32[anchor + 1]) - (uint32_t)suf + (uint32_t)r1]);
+    a1 = 1 + (e1.x == q.x || e1.x == q.y);
+  }
+  res_mul(r, g.m);
+  res_mul(r, S);
+  if (a1 == 2) r.shift = 1;
+  r.hit = true;
+  if (DBG) {
+    double p = 1.0;
+    p = dmul(p, ddiv(1.0, u2d(g.m)));
+    p = dmul(p, ddiv(1.0 * a1, u2d(S)));
+    r.w = ddiv(1.0, p);
+  }
+}
+
+// ---- FourClique: applications/FourClique.cpp:176-234 -------------------------------------
+// Vertices in insertion order a (e0.src), b (e0.dst), c (e1's new end), d (e2's new end); all
+// state in scalars (no dynamically indexed arrays, which would live in local memory).
+template <bool DBG>
+__device__ void prog_four_clique(const ZgDevGraph& g, Ctx& c, Res& r) {
+  if (g.m == 0) {
+    r.fail = true;
+    return;
+  }
+  uint64_t e0 = c.draw(0, g.m - 1);
+  uint4 q = ZG_LDG(&g.rec[e0]);
+  uint64_t S1 = (uint64_t)q.z + q.w;
+  if (DBG) c.sectors += 1 + model_anchor(g, q.x) + model_anchor(g, q.y);
+  if (S1 == 0) {
+    r.fail = true;
+    return;
+  }
+  if (DBG) c.sectors += 1;
+  uint64_t r1 = c.draw(0, S1 - 1);
+  const uint32_t va = q.x, vb = q.y;
+  uint32_t endA = ZG_LDG(&g.off32[va + 1]), endB = ZG_LDG(&g.off32[vb + 1]);
+  const bool s1b = r1 >= q.z;  // the first conditional edge hangs off b
+  uint32_t idx1 = (s1b ? endB - q.w + (uint32_t)(r1 - q.z) : endA - q.z + (uint32_t)r1);
+  uint2 e1 = ZG_LDG(&g.adj_e[idx1]);
+  const uint32_t vc = e1.x;
+  uint32_t a1 = 1 + (vc == va || vc == vb);
+  res_mul(r, g.m);
+  res_mul(r, S1);
+  if (a1 == 2) r.shift++;
+  // second conditional step: anchors [a, b, c], min_valid = id1 + 1
+  uint32_t mv = e1.y + 1;
+  uint4 q1 = ZG_LDG(&g.rec[e1.y]);
+  uint32_t endC = ZG_LDG(&g.off32[vc + 1]);
+  uint32_t lbC = endC - ((q1.x == vc) ? q1.z : q1.w);
+  // the anchor's own list continues right after e1; the other endpoint's list needs a search
+  // (that suffix holds edge ids in [id0 + 1, m - 1])
+  uint32_t lo = lb_eid(g.adj_e, s1b ? endA - q.z : endB - q.w, s1b ? endA : endB, mv, (uint32_t)e0 + 1,
+                       (uint32_t)(g.m - 1));
+  uint32_t lbA = s1b ? lo : idx1 + 1, lbB = s1b ? idx1 + 1 : lo;
+  uint64_t lenA = endA - lbA, lenB = endB - lbB;
+  // when c coincides with a or b (duplicate edges) the reference lists only two vertices
+  uint64_t lenC = a1 == 1 ? (uint64_t)(endC - lbC) : 0;
+  uint64_t S2 = lenA + lenB + lenC;
+  if (DBG) c.sectors += model_anchor(g, va) + model_anchor(g, vb) + (a1 == 1 ? model_anchor(g, vc) : 0);
+  if (S2 == 0) {
+    r.fail = true;
+    return;
+  }
+  if (DBG) c.sectors += 1;
+  uint64_t r2 = c.draw(0, S2 - 1);
+  int s2;
+  uint32_t pos2;
+  if (r2 < lenA) {
+    s2 = 0;
+    pos2 = lbA + (uint32_t)r2;
+  } else if (r2 - lenA < lenB) {
+    s2 = 1;
+    pos2 = lbB + (uint32_t)(r2 - lenA);
+  } else {
+    s2 = 2;
+    pos2 = lbC + (uint32_t)(r2 - lenA - lenB);
+  }
+  uint2 e2 = ZG_LDG(&g.adj_e[pos2]);
+  const uint32_t vd = e2.x;
+  bool dup = vd == va || vd == vb || (a1 == 1 && vd == vc);
+  uint32_t a2 = 1 + (dup ? 1 : 0);
+  res_mul(r, S2);
+  if (a2 == 2) r.shift++;
+  if (a1 != 1 || dup) return;  // three vertices: a triangle was sampled (FourClique.cpp:224-226)
+  // closure: the 3 vertex pairs not sampled, all with edge id >= id2 + 1.  Sampled pairs are
+  // (a,b), (anchor of e1, c) and (anchor of e2, d).  The reference checks the pairs in slot order
+  // up to the first miss (the debug access model follows that); production issues all three
+  // look-ups at once.
+  const int s1 = s1b ? 1 : 0;
+  uint32_t mv2 = e2.y + 1;
+  auto vslot = [&](int i) { return i == 0 ? va : i == 1 ? vb : i == 2 ? vc : vd; };
+  bool ok = true;
+  if (DBG) {
+    for (int i = 0; i < 4; ++i)
+      for (int j = i + 1; j < 4; ++j) {
+        bool sampled = (i == 0 && j == 1) || (i == s1 && j == 2) || (i == s2 && j == 3);
+        if (!sampled && ok) {
+          ok = edge_after(g, vslot(i), vslot(j), mv2);
+          c.sectors += model_close(g, vslot(i), vslot(j));
+        }
+      }
+  } else {
+    uint32_t x0 = s1b ? va : vb;             // the pair (not-anchor-of-e1, c)
+    uint32_t x1 = vslot(s2 == 0 ? 1 : 0);    // the two pairs (?, d) other than e2's own
+    uint32_t x2 = vslot(s2 == 2 ? 1 : 2);
+    EdgeProbe p0 = edge_candidate(g, x0, vc), p1 = edge_candidate(g, x1, vd), p2 = edge_candidate(g, x2, vd);
+    ok = p0.cand != ZG_HASH_EMPTY && p1.cand != ZG_HASH_EMPTY && p2.cand != ZG_HASH_EMPTY;
+    if (ok)
+      ok = edge_confirm(g, p0) >= (int64_t)mv2 && edge_confirm(g, p1) >= (int64_t)mv2 &&
+           edge_confirm(g, p2) >= (int64_t)mv2;
+  }
+  r.hit = ok;
+  if (DBG && ok) {
+    double p = 1.0;
+    p = dmul(p, ddiv(1.0, u2d(g.m)));
+    p = dmul(p, ddiv(1.0 * a1, u2d(S1)));
+    p = dmul(p, ddiv(1.0 * a2, u2d(S2)));
+    r.w = ddiv(1.0, p);
+  }
+}
+
+// ---- FourChain: applications/FourChain.cpp:24-124 ----------------------------------------
+template <bool DBG>
+__device__ void prog_four_chain(const ZgDevGraph& g, Ctx& c, Res& r) {
+  uint64_t sel = c.draw(1, 3);
+  res_mul(r, 3);
+  if (g.m == 0) {
+    r.fail = true;
+    return;
+  }
+  uint64_t e0 = c.draw(0, g.m - 1);
+  res_mul(r, g.m);
+  uint4 q = ZG_LDG(&g.rec[e0]);
+  uint32_t a = q.x, b = q.y;
+  uint64_t S1, S2;
+  uint32_t a1 = 1, a2 = 1;
+  bool ok;
+  if (DBG) c.sectors += 1;
+  if (sel != 3) {
+    // edges [e0], vertices [a, b]
+    S1 = (uint64_t)q.z + q.w;
+    if (DBG) c.sectors += model_anchor(g, a) + model_anchor(g, b);
+    if (S1 == 0) {
+      r.fail = true;
+      return;
+    }
+    if (DBG) c.sectors += 1;
+    uint64_t r1 = c.draw(0, S1 - 1);
+    uint32_t anchor = a, suf = q.z;
+    if (r1 >= q.z) {
+      r1 -= q.z;
+      anchor = b;
+      suf = q.w;
+    }
+    uint32_t idx1 = ZG_LDG(&g.off32[anchor + 1]) - (uint32_t)suf + (uint32_t)r1;
+    uint2 e1 = ZG_LDG(&g.adj_e[idx1]);
+    a1 = 1 + (e1.x == a || e1.x == b);
+    res_mul(r, S1);
+    if (a1 == 2) r.shift++;
+    // the vertex of e1 not shared with e0 (FourChain.cpp:44-54)
+    uint32_t nw;
+    if (a == anchor) nw = e1.x;
+    else if (a == e1.x) nw = anchor;
+    else if (b == anchor) nw = e1.x;
+    else nw = anchor;
+    uint4 q1 = ZG_LDG(&g.rec[e1.y]);
+    uint32_t sufn = (q1.x == nw) ? q1.z : q1.w;  // entries after e1 in nw's list
+    uint32_t endn = ZG_LDG(&g.off32[nw + 1]);
+    uint32_t lbn;
+    if (sel == 1) {
+      // edges [e0, e1]: min_valid = id1 + 1
+      lbn = endn - (uint32_t)sufn;
+    } else {
+      // edges [e0]: min_valid = id0 + 1, at or before e1's own slot in nw's list
+      uint32_t pos1 = endn - (uint32_t)sufn - 1;
+      lbn = lb_eid(g.adj_e, ZG_LDG(&g.off32[nw]), pos1 + 1, (uint32_t)e0 + 1, 0u, e1.y);
+    }
+    S2 = (uint64_t)(endn - lbn);
+    if (DBG) c.sectors += model_anchor(g, nw);
+    if (S2 == 0) {
+      r.fail = true;
+      return;
+    }
+    if (DBG) c.sectors += 1;
+    uint64_t r2 = c.draw(0, S2 - 1);
+    uint2 e2 = ZG_LDG(&g.adj_e[lbn + (uint32_t)r2]);
+    a2 = 1 + (e2.x == nw);
+    res_mul(r, S2);
+    if (a2 == 2) r.shift++;
+    ok = !(nw == a || nw == b) && !(e2.x == a || e2.x == b);
+    if (sel == 2) ok = ok && !(e2.y >= e1.y);
+  } else {
+    // vertices [a]: e1 from a's list; then vertices [b]: e2 from b's list; edges [e0]
+    S1 = q.z;
+    if (DBG) c.sectors += model_anchor(g, a);
+    if (S1 == 0) {
+      r.fail = true;
+      return;
+    }
+    if (DBG) c.sectors += 1;
+    uint64_t r1 = c.draw(0, S1 - 1);
+    uint2 e1 = ZG_LDG(&g.adj_e[ZG_LDG(&g.off32[a + 1]) - (uint32_t)q.z + (uint32_t)r1]);
+    a1 = 1 + (e1.x == a);
+    res_mul(r, S1);
+    if (a1 == 2) r.shift++;
+    S2 = q.w;
+    if (DBG) c.sectors += model_anchor(g, b);
+    if (S2 == 0) {
+      r.fail = true;
+      return;
+    }
+    if (DBG) c.sectors += 1;
+    uint64_t r2 = c.draw(0, S2 - 1);
+    uint2 e2 = ZG_LDG(&g.adj_e[ZG_LDG(&g.off32[b + 1]) - (uint32_t)q.w + (uint32_t)r2]);
+    a2 = 1 + (e2.x == b);
+    res_mul(r, S2);
+    if (a2 == 2) r.shift++;
+    ok = !(b == a || b == e1.x) && !(e2.x == a || e2.x == e1.x);
+  }
+  r.hit = ok;
+  if (DBG && ok) {
+    double p = 1. / 3;
+    p = dmul(p, ddiv(1.0, u2d(g.m)));
+    p = dmul(p, ddiv(1.0 * a1, u2d(S1)));
+    p = dmul(p, ddiv(1.0 * a2, u2d(S2)));
+    r.w = ddiv(1.0, p);
+  }
+}
+
+// canonicality_check (applications/ChainMining.cpp:218-235, src/SamplerGenerator.cpp:368-385)
+__device__ __forceinline__ bool canonical(const uint32_t* es, const uint32_t* ed, const uint32_t* ei, int ne,
+                                          uint32_t s, uint32_t d, uint32_t id) {
+  if (ne <= 1) return true;
+  bool found = false;
+  for (int i = 0; i < ne; ++i) {
+    if (!found) {
+      if (s == es[i] || s == ed[i] || d == es[i] || d == ed[i]) found = true;
+    } else if (ei[i] >= id) {
+      return false;
+    }
+  }
+  return true;
+}
+
+// ---- ChainMining: applications/ChainMining.cpp:240-84 ------------------------------------
+template <bool DBG>
+__device__ void prog_chain(const ZgDevGraph& g, int order, Ctx& c, Res& r) {
+  if (g.m == 0) {
+    r.fail = true;
+    return;
+  }
+  uint64_t e0 = c.draw(0, g.m - 1);
+  res_mul(r, g.m);
+  uint4 q = ZG_LDG(&g.rec[e0]);
+  uint32_t es[ZG_MAX_LIST], ed[ZG_MAX_LIST], ei[ZG_MAX_LIST];
+  uint32_t vs[ZG_MAX_LIST];
+  int ne = 1, nvtx = 2;
+  es[0] = q.x;
+  ed[0] = q.y;
+  ei[0] = (uint32_t)e0;
+  vs[0] = q.x;
+  vs[1] = q.y;
+  uint32_t f[2] = {q.x, q.y};
+  uint32_t fe[2], fl[2];
+  fe[0] = ZG_LDG(&g.off32[q.x + 1]);
+  fe[1] = ZG_LDG(&g.off32[q.y + 1]);
+  fl[0] = fe[0] - q.z;
+  fl[1] = fe[1] - q.w;
+  Ext p;
+  if (DBG) p = ext_from_double(ddiv(1.0, u2d(g.m)));
+  if (DBG) c.sectors += 1;
+  uint32_t mv = (uint32_t)e0 + 1;
+  for (int i = 0; i < order - 2; ++i) {
+    uint64_t l0 = (uint64_t)(fe[0] - fl[0]), l1 = (uint64_t)(fe[1] - fl[1]);
+    uint64_t S = l0 + l1;
+    if (DBG) c.sectors += model_anchor(g, f[0]) + model_anchor(g, f[1]);
+    if (S == 0) {
+      r.fail = true;
+      return;
+    }
+    if (DBG) c.sectors += 1;
+    uint64_t rr = c.draw(0, S - 1);
+    int side = 0;
+    if (rr >= l0) {
+      rr -= l0;
+      side = 1;
+    }
+    uint2 e = ZG_LDG(&g.adj_e[fl[side] + (uint32_t)rr]);
+    uint32_t src = f[side];
+    uint32_t av = (f[0] == src) + (f[1] == src) + (f[0] == e.x) + (f[1] == e.x);
+    res_mul(r, S);
+    if (av == 2) r.shift++;
+    if (DBG) p = ext_mul(p, ext_from_double(ddiv(1.0 * av, u2d(S))));
+    if (!canonical(es, ed, ei, ne, src, e.x, e.y)) return;
+    es[ne] = src;
+    ed[ne] = e.x;
+    ei[ne] = e.y;
+    ++ne;
+    bool seen = false;
+    for (int k = 0; k < nvtx; ++k) seen |= (vs[k] == e.x);
+    if (!seen) vs[nvtx++] = e.x;
+    if (nvtx != i + 3) return;
+    // frontier update (ChainMining.cpp:265-80); here src is a frontier vertex and e.x is new
+    int upd = (f[0] == src) ? 0 : 1;
+    f[upd] = e.x;
+    uint4 qe = ZG_LDG(&g.rec[e.y]);
+    uint32_t sufe = (qe.x == e.x) ? qe.z : qe.w;
+    fe[upd] = ZG_LDG(&g.off32[e.x + 1]);
+    uint32_t pos = fe[upd] - (uint32_t)sufe - 1;  // e's own slot in the new frontier's list
+    fl[upd] = lb_eid(g.adj_e, ZG_LDG(&g.off32[e.x]), pos + 1, mv, 0u, e.y);
+  }
+  r.hit = true;
+  if (DBG) r.w = ext_to_double(ext_inv(p));
+}
+
+// ---- SamplerGenerator<Empty>::estimate: src/SamplerGenerator.cpp:461-546 ----------------
+__device__ __forceinline__ uint32_t pair_bit(uint32_t i, uint32_t j, uint32_t pv) {
+  if (i > j) {
+    uint32_t t = i;
+    i = j;
+    j = t;
+  }
+  return i * (2 * pv - i - 1) / 2 + (j - i - 1);
+}
+
+template <bool DBG>
+__device__ void prog_pattern(const ZgDevGraph& g, const ZgProgParams& pp, Ctx& c, Res& r) {
+  if (g.m == 0) {
+    r.fail = true;
+    return;
+  }
+  uint64_t e0 = c.draw(0, g.m - 1);
+  res_mul(r, g.m);
+  uint4 q = ZG_LDG(&g.rec[e0]);
+  const int MV = ZG_MAX_PATTERN_V + 1;
+  uint32_t vs[MV];
+  uint32_t vl[MV], ve[MV];
+  uint32_t es[ZG_MAX_LIST], ed[ZG_MAX_LIST], ei[ZG_MAX_LIST];
+  int nvtx = 2, ne = 1;
+  vs[0] = q.x;
+  vs[1] = q.y;
+  ve[0] = ZG_LDG(&g.off32[q.x + 1]);
+  ve[1] = ZG_LDG(&g.off32[q.y + 1]);
+  vl[0] = ve[0] - q.z;
+  vl[1] = ve[1] - q.w;
+  es[0] = q.x;
+  ed[0] = q.y;
+  ei[0] = (uint32_t)e0;
+  uint32_t mv = (uint32_t)e0 + 1;
+  double p = 1.0;
+  if (DBG) p = dmul(p, ddiv(1.0, u2d(g.m)));
+  if (DBG) c.sectors += 1;
+  for (uint32_t k = 1; k < pp.pe; ++k) {
+    uint64_t S = 0;
+    for (int i = 0; i < nvtx; ++i) S += (uint64_t)(ve[i] - vl[i]);
+    if (DBG)
+      for (int i = 0; i < nvtx; ++i) c.sectors += model_anchor(g, vs[i]);
+    if (S == 0) {
+      r.fail = true;
+      return;
+    }
+    if (DBG) c.sectors += 1;
+    uint64_t rr = c.draw(0, S - 1);
+    int side = 0;
+    for (; side < nvtx - 1; ++side) {
+      uint64_t len = (uint64_t)(ve[side] - vl[side]);
+      if (rr < len) break;
+      rr -= len;
+    }
+    uint2 e = ZG_LDG(&g.adj_e[vl[side] + (uint32_t)rr]);
+    uint32_t src = vs[side];
+    int nbr_slot = -1;
+    for (int i = 0; i < nvtx; ++i)
+      if (vs[i] == e.x) nbr_slot = i;
+    uint32_t av = 1 + (nbr_slot >= 0);
+    res_mul(r, S);
+    if (av == 2) r.shift++;
+    if (DBG) p = dmul(p, ddiv(1.0 * av, u2d(S)));
+    if (!canonical(es, ed, ei, ne, src, e.x, e.y)) return;
+    es[ne] = src;
+    ed[ne] = e.x;
+    ei[ne] = e.y;
+    ++ne;
+    if (nbr_slot < 0) {
+      vs[nvtx] = e.x;
+      uint4 qe = ZG_LDG(&g.rec[e.y]);
+      uint32_t sufe = (qe.x == e.x) ? qe.z : qe.w;
+      ve[nvtx] = ZG_LDG(&g.off32[e.x + 1]);
+      uint32_t pos = ve[nvtx] - (uint32_t)sufe - 1;
+      vl[nvtx] = lb_eid(g.adj_e, ZG_LDG(&g.off32[e.x]), pos + 1, mv, 0u, e.y);
+      ++nvtx;
+      if ((uint32_t)nvtx > pp.pv) return;
+    }
+  }
+  if ((uint32_t)nvtx != pp.pv) return;
+  // relabel by ascending vertex id (SamplerGenerator.cpp:493-527) and test the edge set
+  uint32_t rank[MV];
+  for (int i = 0; i < nvtx; ++i) {
+    uint32_t rk = 0;
+    for (int j = 0; j < nvtx; ++j) rk += vs[j] < vs[i];
+    rank[i] = rk;
+  }
+  uint32_t mask = 0;
+  for (int k = 0; k < ne; ++k) {
+    uint32_t ri = 0, rj = 0;
+    for (int i = 0; i < nvtx; ++i) {
+      if (vs[i] == es[k]) ri = rank[i];
+      if (vs[i] == ed[k]) rj = rank[i];
+    }
+    mask |= 1u << pair_bit(ri, rj, pp.pv);
+  }
+  int lo = 0, hi = (int)pp.num_unique;
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (ZG_LDG(&pp.masks[mid]) < mask)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  bool ok = lo < (int)pp.num_unique && ZG_LDG(&pp.masks[lo]) == mask;
+  r.hit = ok;
+  if (DBG && ok) r.w = ddiv(1.0, p);
+}
+
+// ---- per-thread exact accumulation and block reduction ----------------------------------
+// Per-thread state kept small: one thread handles < 2^32 estimators, so 32-bit counters.
+struct Acc {
+  uint32_t samples, hits, fails, ovf;
+  uint64_t s[4];
+  double sw, sw2;
+};
+
+__device__ __forceinline__ void acc_init(Acc& a) {
+  a.samples = a.hits = a.fails = a.ovf = 0;
+  a.s[0] = a.s[1] = a.s[2] = a.s[3] = 0;
+  a.sw = a.sw2 = 0.0;
+}
+
+// num / 2^shift as a double truncated to 53 bits, built from integer operations only: GB300's
+// FP64 pipe is narrow, and this runs once per hit (the variance terms; the mean is exact).
+__device__ __forceinline__ double u192_scaled_to_double(const ZgU192& n, uint32_t shift) {
+  uint64_t top = n.l[0], next = 0;
+  int base = 0;
+  if (n.l[2]) {
+    top = n.l[2];
+    next = n.l[1];
+    base = 128;
+  } else if (n.l[1]) {
+    top = n.l[1];
+    next = n.l[0];
+    base = 64;
+  }
+  if (top == 0) return 0.0;
+  int lz = __clzll(top);
+  uint64_t mant = (top << lz) | (lz ? next >> (64 - lz) : 0ull);
+  int64_t e = (int64_t)base + 63 - lz - (int64_t)shift;  // value = mant * 2^(e - 63)
+  uint64_t bits = ((uint64_t)(e + 1023) << 52) | ((mant >> 11) & ((1ull << 52) - 1));
+  return __longlong_as_double((long long)bits);
+}
+
+__device__ __forceinline__ void acc_add(Acc& a, const Res& r, uint32_t den) {
+  a.samples++;
+  a.fails += r.fail;
+  if (!r.hit) return;
+  a.hits++;
+  a.ovf += r.ovf;
+  uint32_t sh = den - r.shift;  // < 64
+  uint64_t v0 = r.num.l[0] << sh;
+  uint64_t v1 = sh ? (r.num.l[1] << sh) | (r.num.l[0] >> (64 - sh)) : r.num.l[1];
+  uint64_t v2 = sh ? (r.num.l[2] << sh) | (r.num.l[1] >> (64 - sh)) : r.num.l[2];
+  uint64_t v3 = sh ? (r.num.l[2] >> (64 - sh)) : 0;
+  asm("add.cc.u64 %0, %0, %4;\n\t"
+      "addc.cc.u64 %1, %1, %5;\n\t"
+      "addc.cc.u64 %2, %2, %6;\n\t"
+      "addc.u64 %3, %3, %7;"
+      : "+l"(a.s[0]), "+l"(a.s[1]), "+l"(a.s[2]), "+l"(a.s[3])
+      : "l"(v0), "l"(v1), "l"(v2), "l"(v3));
+  // sum_w is taken from the exact integer sum at the end; only the square needs the FP64 pipe
+  double w = u192_scaled_to_double(r.num, r.shift);
+  a.sw2 = fma(w, w, a.sw2);
+}
+
+template <int BLOCK>
+__device__ void block_reduce_store(Acc& a, ZgPartial* out) {
+  unsigned long long v[14];
+  v[0] = a.samples;
+  v[1] = a.hits;
+  v[2] = a.fails;
+  v[3] = a.ovf;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    v[4 + 2 * i] = (uint32_t)a.s[i];
+    v[5 + 2 * i] = a.s[i] >> 32;
+  }
+  double d0 = a.sw, d1 = a.sw2;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+    for (int i = 0; i < 12; ++i) v[i] += __shfl_xor_sync(0xffffffffu, v[i], o);
+    d0 += __shfl_xor_sync(0xffffffffu, d0, o);
+    d1 += __shfl_xor_sync(0xffffffffu, d1, o);
+  }
+  __shared__ unsigned long long sv[BLOCK / 32][12];
+  __shared__ double sd[BLOCK / 32][2];
+  int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) {
+#pragma unroll
+    for (int i = 0; i < 12; ++i) sv[warp][i] = v[i];
+    sd[warp][0] = d0;
+    sd[warp][1] = d1;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    ZgPartial p;
+    unsigned long long t[12] = {0};
+    double s0 = 0, s1 = 0;
+    for (int w = 0; w < BLOCK / 32; ++w) {
+      for (int i = 0; i < 12; ++i) t[i] += sv[w][i];
+      s0 += sd[w][0];
+      s1 += sd[w][1];
+    }
+    p.samples = t[0];
+    p.hits = t[1];
+    p.fails = t[2];
+    p.overflow = t[3];
+    for (int i = 0; i < 8; ++i) p.lane[i] = t[4 + i];
+    p.sum_w = s0;
+    p.sum_w2 = s1;
+    *out = p;
+  }
+}
+
+
+}  // namespace

@@ -23,12 +23,16 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_build", "libzgraph_gpu.so")
 
 ZG_OK = 0
+(ZG_ERR_INVALID_ARG, ZG_ERR_OOM, ZG_ERR_CUDA, ZG_ERR_INVALID_GRAPH, ZG_ERR_UNSUPPORTED_ESTIMATOR, ZG_ERR_TIMEOUT,
+ ZG_ERR_BOUND_NOT_MET, ZG_ERR_NO_DEVICE, ZG_ERR_OVERFLOW, ZG_ERR_TOO_LARGE) = range(1, 11)
 ERRORS = {1: "INVALID_ARG", 2: "OOM", 3: "CUDA", 4: "INVALID_GRAPH", 5: "UNSUPPORTED_ESTIMATOR",
           6: "TIMEOUT", 7: "BOUND_NOT_MET", 8: "NO_DEVICE", 9: "OVERFLOW", 10: "TOO_LARGE"}
 
 PROG_TRIANGLE, PROG_FOUR_CLIQUE, PROG_THREE_CHAIN, PROG_FOUR_CHAIN, PROG_CHAIN, PROG_PATTERN = 1, 2, 3, 4, 5, 6
 EXACT_TRIANGLE, EXACT_WEDGE, EXACT_THREE_PATH, EXACT_FIVE_STAR, EXACT_FOUR_CLIQUE = 1, 2, 3, 4, 5
 PRED_GE, PRED_LT, PRED_GT, PRED_LE, PRED_EQ, PRED_NE, PRED_RANGE = 1, 2, 3, 4, 5, 6, 7
+QUERY_THREE_MOTIF = 16
+BATCH_MAX_QUERIES, BATCH_MAX_CHUNKS = 65536, 65536
 NO_SHUFFLE = 0xFFFFFFFFFFFFFFFF
 MAX_DRAWS = 16
 
@@ -63,6 +67,11 @@ class Counters(C.Structure):
                 "den_log2": self.den_log2, "overflow": self.overflow,
                 "sum_num": [int(x) for x in self.sum_num], "sum_w": self.sum_w,
                 "sum_w2": self.sum_w2, "estimate": self.estimate}
+
+
+class BatchQuery(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("param", C.c_uint32), ("pred_op", C.c_int32), ("stream_id", C.c_uint32),
+                ("t0", C.c_int64), ("t1", C.c_int64), ("n", C.c_uint64), ("seed", C.c_uint64)]
 
 
 class ElpResult(C.Structure):
@@ -142,6 +151,12 @@ def lib():
             "zg_gen_rmat": ([U32, U32, D, D, D, U64, U64, P, C.POINTER(U64)], I32),
             "zg_gen_chung_lu": ([U32, D, D, U64, U64, P, C.POINTER(U64)], I32),
             "zg_gen_weights": ([U64, U32, U64, P], I32),
+            "zg_batch_create": ([P, U32, U64, U64, C.POINTER(P)], I32),
+            "zg_batch_free": ([P], I32),
+            "zg_batch_submit": ([P, P, U32, P], I32),
+            "zg_batch_wait": ([P, P], I32),
+            "zg_batch_filtered_graph": ([P, I32, I64, I64, P, C.POINTER(P)], I32),
+            "zg_batch_tune": ([P, P, U32, P, C.POINTER(I32), P], I32),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -300,7 +315,80 @@ class Graph:
 
     def free(self):
         if self._h:
-            lib().zg_graph_free(self._h)
+            if not getattr(self, "_borrowed", False):  # a batch's cached graph belongs to the batch
+                lib().zg_graph_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+# ---- batched mixed queries ----------------------------------------------------------------
+class Batch:
+    """zg_batch_*: many queries (program, optional predicate filter, budget, Philox stream) in one
+    persistent launch replayed through a CUDA graph; filtered graphs are cached on the device."""
+
+    def __init__(self, graph, max_queries=1024, cache_bytes=16 << 30, filter_seed=1):
+        init()
+        self.graph = graph  # the base graph must outlive the batch
+        h = C.c_void_p()
+        check(lib().zg_batch_create(graph.handle, max_queries, cache_bytes, filter_seed, C.byref(h)))
+        self._h = h
+        self.max_queries = max_queries
+        self._nq = 0
+
+    @staticmethod
+    def queries(qs):
+        """qs: iterable of dicts with kind, n, seed and optional param, pred_op, t0, t1, stream_id."""
+        qs = list(qs)
+        arr = (BatchQuery * max(1, len(qs)))()
+        for i, q in enumerate(qs):
+            arr[i].kind = q["kind"]
+            arr[i].param = q.get("param", 0)
+            arr[i].pred_op = q.get("pred_op", 0)
+            arr[i].stream_id = q.get("stream_id", 0)
+            arr[i].t0 = q.get("t0", 0)
+            arr[i].t1 = q.get("t1", 0)
+            arr[i].n = q["n"]
+            arr[i].seed = q["seed"]
+        return arr, len(qs)
+
+    def submit(self, qs, cuda_stream=None):
+        arr, nq = self.queries(qs)
+        check(lib().zg_batch_submit(self._h, arr, nq, cuda_stream))
+        self._nq = nq
+
+    def wait(self):
+        """Counters per query: [(c, None) or (chain, triangle) for 3-motif queries]."""
+        out = (Counters * max(2, 2 * self._nq))()
+        check(lib().zg_batch_wait(self._h, out))
+        return [(out[2 * i], out[2 * i + 1]) for i in range(self._nq)]
+
+    def run(self, qs, cuda_stream=None):
+        self.submit(qs, cuda_stream)
+        return self.wait()
+
+    def filtered_graph(self, op, t0, t1=0):
+        """The cached filtered graph a predicate query samples (owned by the batch)."""
+        h = C.c_void_p()
+        check(lib().zg_batch_filtered_graph(self._h, op, t0, t1, None, C.byref(h)))
+        g = Graph(h, self.graph.num_vertices)
+        g._borrowed = True
+        return g
+
+    def tune(self, qs, cuda_stream=None):
+        arr, nq = self.queries(qs)
+        best = C.c_int(0)
+        ms = (C.c_float * 3)()
+        check(lib().zg_batch_tune(self._h, arr, nq, cuda_stream, C.byref(best), ms))
+        return best.value, [float(x) for x in ms]
+
+    def free(self):
+        if getattr(self, "_h", None):
+            lib().zg_batch_free(self._h)
             self._h = None
 
     def __del__(self):

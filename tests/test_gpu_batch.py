@@ -1,0 +1,133 @@
+"""Batched mixed queries (zg_batch_*): every query of a mixed batch equals its single run on the
+same draws — zg_run on the base graph or on the batch's cached filtered graph, zg_run_three_motif
+for 3-motif queries — exactly (samples, hits, fails, 320-bit sums, estimate); batches are
+deterministic, survive cache eviction, replay through their CUDA graph with changing sizes, and
+refuse what they cannot run."""
+import numpy as np
+import pytest
+
+import zgraph as Z
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def wgraph():
+    Z.init(0)
+    e = Z.gen_rmat(12, 12, seed=31)
+    w = Z.gen_weights(len(e), 100, seed=5)
+    return Z.Graph.from_edges(e, 1 << 12, weights=w, shuffle_seed=77)
+
+
+def _same(a, b, what):
+    assert (a.samples, a.hits, a.fails) == (b.samples, b.hits, b.fails), what
+    assert [int(x) for x in a.sum_num] == [int(x) for x in b.sum_num], what
+    assert a.den_log2 == b.den_log2 and a.estimate == b.estimate, what
+    assert a.sum_w == b.sum_w, what
+    assert abs(a.sum_w2 - b.sum_w2) <= 1e-12 * max(1.0, abs(b.sum_w2)), what
+
+
+def _mixed(rng, nq):
+    kinds = [(Z.PROG_TRIANGLE, 0), (Z.PROG_FOUR_CLIQUE, 0), (Z.PROG_THREE_CHAIN, 0), (Z.PROG_FOUR_CHAIN, 0),
+             (Z.PROG_CHAIN, 5), (Z.QUERY_THREE_MOTIF, 0)]
+    qs = []
+    for i in range(nq):
+        k, prm = kinds[int(rng.integers(len(kinds)))]
+        q = {"kind": k, "param": prm, "n": int(2 ** rng.uniform(0, 17)) + 1, "seed": int(rng.integers(1, 1 << 40)),
+             "stream_id": int(rng.integers(0, 1 << 20))}
+        if k in (Z.PROG_TRIANGLE, Z.QUERY_THREE_MOTIF) and rng.random() < 0.6:
+            q["pred_op"] = [Z.PRED_GE, Z.PRED_LT][int(rng.integers(2))] if k == Z.PROG_TRIANGLE else 0
+            q["t0"] = int(rng.integers(10, 91))
+        qs.append(q)
+    return qs
+
+
+def _check_against_single(b, g, qs, res):
+    for q, (c, c2) in zip(qs, res):
+        gg = b.filtered_graph(q["pred_op"], q["t0"]) if q.get("pred_op") else g
+        if q["kind"] == Z.QUERY_THREE_MOTIF:
+            ch, tr = Z.run_three_motif(gg, q["n"], q["n"], q["seed"], q["stream_id"], q["stream_id"] + 1)
+            _same(c, ch, q)
+            _same(c2, tr, q)
+        else:
+            p = Z.Program(q["kind"], q.get("param", 0))
+            _same(c, p.run(gg, q["n"], q["seed"], stream_id=q["stream_id"]), q)
+
+
+def test_mixed_batch_equals_single_runs(wgraph):
+    rng = np.random.default_rng(7)
+    qs = _mixed(rng, 60)
+    b = Z.Batch(wgraph, max_queries=128)
+    res = b.run(qs)
+    _check_against_single(b, wgraph, qs, res)
+
+
+def test_batch_is_deterministic_and_shape_independent(wgraph):
+    rng = np.random.default_rng(8)
+    qs = _mixed(rng, 40)
+    b = Z.Batch(wgraph, max_queries=64)
+    r1 = b.run(qs)
+    r2 = b.run(qs)
+    for (a, a2), (c, c2) in zip(r1, r2):
+        assert a.as_dict() == c.as_dict() and a2.as_dict() == c2.as_dict()
+    best, ms = b.tune(qs)
+    assert 0 <= best < 3 and all(m > 0 for m in ms)
+    r3 = b.run(qs)
+    for q, (a, a2), (c, c2) in zip(qs, r1, r3):
+        _same(a, c, q)
+        _same(a2, c2, q)
+
+
+def test_filtered_graph_matches_zg_graph_filter_semantics(wgraph):
+    b = Z.Batch(wgraph, max_queries=8)
+    fg = b.filtered_graph(Z.PRED_GE, 50)
+    d = wgraph.download()
+    assert fg.num_local_edges == int((d["weights"] >= 50).sum())
+    fd = fg.download()
+    assert (fd["weights"] >= 50).all()
+    # same edge multiset as the base graph's kept edges
+    keep = d["edges"][d["weights"] >= 50]
+    a = np.sort(np.sort(keep, axis=1).view(np.uint64).ravel())
+    c = np.sort(np.sort(fd["edges"], axis=1).view(np.uint64).ravel())
+    assert np.array_equal(a, c)
+    # exact triangle count of the filtered graph: all-predicate triangles w >= 50
+    ex = fg.exact_count(Z.EXACT_TRIANGLE)
+    est = b.run([{"kind": Z.PROG_TRIANGLE, "pred_op": Z.PRED_GE, "t0": 50, "n": 1 << 24, "seed": 3}])[0][0]
+    assert abs(est.estimate / ex - 1) < 0.05
+
+
+def test_cache_eviction_keeps_results_exact(wgraph):
+    b = Z.Batch(wgraph, max_queries=32, cache_bytes=1)  # every new predicate evicts the others
+    qs = [{"kind": Z.PROG_TRIANGLE, "pred_op": Z.PRED_GE, "t0": t, "n": 5000, "seed": 11 + t} for t in (20, 40, 60, 80)]
+    res = b.run(qs)
+    for q, (c, _) in zip(qs, res):
+        fg = b.filtered_graph(q["pred_op"], q["t0"])
+        _same(c, Z.Program(Z.PROG_TRIANGLE).run(fg, q["n"], q["seed"]), q)
+
+
+def test_graph_replay_with_changing_sizes(wgraph):
+    b = Z.Batch(wgraph, max_queries=16)
+    rng = np.random.default_rng(9)
+    for nq in (1, 16, 3, 9):
+        qs = [{"kind": Z.PROG_THREE_CHAIN, "n": int(rng.integers(1, 300000)), "seed": int(rng.integers(1, 99999)),
+               "stream_id": 5} for _ in range(nq)]
+        res = b.run(qs)
+        assert len(res) == nq
+        for q, (c, _) in zip(qs, res):
+            _same(c, Z.Program(Z.PROG_THREE_CHAIN).run(wgraph, q["n"], q["seed"], stream_id=5), q)
+
+
+def test_refusals(wgraph):
+    b = Z.Batch(wgraph, max_queries=4)
+    with pytest.raises(Z.ZgError) as e:
+        b.run([{"kind": Z.PROG_TRIANGLE, "n": 0, "seed": 1}])
+    assert e.value.code == Z.ZG_ERR_INVALID_ARG
+    with pytest.raises(Z.ZgError) as e:
+        b.run([{"kind": Z.PROG_PATTERN, "n": 10, "seed": 1}])
+    assert e.value.code == Z.ZG_ERR_UNSUPPORTED_ESTIMATOR
+    with pytest.raises(Z.ZgError) as e:
+        b.run([{"kind": Z.PROG_TRIANGLE, "n": 10, "seed": 1}] * 5)
+    assert e.value.code == Z.ZG_ERR_TOO_LARGE
+    # the batch still works after refusals
+    c = b.run([{"kind": Z.PROG_TRIANGLE, "n": 1000, "seed": 2}])[0][0]
+    _same(c, Z.Program(Z.PROG_TRIANGLE).run(wgraph, 1000, 2), "after refusal")
