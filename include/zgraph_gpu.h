@@ -234,8 +234,9 @@ int zg_run_three_motif_debug(const zg_graph* g, uint64_t n_chain, uint64_t n_tri
 /* ---- batched mixed queries ----------------------------------------------------- */
 /* Many estimator queries of uneven program, predicate and budget in one persistent launch (no
  * counterpart in the reference, whose applications run one calculate() at a time).  A query runs
- * n estimators of `kind` (ZG_PROG_TRIANGLE .. ZG_PROG_CHAIN, param = chain order) with sample
- * indices [0, n) on Philox stream (seed, stream_id), on the batch's base graph or, when pred_op
+ * n estimators of `kind` (ZG_PROG_TRIANGLE .. ZG_PROG_CHAIN with param = chain order, or
+ * ZG_PROG_PATTERN with a program from zg_program_create_pattern) with sample indices
+ * [first_sample, first_sample + n) on Philox stream (seed, stream_id), on the batch's base graph or, when pred_op
  * != 0, on the base graph filtered by (pred_op, t0, t1) as AllPredicateZGraphInstance does
  * (src/ZGraphInstance.cpp:492-525).  ZG_QUERY_THREE_MOTIF runs ThreeMotif's pair: n 3-chain
  * estimators and the triangle estimators that close their wedges (zg_run_three_motif with
@@ -252,6 +253,8 @@ typedef struct zg_batch_query {
   int64_t  t0, t1;
   uint64_t n;
   uint64_t seed;
+  uint64_t first_sample;   /* sample indices [first_sample, first_sample + n) */
+  const zg_program* program; /* ZG_PROG_PATTERN: the pattern program (must outlive zg_batch_wait) */
 } zg_batch_query;
 typedef struct zg_batch zg_batch;
 /* A batch engine over base (which must outlive it): capacity max_queries per submit; filtered
@@ -388,6 +391,18 @@ int zg_gen_chung_lu(uint32_t num_vertices, double exponent, double avg_degree, u
                     uint64_t capacity, uint32_t* edges, uint64_t* m_out);
 /* Edge data uniform in [0, max_value) (datasets/toolkits/get_weighted_datasets.cpp:28-43). */
 int zg_gen_weights(uint64_t m, uint32_t max_value, uint64_t seed, uint32_t* weights);
+/* The same generators on the device, built straight into a device graph: the graph equals
+ * zg_graph_create() of zg_gen_rmat / zg_gen_chung_lu's output (edge for edge, in that order), with
+ * zg_gen_weights(m, max_weight, weight_seed) as edge data when max_weight > 0.  flags:
+ * ZG_GRAPH_SAMPLING_ONLY leaves out the neighbour-ordered adjacency (zg_graph_download's adj_n),
+ * which only exports use: a third less memory for the largest graphs. */
+#define ZG_GRAPH_SAMPLING_ONLY 1u
+int zg_graph_gen_rmat(uint32_t scale, uint32_t edge_factor, double a, double b, double c, uint64_t seed,
+                      uint32_t max_weight, uint64_t weight_seed, uint32_t flags, void* cuda_stream,
+                      zg_graph** out);
+int zg_graph_gen_chung_lu(uint32_t num_vertices, double exponent, double avg_degree, uint64_t seed,
+                          uint32_t max_weight, uint64_t weight_seed, uint32_t flags, void* cuda_stream,
+                          zg_graph** out);
 
 #ifdef __cplusplus
 }

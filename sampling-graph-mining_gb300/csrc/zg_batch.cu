@@ -22,6 +22,9 @@
 
 #include "zg_programs.cuh"
 
+int zg_graph_filter_sampling(const zg_graph* g, int pred_op, int64_t t0, int64_t t1, uint64_t shuffle_seed,
+                             cudaStream_t s, uint64_t* out_m, zg_graph** out);
+
 namespace {
 
 constexpr int kBB = 256;  // threads per block
@@ -29,7 +32,7 @@ constexpr int kBB = 256;  // threads per block
 struct BatchQuery {
   ZgDevGraph g;
   ZgProgParams pp;  // pp.kind == ZG_QUERY_THREE_MOTIF: chain + triangle on the same wedges
-  uint64_t n, seed;
+  uint64_t n, seed, first;
   uint64_t slot0;  // first partial slot of this query (two partials per chunk)
   uint32_t stream;
   uint32_t nchunks;
@@ -39,8 +42,10 @@ struct BatchWork {
   uint32_t query, chunk;
 };
 
+// Work items [0, nsimple) run in k_batch, [nsimple, nwork) (pattern programs, whose per-sample
+// state is larger) in k_batch_pattern, each kernel taking items from its own counter.
 struct BatchHeader {
-  uint32_t nwork, nq, chunk_log2, pad;
+  uint32_t nwork, nsimple, nq, chunk_log2;
 };
 
 // The 3-motif sample: a 3-chain estimator whose wedge the triangle estimator closes
@@ -76,58 +81,69 @@ __device__ __forceinline__ void motif_sample(const ZgDevGraph& g, Ctx& c, Res& r
   rt.shift = r.shift;
 }
 
-template <int MINB>
+// One work item: a chunk of one query's samples, reduced into its partial slot(s).
+template <bool PATTERN>
+__device__ __forceinline__ void batch_item(const BatchQuery& sq, uint32_t chunk, uint32_t clog,
+                                           ZgPartial* __restrict__ parts) {
+  const uint64_t lo = (uint64_t)chunk << clog;
+  const uint64_t end = lo + (1ull << clog);
+  const uint64_t hi = end < sq.n ? end : sq.n;
+  const bool motif = !PATTERN && sq.pp.kind == ZG_QUERY_THREE_MOTIF;
+  Acc a, at;
+  acc_init(a);
+  acc_init(at);
+  for (uint64_t i = lo + threadIdx.x; i < hi; i += kBB) {
+    Ctx c{sq.seed, sq.first + i, sq.stream, 0, nullptr, 0};
+    Res r;
+    res_init(r);
+    if (PATTERN) {
+      prog_pattern<false>(sq.g, sq.pp, c, r);
+      acc_add(a, r, sq.pp.den_log2);
+    } else if (motif) {
+      Res rt;
+      res_init(rt);
+      motif_sample(sq.g, c, r, rt);
+      acc_add(a, r, 1);
+      acc_add(at, rt, 1);
+    } else {
+      switch (sq.pp.kind) {
+        case ZG_PROG_TRIANGLE: prog_triangle<false>(sq.g, c, r); break;
+        case ZG_PROG_FOUR_CLIQUE: prog_four_clique<false>(sq.g, c, r); break;
+        case ZG_PROG_THREE_CHAIN: prog_three_chain<false>(sq.g, c, r); break;
+        case ZG_PROG_FOUR_CHAIN: prog_four_chain<false>(sq.g, c, r); break;
+        default: prog_chain<false>(sq.g, (int)sq.pp.param, c, r); break;  // ZG_PROG_CHAIN
+      }
+      acc_add(a, r, sq.pp.den_log2);
+    }
+  }
+  const uint64_t slot = 2 * (sq.slot0 + chunk);
+  block_reduce_store<kBB>(a, &parts[slot]);
+  __syncthreads();
+  if (motif) block_reduce_store<kBB>(at, &parts[slot + 1]);
+}
+
+template <bool PATTERN, int MINB>
 __global__ void __launch_bounds__(kBB, MINB)
     k_batch(const BatchHeader* __restrict__ hdr, const BatchQuery* __restrict__ qs, const BatchWork* __restrict__ work,
-            ZgPartial* __restrict__ parts, unsigned int* __restrict__ counter) {
+            ZgPartial* __restrict__ parts, unsigned int* __restrict__ counters) {
   __shared__ BatchQuery sq;
   __shared__ uint32_t sw;
-  const uint32_t nwork = hdr->nwork, clog = hdr->chunk_log2;
+  const uint32_t base = PATTERN ? hdr->nsimple : 0, limit = PATTERN ? hdr->nwork : hdr->nsimple;
+  const uint32_t clog = hdr->chunk_log2;
   for (;;) {
-    if (threadIdx.x == 0) sw = atomicAdd(counter, 1u);
+    if (threadIdx.x == 0) sw = base + atomicAdd(&counters[PATTERN ? 1 : 0], 1u);
     __syncthreads();
     const uint32_t w = sw;
-    if (w >= nwork) break;
+    if (w >= limit) break;
     const BatchWork wk = work[w];
     {
-      // copy the query descriptor into shared memory, one word per thread
+      // the query descriptor into shared memory, one word per thread
       const uint32_t* src = reinterpret_cast<const uint32_t*>(&qs[wk.query]);
       uint32_t* dst = reinterpret_cast<uint32_t*>(&sq);
       for (uint32_t i = threadIdx.x; i < sizeof(BatchQuery) / 4; i += kBB) dst[i] = src[i];
     }
     __syncthreads();
-    const uint64_t lo = (uint64_t)wk.chunk << clog;
-    const uint64_t end = lo + (1ull << clog);
-    const uint64_t hi = end < sq.n ? end : sq.n;
-    const bool motif = sq.pp.kind == ZG_QUERY_THREE_MOTIF;
-    Acc a, at;
-    acc_init(a);
-    acc_init(at);
-    for (uint64_t i = lo + threadIdx.x; i < hi; i += kBB) {
-      Ctx c{sq.seed, i, sq.stream, 0, nullptr, 0};
-      Res r;
-      res_init(r);
-      if (motif) {
-        Res rt;
-        res_init(rt);
-        motif_sample(sq.g, c, r, rt);
-        acc_add(a, r, 1);
-        acc_add(at, rt, 1);
-      } else {
-        switch (sq.pp.kind) {
-          case ZG_PROG_TRIANGLE: prog_triangle<false>(sq.g, c, r); break;
-          case ZG_PROG_FOUR_CLIQUE: prog_four_clique<false>(sq.g, c, r); break;
-          case ZG_PROG_THREE_CHAIN: prog_three_chain<false>(sq.g, c, r); break;
-          case ZG_PROG_FOUR_CHAIN: prog_four_chain<false>(sq.g, c, r); break;
-          default: prog_chain<false>(sq.g, (int)sq.pp.param, c, r); break;  // ZG_PROG_CHAIN
-        }
-        acc_add(a, r, sq.pp.den_log2);
-      }
-    }
-    const uint64_t slot = 2 * (sq.slot0 + wk.chunk);
-    block_reduce_store<kBB>(a, &parts[slot]);
-    __syncthreads();
-    if (motif) block_reduce_store<kBB>(at, &parts[slot + 1]);
+    batch_item<PATTERN>(sq, wk.chunk, clog, parts);
     __syncthreads();  // sq and sw are rewritten by the next item
   }
 }
@@ -194,11 +210,11 @@ __global__ void __launch_bounds__(kBB) k_batch_finalize(const BatchHeader* __res
 
 typedef void (*BatchKernel)(const BatchHeader*, const BatchQuery*, const BatchWork*, ZgPartial*, unsigned int*);
 constexpr int kBatchVariants = 3;  // 2, 3 or 4 resident blocks of 256 threads
-BatchKernel batch_kernel(int v) {
+BatchKernel batch_kernel(int v, bool pattern) {
   switch (v) {
-    case 0: return k_batch<2>;
-    case 1: return k_batch<3>;
-    default: return k_batch<4>;
+    case 0: return pattern ? k_batch<true, 2> : k_batch<false, 2>;
+    case 1: return pattern ? k_batch<true, 3> : k_batch<false, 3>;
+    default: return pattern ? k_batch<true, 4> : k_batch<false, 4>;
   }
 }
 
@@ -257,7 +273,7 @@ struct zg_batch {
   uint32_t nq = 0;
   // graph
   int variant = 2;
-  int grid = 0;
+  int grid = 0, grid_pattern = 0;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   cudaStream_t last_stream = nullptr;
@@ -279,9 +295,11 @@ int batch_enqueue(zg_batch* b, cudaStream_t s) {
   if ((e = cudaMemcpyAsync(b->d_hdr, b->h_hdr, sizeof(BatchHeader), cudaMemcpyHostToDevice, s)) ||
       (e = cudaMemcpyAsync(b->d_q, b->h_q, sizeof(BatchQuery) * b->max_queries, cudaMemcpyHostToDevice, s)) ||
       (e = cudaMemcpyAsync(b->d_work, b->h_work, sizeof(BatchWork) * b->max_work, cudaMemcpyHostToDevice, s)) ||
-      (e = cudaMemsetAsync(b->d_counter, 0, sizeof(unsigned int), s)))
+      (e = cudaMemsetAsync(b->d_counter, 0, 2 * sizeof(unsigned int), s)))
     return zg_check_cuda(e, "batch copy-in");
-  batch_kernel(b->variant)<<<b->grid, kBB, 0, s>>>(b->d_hdr, b->d_q, b->d_work, b->d_parts, b->d_counter);
+  batch_kernel(b->variant, false)<<<b->grid, kBB, 0, s>>>(b->d_hdr, b->d_q, b->d_work, b->d_parts, b->d_counter);
+  batch_kernel(b->variant, true)<<<b->grid_pattern, kBB, 0, s>>>(b->d_hdr, b->d_q, b->d_work, b->d_parts,
+                                                                 b->d_counter);
   k_batch_finalize<<<b->max_queries, kBB, 0, s>>>(b->d_hdr, b->d_q, b->d_parts, b->d_out);
   if ((e = cudaMemcpyAsync(b->h_out, b->d_out, sizeof(ZgPartial) * 2 * b->max_queries, cudaMemcpyDeviceToHost, s)))
     return zg_check_cuda(e, "batch copy-out");
@@ -319,9 +337,11 @@ int batch_build_graph(zg_batch* b) {
 int batch_set_variant(zg_batch* b, int v) {
   b->variant = v;
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel(v), kBB, 0);
-  if (per_sm < 1) per_sm = 1;
-  b->grid = per_sm * zg_num_sms();
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel(v, false), kBB, 0);
+  b->grid = (per_sm < 1 ? 1 : per_sm) * zg_num_sms();
+  per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel(v, true), kBB, 0);
+  b->grid_pattern = (per_sm < 1 ? 1 : per_sm) * zg_num_sms();
   return batch_build_graph(b);
 }
 
@@ -343,7 +363,7 @@ int batch_filtered(zg_batch* b, int op, int64_t t0, int64_t t1, cudaStream_t s,
   }
   zg_graph* g = nullptr;
   uint64_t m = 0;
-  int rc = zg_graph_filter(b->base, op, t0, t1, filter_seed_of(b->filter_seed, op, t0, t1), s, nullptr, &m, &g);
+  int rc = zg_graph_filter_sampling(b->base, op, t0, t1, filter_seed_of(b->filter_seed, op, t0, t1), s, &m, &g);
   if (rc) return rc;
   zg_graph_meta meta;
   zg_graph_get_meta(g, &meta);
@@ -383,7 +403,7 @@ extern "C" int zg_batch_create(const zg_graph* base, uint32_t max_queries, uint6
   cudaError_t e;
   if ((rc = dalloc(&b->d_hdr, 1)) || (rc = dalloc(&b->d_q, max_queries)) || (rc = dalloc(&b->d_work, b->max_work)) ||
       (rc = dalloc(&b->d_parts, 2 * (size_t)b->max_work)) || (rc = dalloc(&b->d_out, 2 * (size_t)max_queries)) ||
-      (rc = dalloc(&b->d_counter, 1))) {
+      (rc = dalloc(&b->d_counter, 2))) {
     zg_batch_free(b);
     return rc;
   }
@@ -446,29 +466,30 @@ extern "C" int zg_batch_submit(zg_batch* b, const zg_batch_query* q, uint32_t nq
     cudaError_t e = cudaStreamSynchronize(b->last_stream);  // the staging buffers are reused
     if (e) return zg_check_cuda(e, "previous batch");
   }
-  // programs and graphs
+  // validate, then programs (built-in kinds are created here; patterns come with the query)
+  for (uint32_t i = 0; i < nq; ++i) {
+    const zg_batch_query& x = q[i];
+    if (x.n == 0) return zg_set_error(ZG_ERR_INVALID_ARG, "query %u: zero estimators", i), ZG_ERR_INVALID_ARG;
+    bool builtin = x.kind >= ZG_PROG_TRIANGLE && x.kind <= ZG_PROG_CHAIN;
+    bool pattern = x.kind == ZG_PROG_PATTERN && x.program && x.program->kind == ZG_PROG_PATTERN;
+    if (!builtin && !pattern && x.kind != ZG_QUERY_THREE_MOTIF)
+      return zg_set_error(ZG_ERR_UNSUPPORTED_ESTIMATOR, "query %u: kind %d%s", i, x.kind,
+                          x.kind == ZG_PROG_PATTERN ? " needs its pattern program" : ""),
+             ZG_ERR_UNSUPPORTED_ESTIMATOR;
+  }
   std::vector<const zg_graph*> graphs(nq);
-  std::vector<zg_program*> progs(nq, nullptr);
-  uint64_t total = 0;
+  std::vector<zg_program*> own(nq, nullptr);
   int rc = ZG_OK;
   for (uint32_t i = 0; i < nq && rc == ZG_OK; ++i) {
     const zg_batch_query& x = q[i];
-    if (x.n == 0) {
-      zg_set_error(ZG_ERR_INVALID_ARG, "query %u: zero estimators", i);
-      rc = ZG_ERR_INVALID_ARG;
-    } else if (x.kind != ZG_QUERY_THREE_MOTIF && (x.kind < ZG_PROG_TRIANGLE || x.kind > ZG_PROG_CHAIN)) {
-      zg_set_error(ZG_ERR_UNSUPPORTED_ESTIMATOR, "query %u: kind %d", i, x.kind);
-      rc = ZG_ERR_UNSUPPORTED_ESTIMATOR;
+    if (x.kind >= ZG_PROG_TRIANGLE && x.kind <= ZG_PROG_CHAIN) rc = zg_program_create(x.kind, x.param, &own[i]);
+    if (rc == ZG_OK) {
+      if (x.pred_op) rc = batch_filtered(b, x.pred_op, x.t0, x.t1, s, graphs, &graphs[i]);
+      else graphs[i] = b->base;
     }
-    if (rc) break;
-    if (x.kind != ZG_QUERY_THREE_MOTIF) rc = zg_program_create(x.kind, x.param, &progs[i]);
-    if (rc) break;
-    if (x.pred_op) rc = batch_filtered(b, x.pred_op, x.t0, x.t1, s, graphs, &graphs[i]);
-    else graphs[i] = b->base;
-    total += x.n;
   }
   if (rc) {
-    for (auto* p : progs)
+    for (auto* p : own)
       if (p) zg_program_free(p);
     return rc;
   }
@@ -481,49 +502,59 @@ extern "C" int zg_batch_submit(zg_batch* b, const zg_batch_query* q, uint32_t nq
     ++clog;
   }
   b->den.assign(nq, 0);
-  uint64_t slot = 0;
-  uint32_t nwork = 0;
-  // work items: chunks of every query, interleaved round-robin so long and short queries mix
   std::vector<uint32_t> nch(nq);
+  std::vector<char> is_pattern(nq, 0);
+  uint64_t slot = 0;
   for (uint32_t i = 0; i < nq; ++i) {
     const zg_batch_query& x = q[i];
+    const zg_program* p = own[i] ? own[i] : x.program;  // null for the 3-motif
     BatchQuery& d = b->h_q[i];
     memset(&d, 0, sizeof(d));
     d.g = graphs[i]->d;
-    if (progs[i]) {
-      d.pp.kind = progs[i]->kind;
-      d.pp.param = progs[i]->param;
-      d.pp.pv = progs[i]->pv;
-      d.pp.pe = progs[i]->pe;
-      d.pp.num_unique = progs[i]->num_unique;
-      d.pp.masks = progs[i]->d_masks;
+    if (p) {
+      d.pp.kind = p->kind;
+      d.pp.param = p->param;
+      d.pp.pv = p->pv;
+      d.pp.pe = p->pe;
+      d.pp.num_unique = p->num_unique;
+      d.pp.masks = p->d_masks;
     } else {
       d.pp.kind = ZG_QUERY_THREE_MOTIF;
     }
-    d.pp.den_log2 = den_of(x.kind, x.param, progs[i]);
+    is_pattern[i] = p && p->kind == ZG_PROG_PATTERN;
+    d.pp.den_log2 = den_of(x.kind, x.param, p);
     b->den[i] = d.pp.den_log2;
     d.n = x.n;
     d.seed = x.seed;
+    d.first = x.first_sample;
     d.stream = x.stream_id;
     nch[i] = (uint32_t)((x.n + (1ull << clog) - 1) >> clog);
     d.nchunks = nch[i];
     d.slot0 = slot;
     slot += nch[i];
   }
-  for (uint32_t round = 0, left = 1; left; ++round) {
-    left = 0;
-    for (uint32_t i = 0; i < nq; ++i)
-      if (round < nch[i]) {
-        b->h_work[nwork++] = {i, round};
-        left = 1;
-      }
+  // work items, built-in programs first, then patterns; within each, round-robin over queries so
+  // long and short queries mix
+  uint32_t nwork = 0, nsimple = 0;
+  for (int pass = 0; pass < 2; ++pass) {
+    for (uint32_t round = 0, left = 1; left; ++round) {
+      left = 0;
+      for (uint32_t i = 0; i < nq; ++i)
+        if (is_pattern[i] == pass && round < nch[i]) {
+          b->h_work[nwork++] = {i, round};
+          left = 1;
+        }
+    }
+    if (pass == 0) nsimple = nwork;
   }
   b->h_hdr->nwork = nwork;
+  b->h_hdr->nsimple = nsimple;
   b->h_hdr->nq = nq;
   b->h_hdr->chunk_log2 = clog;
   b->nq = nq;
-  for (auto* p : progs)
-    if (p) zg_program_free(p);  // pattern programs (device mask tables) are not batched
+  // built-in programs carry no device tables: their descriptors are complete without them
+  for (auto* p : own)
+    if (p) zg_program_free(p);
   cudaError_t e = cudaGraphLaunch(b->exec, s);
   if (e) return zg_check_cuda(e, "batch graph launch");
   b->last_stream = s;

@@ -17,6 +17,10 @@
 
 #include "zg_internal.cuh"
 
+int zg_graph_filter_sampling(const zg_graph* g, int pred_op, int64_t t0, int64_t t1, uint64_t shuffle_seed,
+                             cudaStream_t s, uint64_t* out_m, zg_graph** out);
+int zg_graph_subsample_sampling(const zg_graph* g, double rate, uint64_t keep_seed, uint64_t shuffle_seed,
+                                cudaStream_t s, uint64_t* out_m, zg_graph** out);
 int zg_launch_groups(const zg_graph* g, const zg_program* p, uint64_t n_groups, uint32_t group, uint64_t first,
                      uint64_t seed, uint32_t stream_id, cudaStream_t s, double* out);
 double zg_exact_mean_host(const uint64_t s[5], uint32_t den, uint64_t n);
@@ -164,13 +168,14 @@ extern "C" int zg_elp_plain(const zg_graph* g, const zg_program* p, int pred_op,
   const uint32_t group = 16;
   zg_graph *sub = nullptr, *fsub = nullptr;
   uint64_t m_s = 0;
-  int rc = zg_graph_subsample(g, 0.1, seed + ZG_ELP_KEEP_OFFSET, seed + ZG_ELP_SHUFFLE_OFFSET, cuda_stream,
-                              nullptr, &m_s, &sub);
+  int rc = zg_graph_subsample_sampling(g, 0.1, seed + ZG_ELP_KEEP_OFFSET, seed + ZG_ELP_SHUFFLE_OFFSET,
+                                       (cudaStream_t)cuda_stream, &m_s, &sub);
   if (rc) return rc;
   const zg_graph* run_g = sub;
   if (pred_op) {
     uint64_t mf = 0;
-    rc = zg_graph_filter(sub, pred_op, t0, t1, seed + ZG_ELP_FILTER_OFFSET, cuda_stream, nullptr, &mf, &fsub);
+    rc = zg_graph_filter_sampling(sub, pred_op, t0, t1, seed + ZG_ELP_FILTER_OFFSET, (cudaStream_t)cuda_stream, &mf,
+                                  &fsub);
     if (rc) {
       zg_graph_free(sub);
       return rc;

@@ -106,8 +106,10 @@ __global__ void k_suffix(const uint32_t* __restrict__ vkeys, const uint2* __rest
       r->z = suf;
     else
       r->w = suf;
-    nkeys[g] = ((unsigned long long)v << 32) | a.x;
-    nvals[g] = a.y;
+    if (nkeys) {
+      nkeys[g] = ((unsigned long long)v << 32) | a.x;
+      nvals[g] = a.y;
+    }
   }
 }
 
@@ -228,8 +230,10 @@ int build_hash(zg_graph* g, cudaStream_t s) {
 }
 
 // Builds a graph from a device COO (consumed: freed by the caller afterwards).
+// sampling_only: skip the neighbour-ordered adjacency (exports only) and its duplicate check; for
+// graphs derived from an already validated graph (filters, subsamples) that only sampling reads.
 int build_graph(const uint2* d_coo, const uint32_t* d_w_in, uint64_t m, uint32_t nv,
-                cudaStream_t s, zg_graph** out) {
+                cudaStream_t s, zg_graph** out, bool sampling_only = false) {
   // edge ids and adjacency positions (< 2m) are 32-bit
   if (m > 0x7FFFFFFFull)
     return zg_set_error(ZG_ERR_TOO_LARGE, "at most 2^31-1 edges (32-bit positions): m=%llu", (unsigned long long)m),
@@ -246,7 +250,7 @@ int build_graph(const uint2* d_coo, const uint32_t* d_w_in, uint64_t m, uint32_t
   // adj_e and off32 share one allocation
   g->hot_bytes = sizeof(uint2) * n2 + sizeof(uint32_t) * ((size_t)nv + 1);
   if ((rc = dev_alloc((char**)&g->hot, g->hot_bytes)) || (rc = dev_alloc(&g->rec, m)) ||
-      (rc = dev_alloc(&g->off, (size_t)nv + 1)) || (rc = dev_alloc(&g->adj_n, n2)))
+      (rc = dev_alloc(&g->off, (size_t)nv + 1)) || (!sampling_only && (rc = dev_alloc(&g->adj_n, n2))))
     return fail(rc);
   g->adj_e = (uint2*)g->hot;
   g->off32 = (uint32_t*)((char*)g->hot + sizeof(uint2) * n2);
@@ -257,8 +261,8 @@ int build_graph(const uint2* d_coo, const uint32_t* d_w_in, uint64_t m, uint32_t
       if (e != cudaSuccess) return fail(zg_check_cuda(e, "copy weights"));
     }
   }
-  g->bytes = sizeof(uint4) * m + (sizeof(int64_t) + sizeof(uint32_t)) * ((size_t)nv + 1) + 2 * sizeof(uint2) * n2 +
-             (d_w_in ? sizeof(uint32_t) * m : 0);
+  g->bytes = sizeof(uint4) * m + (sizeof(int64_t) + sizeof(uint32_t)) * ((size_t)nv + 1) +
+             (sampling_only ? 1 : 2) * sizeof(uint2) * n2 + (d_w_in ? sizeof(uint32_t) * m : 0);
   DevBuf deg, keys, keys2, vals, vals2, flags, tmp, nk, nk2, nv1, nv2;
   if ((rc = deg.alloc(sizeof(unsigned long long) * ((size_t)nv + 1))) ||
       (rc = keys.alloc(sizeof(uint32_t) * n2)) || (rc = keys2.alloc(sizeof(uint32_t) * n2)) ||
@@ -304,23 +308,25 @@ int build_graph(const uint2* d_coo, const uint32_t* d_w_in, uint64_t m, uint32_t
     vals.reset();
     keys.reset();
     // 2. suffix counts and (v:nbr) keys
-    if ((rc = nk.alloc(sizeof(unsigned long long) * n2)) ||
-        (rc = nk2.alloc(sizeof(unsigned long long) * n2)) || (rc = nv1.alloc(sizeof(uint32_t) * n2)) ||
-        (rc = nv2.alloc(sizeof(uint32_t) * n2)))
+    if (!sampling_only &&
+        ((rc = nk.alloc(sizeof(unsigned long long) * n2)) || (rc = nk2.alloc(sizeof(unsigned long long) * n2)) ||
+         (rc = nv1.alloc(sizeof(uint32_t) * n2)) || (rc = nv2.alloc(sizeof(uint32_t) * n2))))
       return fail(rc);
     k_suffix<<<grid_for(n2, B), B, 0, s>>>(keys2.as<uint32_t>(), g->adj_e, n2, g->off, g->rec,
                                            nk.as<unsigned long long>(), nv1.as<uint32_t>());
     keys2.reset();
-    // 3. neighbour order within each vertex (stable: duplicates keep edge-id order)
-    tmp.reset();
-    tb = 0;
-    cub::DeviceRadixSort::SortPairs(nullptr, tb, nk.as<unsigned long long>(), nk2.as<unsigned long long>(),
-                                    nv1.as<uint32_t>(), nv2.as<uint32_t>(), (int64_t)n2, 0, 32 + vb, s);
-    if ((rc = tmp.alloc(tb))) return fail(rc);
-    cub::DeviceRadixSort::SortPairs(tmp.p, tb, nk.as<unsigned long long>(), nk2.as<unsigned long long>(),
-                                    nv1.as<uint32_t>(), nv2.as<uint32_t>(), (int64_t)n2, 0, 32 + vb, s);
-    k_adj_n<<<grid_for(n2, B), B, 0, s>>>(nk2.as<unsigned long long>(), nv2.as<uint32_t>(), n2, g->adj_n,
-                                          flags.as<unsigned int>() + 1);
+    if (!sampling_only) {
+      // 3. neighbour order within each vertex (stable: duplicates keep edge-id order)
+      tmp.reset();
+      tb = 0;
+      cub::DeviceRadixSort::SortPairs(nullptr, tb, nk.as<unsigned long long>(), nk2.as<unsigned long long>(),
+                                      nv1.as<uint32_t>(), nv2.as<uint32_t>(), (int64_t)n2, 0, 32 + vb, s);
+      if ((rc = tmp.alloc(tb))) return fail(rc);
+      cub::DeviceRadixSort::SortPairs(tmp.p, tb, nk.as<unsigned long long>(), nk2.as<unsigned long long>(),
+                                      nv1.as<uint32_t>(), nv2.as<uint32_t>(), (int64_t)n2, 0, 32 + vb, s);
+      k_adj_n<<<grid_for(n2, B), B, 0, s>>>(nk2.as<unsigned long long>(), nv2.as<uint32_t>(), n2, g->adj_n,
+                                            flags.as<unsigned int>() + 1);
+    }
     // max degree (src/Graph.cpp:467-474)
     tmp.reset();
     DevBuf dmax;
@@ -466,7 +472,8 @@ __global__ void k_compact(uint64_t m, const unsigned long long* __restrict__ fla
 }
 
 // GraphFilter::generate_graph / GraphSampler::sample_graph on the device.
-int derive(const zg_graph* g, int mode, int op, int64_t t0, int64_t t1, double rate, uint64_t keep_seed,
+int derive(bool sampling_only, const zg_graph* g, int mode, int op, int64_t t0, int64_t t1, double rate,
+           uint64_t keep_seed,
            uint64_t shuffle_seed, cudaStream_t s, uint64_t* parent_index, uint64_t* out_m, zg_graph** out) {
   if (!g || !out) return zg_set_error(ZG_ERR_INVALID_ARG, "null argument"), ZG_ERR_INVALID_ARG;
   if (mode == 0 && !g->w) return zg_set_error(ZG_ERR_INVALID_ARG, "graph has no edge weights"), ZG_ERR_INVALID_ARG;
@@ -504,7 +511,7 @@ int derive(const zg_graph* g, int mode, int op, int64_t t0, int64_t t1, double r
     k_compact<<<grid_for(m, B), B, 0, s>>>(m, flag.as<unsigned long long>(), pos.as<unsigned long long>(),
                                            g->rec, g->w, coo, w, parent);
   if (shuffle_seed != ZG_NO_SHUFFLE) rc = permute(&coo, &w, &parent, kept, shuffle_seed, s);
-  if (rc == ZG_OK) rc = build_graph(coo, w, kept, g->d.nv, s, out);
+  if (rc == ZG_OK) rc = build_graph(coo, w, kept, g->d.nv, s, out, sampling_only);
   if (rc == ZG_OK) {
     // src/GraphFilters.cpp:90-135 (identical in src/Graph.cpp:704-749)
     double sample_rate_after_partition =
@@ -545,6 +552,23 @@ int upload_coo(const uint32_t* edges, const uint32_t* weights, uint64_t m, cudaS
 }
 
 }  // namespace
+
+// zg_graph_filter / zg_graph_subsample without the neighbour-ordered adjacency: derived graphs that
+// only the sampling kernels read (the batch cache, the error profile's subsample).
+int zg_graph_filter_sampling(const zg_graph* g, int pred_op, int64_t t0, int64_t t1, uint64_t shuffle_seed,
+                             cudaStream_t s, uint64_t* out_m, zg_graph** out) {
+  return derive(true, g, 0, pred_op, t0, t1, 0.0, 0, shuffle_seed, s, nullptr, out_m, out);
+}
+int zg_graph_subsample_sampling(const zg_graph* g, double rate, uint64_t keep_seed, uint64_t shuffle_seed,
+                                cudaStream_t s, uint64_t* out_m, zg_graph** out) {
+  return derive(true, g, 1, 0, 0, 0, rate, keep_seed, shuffle_seed, s, nullptr, out_m, out);
+}
+
+// A graph from a device COO in edge-id order (the device generators' entry into the build).
+int zg_build_graph_device(const uint2* d_coo, const uint32_t* d_w, uint64_t m, uint32_t nv, cudaStream_t s,
+                          zg_graph** out, bool sampling_only) {
+  return build_graph(d_coo, d_w, m, nv, s, out, sampling_only);
+}
 
 extern "C" int zg_graph_create(const uint32_t* edges, uint64_t m, uint32_t num_vertices,
                                const uint32_t* weights, void* cuda_stream, zg_graph** out) {
@@ -638,6 +662,9 @@ extern "C" int zg_graph_download(const zg_graph* g, uint32_t* edges, uint32_t* w
   if (ce == cudaSuccess && offsets)
     ce = cudaMemcpy(offsets, g->off, 8 * ((size_t)g->d.nv + 1), cudaMemcpyDeviceToHost);
   if (ce == cudaSuccess && adj_e && m) ce = cudaMemcpy(adj_e, g->adj_e, 16 * m, cudaMemcpyDeviceToHost);
+  if (adj_n && m && !g->adj_n)
+    return zg_set_error(ZG_ERR_INVALID_ARG, "this derived graph has no neighbour-ordered adjacency"),
+           ZG_ERR_INVALID_ARG;
   if (ce == cudaSuccess && adj_n && m) ce = cudaMemcpy(adj_n, g->adj_n, 16 * m, cudaMemcpyDeviceToHost);
   if (ce != cudaSuccess) return zg_check_cuda(ce, "download");
   return ZG_OK;
@@ -645,7 +672,7 @@ extern "C" int zg_graph_download(const zg_graph* g, uint32_t* edges, uint32_t* w
 
 extern "C" int zg_graph_filter(const zg_graph* g, int pred_op, int64_t t0, int64_t t1, uint64_t shuffle_seed,
                                void* cuda_stream, uint64_t* parent_index, uint64_t* out_m, zg_graph** out) {
-  return derive(g, 0, pred_op, t0, t1, 0.0, 0, shuffle_seed, (cudaStream_t)cuda_stream, parent_index, out_m,
+  return derive(false, g, 0, pred_op, t0, t1, 0.0, 0, shuffle_seed, (cudaStream_t)cuda_stream, parent_index, out_m,
                 out);
 }
 
@@ -653,6 +680,6 @@ extern "C" int zg_graph_subsample(const zg_graph* g, double rate, uint64_t keep_
                                   void* cuda_stream, uint64_t* parent_index, uint64_t* out_m, zg_graph** out) {
   if (!(rate >= 0.0 && rate <= 1.0))
     return zg_set_error(ZG_ERR_INVALID_ARG, "sample rate %g outside [0,1]", rate), ZG_ERR_INVALID_ARG;
-  return derive(g, 1, 0, 0, 0, rate, keep_seed, shuffle_seed, (cudaStream_t)cuda_stream, parent_index, out_m,
+  return derive(false, g, 1, 0, 0, 0, rate, keep_seed, shuffle_seed, (cudaStream_t)cuda_stream, parent_index, out_m,
                 out);
 }

@@ -32,6 +32,7 @@ PROG_TRIANGLE, PROG_FOUR_CLIQUE, PROG_THREE_CHAIN, PROG_FOUR_CHAIN, PROG_CHAIN, 
 EXACT_TRIANGLE, EXACT_WEDGE, EXACT_THREE_PATH, EXACT_FIVE_STAR, EXACT_FOUR_CLIQUE = 1, 2, 3, 4, 5
 PRED_GE, PRED_LT, PRED_GT, PRED_LE, PRED_EQ, PRED_NE, PRED_RANGE = 1, 2, 3, 4, 5, 6, 7
 QUERY_THREE_MOTIF = 16
+GRAPH_SAMPLING_ONLY = 1
 BATCH_MAX_QUERIES, BATCH_MAX_CHUNKS = 65536, 65536
 NO_SHUFFLE = 0xFFFFFFFFFFFFFFFF
 MAX_DRAWS = 16
@@ -71,7 +72,8 @@ class Counters(C.Structure):
 
 class BatchQuery(C.Structure):
     _fields_ = [("kind", C.c_int32), ("param", C.c_uint32), ("pred_op", C.c_int32), ("stream_id", C.c_uint32),
-                ("t0", C.c_int64), ("t1", C.c_int64), ("n", C.c_uint64), ("seed", C.c_uint64)]
+                ("t0", C.c_int64), ("t1", C.c_int64), ("n", C.c_uint64), ("seed", C.c_uint64),
+                ("first_sample", C.c_uint64), ("program", C.c_void_p)]
 
 
 class ElpResult(C.Structure):
@@ -151,6 +153,8 @@ def lib():
             "zg_gen_rmat": ([U32, U32, D, D, D, U64, U64, P, C.POINTER(U64)], I32),
             "zg_gen_chung_lu": ([U32, D, D, U64, U64, P, C.POINTER(U64)], I32),
             "zg_gen_weights": ([U64, U32, U64, P], I32),
+            "zg_graph_gen_rmat": ([U32, U32, D, D, D, U64, U32, U64, U32, P, C.POINTER(P)], I32),
+            "zg_graph_gen_chung_lu": ([U32, D, D, U64, U32, U64, U32, P, C.POINTER(P)], I32),
             "zg_batch_create": ([P, U32, U64, U64, C.POINTER(P)], I32),
             "zg_batch_free": ([P], I32),
             "zg_batch_submit": ([P, P, U32, P], I32),
@@ -236,6 +240,26 @@ class Graph:
         return cls(h, num_vertices, parent)
 
     @classmethod
+    def gen_rmat(cls, scale, edge_factor, a=0.57, b=0.19, c=0.19, seed=1, max_weight=0, weight_seed=1,
+                 sampling_only=False):
+        """zg_graph_gen_rmat: the seeded R-MAT graph generated and built on the device."""
+        init()
+        h = C.c_void_p()
+        check(lib().zg_graph_gen_rmat(scale, edge_factor, a, b, c, seed, max_weight, weight_seed,
+                                      GRAPH_SAMPLING_ONLY if sampling_only else 0, None, C.byref(h)))
+        return cls(h, 1 << scale)
+
+    @classmethod
+    def gen_chung_lu(cls, num_vertices, exponent, avg_degree, seed=1, max_weight=0, weight_seed=1,
+                     sampling_only=False):
+        """zg_graph_gen_chung_lu: the seeded Chung-Lu graph generated and built on the device."""
+        init()
+        h = C.c_void_p()
+        check(lib().zg_graph_gen_chung_lu(num_vertices, exponent, avg_degree, seed, max_weight, weight_seed,
+                                          GRAPH_SAMPLING_ONLY if sampling_only else 0, None, C.byref(h)))
+        return cls(h, num_vertices)
+
+    @classmethod
     def load(cls, path, weighted=False, shuffle_seed=None):
         """Reads the reference's binary .biedgelist (+ .csv vertex count, src/Utilities.cpp:24-35)."""
         raw = np.fromfile(path + ".biedgelist", dtype=np.uint32)
@@ -278,11 +302,14 @@ class Graph:
     def set_meta(self, num_edges, max_degree):
         check(lib().zg_graph_set_meta(self.handle, num_edges, max_degree))
 
-    def download(self):
+    def download(self, neighbour_order=True):
+        """Device arrays on the host; neighbour_order=False skips adj_n (absent from the graphs a
+        batch caches)."""
         m = self.num_local_edges
         nv = self.num_vertices
         out = {"edges": np.empty((m, 2), np.uint32), "offsets": np.empty(nv + 1, np.int64),
-               "adj_e": np.empty((2 * m, 2), np.uint32), "adj_n": np.empty((2 * m, 2), np.uint32),
+               "adj_e": np.empty((2 * m, 2), np.uint32),
+               "adj_n": np.empty((2 * m, 2), np.uint32) if neighbour_order else None,
                "suffix": np.empty((m, 2), np.uint32)}
         w = np.empty(m, np.uint32) if self.meta().weighted else None
         check(lib().zg_graph_download(self.handle, _ptr(out["edges"]), _ptr(w), _ptr(out["offsets"]),
@@ -342,9 +369,11 @@ class Batch:
 
     @staticmethod
     def queries(qs):
-        """qs: iterable of dicts with kind, n, seed and optional param, pred_op, t0, t1, stream_id."""
+        """qs: iterable of dicts with kind, n, seed and optional param, pred_op, t0, t1, stream_id,
+        first_sample and program (a Program, for PROG_PATTERN)."""
         qs = list(qs)
         arr = (BatchQuery * max(1, len(qs)))()
+        keep = []
         for i, q in enumerate(qs):
             arr[i].kind = q["kind"]
             arr[i].param = q.get("param", 0)
@@ -354,17 +383,24 @@ class Batch:
             arr[i].t1 = q.get("t1", 0)
             arr[i].n = q["n"]
             arr[i].seed = q["seed"]
-        return arr, len(qs)
+            arr[i].first_sample = q.get("first_sample", 0)
+            prog = q.get("program")
+            if prog is not None:
+                arr[i].program = prog._h
+                keep.append(prog)
+        return arr, len(qs), keep
 
     def submit(self, qs, cuda_stream=None):
-        arr, nq = self.queries(qs)
+        arr, nq, keep = self.queries(qs)
         check(lib().zg_batch_submit(self._h, arr, nq, cuda_stream))
         self._nq = nq
+        self._keep = keep  # pattern programs stay alive until the batch completes
 
     def wait(self):
         """Counters per query: [(c, None) or (chain, triangle) for 3-motif queries]."""
         out = (Counters * max(2, 2 * self._nq))()
         check(lib().zg_batch_wait(self._h, out))
+        self._keep = []
         return [(out[2 * i], out[2 * i + 1]) for i in range(self._nq)]
 
     def run(self, qs, cuda_stream=None):
@@ -380,7 +416,7 @@ class Batch:
         return g
 
     def tune(self, qs, cuda_stream=None):
-        arr, nq = self.queries(qs)
+        arr, nq, keep = self.queries(qs)
         best = C.c_int(0)
         ms = (C.c_float * 3)()
         check(lib().zg_batch_tune(self._h, arr, nq, cuda_stream, C.byref(best), ms))

@@ -83,7 +83,7 @@ def test_filtered_graph_matches_zg_graph_filter_semantics(wgraph):
     fg = b.filtered_graph(Z.PRED_GE, 50)
     d = wgraph.download()
     assert fg.num_local_edges == int((d["weights"] >= 50).sum())
-    fd = fg.download()
+    fd = fg.download(neighbour_order=False)
     assert (fd["weights"] >= 50).all()
     # same edge multiset as the base graph's kept edges
     keep = d["edges"][d["weights"] >= 50]
@@ -131,3 +131,21 @@ def test_refusals(wgraph):
     # the batch still works after refusals
     c = b.run([{"kind": Z.PROG_TRIANGLE, "n": 1000, "seed": 2}])[0][0]
     _same(c, Z.Program(Z.PROG_TRIANGLE).run(wgraph, 1000, 2), "after refusal")
+
+
+def test_pattern_queries_and_first_sample(wgraph):
+    star = Z.Program(Z.PROG_PATTERN, pattern=(5, [(0, 1), (0, 2), (0, 3), (0, 4)]))
+    house = Z.Program(Z.PROG_PATTERN, pattern=(5, [(0, 1), (0, 2), (1, 2), (1, 3), (2, 4), (3, 4)]))
+    tri = Z.Program(Z.PROG_PATTERN, pattern=(3, [(0, 1), (0, 2), (1, 2)]))
+    qs = [{"kind": Z.PROG_PATTERN, "program": star, "n": 300000, "seed": 4, "stream_id": 2},
+          {"kind": Z.PROG_TRIANGLE, "n": 50000, "seed": 9, "first_sample": 12345},
+          {"kind": Z.PROG_PATTERN, "program": house, "n": 200000, "seed": 5, "first_sample": 777},
+          {"kind": Z.PROG_PATTERN, "program": tri, "pred_op": Z.PRED_GE, "t0": 30, "n": 100000, "seed": 6},
+          {"kind": Z.PROG_FOUR_CHAIN, "n": 70000, "seed": 8, "first_sample": 1 << 40}]
+    b = Z.Batch(wgraph, max_queries=8)
+    res = b.run(qs)
+    for q, (c, _) in zip(qs, res):
+        gg = b.filtered_graph(q["pred_op"], q["t0"]) if q.get("pred_op") else wgraph
+        p = q.get("program") or Z.Program(q["kind"])
+        _same(c, p.run(gg, q["n"], q["seed"], stream_id=q.get("stream_id", 0),
+                       first_sample=q.get("first_sample", 0)), q)
