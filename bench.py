@@ -37,6 +37,16 @@ WORKLOADS = {
     "rmat13": {"scale": 13, "edge_factor": 12, "a": 0.57, "b": 0.19, "c": 0.19, "seed": 1, "samples": 1 << 20,
                "programs": ["triangle"]},
 }
+# Batched workloads (one submit of many queries per step; graphs generated on the device):
+#   chunglu_batch: Chung-Lu 4.8 M vertices, exponent 2.3, ~43 M edges, edge data in [0, 100);
+#                  512 queries over {triangle, 3-motif, all-predicate w >= T, at-least-one w >= T},
+#                  T uniform in [10, 90], budgets 2^U(12, 24).
+#   rmat26:        R-MAT scale 26, edge factor 24 (~1.4 G edges); 4-clique, 5-star, 5-house at 2^30.
+BATCH_WORKLOADS = {
+    "chunglu_batch": {"gen": "chung_lu", "n": 4800000, "exponent": 2.3, "avg_degree": 18.0, "seed": 2024,
+                      "max_weight": 100, "queries": 512},
+    "rmat26": {"gen": "rmat", "scale": 26, "edge_factor": 24, "seed": 26, "samples": 1 << 30},
+}
 PROG_IDS = {"triangle": 1, "four_clique": 2, "three_chain": 3, "four_chain": 4}
 EXACT_IDS = {"triangle": 1, "three_chain": 2, "four_chain": 3, "four_clique": 5}
 
@@ -47,7 +57,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="rmat20", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="rmat20", choices=sorted(WORKLOADS) + sorted(BATCH_WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-time-to-bound", action="store_true")
     ap.add_argument("--variants", default=None,
@@ -401,9 +411,128 @@ def run_gb300(args):
         torch.distributed.destroy_process_group()
 
 
+def batch_queries(Z, rng, nq):
+    """The Chung-Lu batched workload's queries; an at-least-one-predicate query is two batch
+    queries (all triangles, and triangles of the w < T graph) whose estimates are subtracted."""
+    qs = []
+    for i in range(nq):
+        kind = int(rng.integers(4))
+        n = int(2 ** rng.uniform(12, 24))
+        t = int(rng.integers(10, 91))
+        seed = int(rng.integers(1, 1 << 40))
+        if kind == 0:
+            qs.append({"kind": Z.PROG_TRIANGLE, "n": n, "seed": seed, "stream_id": i})
+        elif kind == 1:
+            qs.append({"kind": Z.QUERY_THREE_MOTIF, "n": n, "seed": seed, "stream_id": 2 * i})
+        elif kind == 2:
+            qs.append({"kind": Z.PROG_TRIANGLE, "n": n, "seed": seed, "pred_op": Z.PRED_GE, "t0": t, "stream_id": i})
+        else:
+            qs.append({"kind": Z.PROG_TRIANGLE, "n": n, "seed": seed, "stream_id": i})
+            qs.append({"kind": Z.PROG_TRIANGLE, "n": n, "seed": seed + 1, "pred_op": Z.PRED_LT, "t0": t,
+                       "stream_id": i})
+    return qs
+
+
+def run_batch(args):
+    """One step = one submit of the workload's queries (zg_batch: persistent kernel replayed through
+    a CUDA graph).  value: samples/s from CUDA events around the graph launch; e2e: submit + wait
+    wall time (descriptors in, counters out)."""
+    import numpy as np
+    import torch
+    import zgraph as Z
+    wl = BATCH_WORKLOADS[args.workload]
+    Z.init(0)
+    torch.cuda.set_device(0)
+    t0 = time.perf_counter()
+    if wl["gen"] == "chung_lu":
+        g = Z.Graph.gen_chung_lu(wl["n"], wl["exponent"], wl["avg_degree"], seed=wl["seed"],
+                                 max_weight=wl["max_weight"], weight_seed=7)
+        qs = batch_queries(Z, np.random.default_rng(3), wl["queries"])
+        desc = ("Chung-Lu %d vertices, exponent %.1f, %d edges, edge data in [0, 100); %d queries (%d batch "
+                "queries) over triangle / 3-motif / all-predicate / at-least-one-predicate, budgets 2^U(12,24)"
+                % (wl["n"], wl["exponent"], g.num_local_edges, wl["queries"], len(qs)))
+    else:
+        g = Z.Graph.gen_rmat(wl["scale"], wl["edge_factor"], seed=wl["seed"], sampling_only=True)
+        star = Z.Program(Z.PROG_PATTERN, pattern=(5, [(0, 1), (0, 2), (0, 3), (0, 4)]))
+        house = Z.Program(Z.PROG_PATTERN, pattern=(5, [(0, 1), (0, 2), (1, 2), (1, 3), (2, 4), (3, 4)]))
+        n = wl["samples"]
+        qs = [{"kind": Z.PROG_FOUR_CLIQUE, "n": n, "seed": 1},
+              {"kind": Z.PROG_PATTERN, "program": star, "n": n, "seed": 2},
+              {"kind": Z.PROG_PATTERN, "program": house, "n": n, "seed": 3}]
+        desc = ("R-MAT scale %d, edge factor %d, %d edges (built on the device); 4-clique, 5-star, 5-house x 2^%d"
+                % (wl["scale"], wl["edge_factor"], g.num_local_edges, n.bit_length() - 1))
+    torch.cuda.synchronize()
+    gen_s = time.perf_counter() - t0
+    b = Z.Batch(g, max_queries=max(8, len(qs)), cache_bytes=200 << 30)
+    t0 = time.perf_counter()
+    first = b.run(qs)  # builds the filtered graphs the predicates need
+    first_s = time.perf_counter() - t0
+    best, ms_variants = b.tune(qs)
+    samples = sum(q["n"] for q in qs) + sum(q["n"] for q in qs if q["kind"] == Z.QUERY_THREE_MOTIF)
+    for _ in range(max(0, args.warmup - 1)):
+        b.run(qs)
+    st = torch.cuda.current_stream()
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    clocks = ClockSampler(0)
+    clocks.start()
+    dev_ms, wall = [], []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        w0 = time.perf_counter()
+        b.submit(qs, cuda_stream=st.cuda_stream)
+        res = b.wait()
+        wall.append(time.perf_counter() - w0)
+        dev_ms.append(b.elapsed_ms())  # CUDA events on the stream around the batch's graph launch
+    clk = clocks.stop()
+    total_ms = sum(dev_ms)
+    value = samples * args.steps / (total_ms / 1000.0)
+    # algorithmic bytes: access-model sectors per sample of every (program, graph) pair, 2^14 samples
+    model_bytes, seen = 0.0, {}
+    for q in qs:
+        key = (q["kind"], q.get("pred_op", 0), q.get("t0", 0), id(q.get("program")))
+        if key not in seen:
+            gg = b.filtered_graph(q["pred_op"], q["t0"]) if q.get("pred_op") else g
+            if q["kind"] == Z.QUERY_THREE_MOTIF:
+                tc, tt = Z.run_three_motif_debug(gg, 1 << 14, 1 << 14, 5)[:2]
+                seen[key] = 32.0 * (float(tc["sectors"].mean()) + float(tt["sectors"].mean()))
+            else:
+                p = q.get("program") or Z.Program(q["kind"])
+                seen[key] = 32.0 * float(p.run_debug(gg, 1 << 14, 5)["sectors"].mean())
+        model_bytes += seen[key] * q["n"]
+    peak, peak_kind = peaks()
+    ach = model_bytes / (total_ms / args.steps / 1000.0) / 1e9
+    h2d = len(qs) * 72 + 8 * (Z.BATCH_MAX_CHUNKS + max(8, len(qs))) + 16
+    line = {"metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int64/u192 exact", "data": "synthetic (device generator)",
+            "config": {"workload": "%s: %s" % (args.workload, desc), "queries_per_step": len(qs),
+                       "samples_per_step": samples, "graph_gen_and_build_s": round(gen_s, 3),
+                       "first_batch_s (builds filtered graphs)": round(first_s, 3),
+                       "batch_variant": best, "ms_per_variant": [round(x, 3) for x in ms_variants],
+                       "l2": "flushed between steps (512 MiB write)"},
+            "e2e": {"value": samples * args.steps / sum(wall), "unit": "samples/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": 2 * 112 * max(8, len(qs)),
+                    "queries_per_s": len(qs) * args.steps / sum(wall)},
+            "gpu_launches": 3 * args.steps, "clocks": clk,
+            "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                         "traffic": None, "kernel": "k_batch (all queries of the step)",
+                         "peak_source": peak_kind}}
+    if wl["gen"] == "rmat":
+        line["results"] = {name: {"hits": int(c.hits), "estimate": c.estimate}
+                           for name, (c, _) in zip(["four_clique", "five_star", "five_house"], res)}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
-    if args.impl == "reference":
+    if args.workload in BATCH_WORKLOADS:
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the batched workloads have no CPU arm here: the "
+                              "reference runs one query at a time; see the rmat20 workload's reference arm"}))
+        else:
+            run_batch(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gb300(args)

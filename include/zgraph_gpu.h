@@ -269,6 +269,8 @@ int zg_batch_submit(zg_batch* b, const zg_batch_query* queries, uint32_t nq, voi
 /* Waits for the submitted batch; out[2i] receives query i's counters (ZG_QUERY_THREE_MOTIF:
  * out[2i] the 3-chain, out[2i+1] the triangle). */
 int zg_batch_wait(zg_batch* b, zg_counters* out);
+/* Device time of the last waited batch (CUDA events around its graph launch), in ms. */
+int zg_batch_elapsed_ms(const zg_batch* b, float* ms);
 /* The cached filtered graph of a predicate (built if missing): what a filtered query samples. */
 int zg_batch_filtered_graph(zg_batch* b, int pred_op, int64_t t0, int64_t t1, void* cuda_stream,
                             const zg_graph** out);

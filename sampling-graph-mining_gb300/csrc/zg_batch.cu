@@ -278,6 +278,8 @@ struct zg_batch {
   cudaGraphExec_t exec = nullptr;
   cudaStream_t last_stream = nullptr;
   bool submitted = false;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;  // around the graph launch
+  float last_ms = 0;
 };
 
 namespace {
@@ -415,6 +417,10 @@ extern "C" int zg_batch_create(const zg_graph* base, uint32_t max_queries, uint6
     zg_batch_free(b);
     return zg_set_error(ZG_ERR_OOM, "pinned host buffers: %s", cudaGetErrorString(e)), ZG_ERR_OOM;
   }
+  if ((e = cudaEventCreate(&b->ev0)) || (e = cudaEventCreate(&b->ev1))) {
+    zg_batch_free(b);
+    return zg_check_cuda(e, "batch events");
+  }
   memset(b->h_hdr, 0, sizeof(BatchHeader));
   memset(b->h_q, 0, sizeof(BatchQuery) * max_queries);
   memset(b->h_work, 0, sizeof(BatchWork) * b->max_work);
@@ -430,6 +436,8 @@ extern "C" int zg_batch_free(zg_batch* b) {
   if (!b) return ZG_OK;
   if (b->submitted && b->last_stream) cudaStreamSynchronize(b->last_stream);
   batch_release_graph(b);
+  if (b->ev0) cudaEventDestroy(b->ev0);
+  if (b->ev1) cudaEventDestroy(b->ev1);
   for (auto& kv : b->cache) zg_graph_free(kv.second.g);
   cudaFree(b->d_hdr);
   cudaFree(b->d_q);
@@ -555,8 +563,10 @@ extern "C" int zg_batch_submit(zg_batch* b, const zg_batch_query* q, uint32_t nq
   // built-in programs carry no device tables: their descriptors are complete without them
   for (auto* p : own)
     if (p) zg_program_free(p);
+  cudaEventRecord(b->ev0, s);
   cudaError_t e = cudaGraphLaunch(b->exec, s);
   if (e) return zg_check_cuda(e, "batch graph launch");
+  cudaEventRecord(b->ev1, s);
   b->last_stream = s;
   b->submitted = true;
   return ZG_OK;
@@ -567,6 +577,7 @@ extern "C" int zg_batch_wait(zg_batch* b, zg_counters* out) {
   if (!b->submitted) return zg_set_error(ZG_ERR_INVALID_ARG, "zg_batch_wait: nothing submitted"), ZG_ERR_INVALID_ARG;
   cudaError_t e = cudaStreamSynchronize(b->last_stream);
   if (e) return zg_check_cuda(e, "batch");
+  cudaEventElapsedTime(&b->last_ms, b->ev0, b->ev1);
   for (uint32_t i = 0; i < b->nq; ++i) {
     zg_partial_to_counters(&b->h_out[2 * i], b->den[i], &out[2 * i]);
     zg_partial_to_counters(&b->h_out[2 * i + 1], b->den[i], &out[2 * i + 1]);
@@ -609,4 +620,10 @@ extern "C" int zg_batch_tune(zg_batch* b, const zg_batch_query* q, uint32_t nq, 
   if (rc) return rc;
   if (best_variant) *best_variant = best;
   return batch_set_variant(b, best);
+}
+
+extern "C" int zg_batch_elapsed_ms(const zg_batch* b, float* ms) {
+  if (!b || !ms) return zg_set_error(ZG_ERR_INVALID_ARG, "zg_batch_elapsed_ms: null argument"), ZG_ERR_INVALID_ARG;
+  *ms = b->last_ms;
+  return ZG_OK;
 }

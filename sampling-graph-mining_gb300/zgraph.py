@@ -161,6 +161,7 @@ def lib():
             "zg_batch_wait": ([P, P], I32),
             "zg_batch_filtered_graph": ([P, I32, I64, I64, P, C.POINTER(P)], I32),
             "zg_batch_tune": ([P, P, U32, P, C.POINTER(I32), P], I32),
+            "zg_batch_elapsed_ms": ([P, C.POINTER(C.c_float)], I32),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -406,6 +407,12 @@ class Batch:
     def run(self, qs, cuda_stream=None):
         self.submit(qs, cuda_stream)
         return self.wait()
+
+    def elapsed_ms(self):
+        """Device time of the last waited batch (CUDA events around its graph launch)."""
+        ms = C.c_float(0)
+        check(lib().zg_batch_elapsed_ms(self._h, C.byref(ms)))
+        return ms.value
 
     def filtered_graph(self, op, t0, t1=0):
         """The cached filtered graph a predicate query samples (owned by the batch)."""
