@@ -144,16 +144,24 @@ __host__ __device__ __forceinline__ uint64_t zg_mulhi64(uint64_t a, uint64_t b) 
 #endif
 }
 
-// Draw d of `sample` in [lo, hi]: counter (sample, d, stream), key seed; multiply-high mapping.
-__host__ __device__ __forceinline__ uint64_t zg_draw(uint64_t seed, uint32_t stream, uint64_t sample,
-                                                     uint32_t d, uint64_t lo, uint64_t hi) {
+// The 64-bit Philox word of draw d of `sample`: counter (sample, d, stream), key seed.
+__host__ __device__ __forceinline__ uint64_t zg_draw_word(uint64_t seed, uint32_t stream, uint64_t sample,
+                                                          uint32_t d) {
   uint32_t o0, o1;
   zg_philox((uint32_t)sample, (uint32_t)(sample >> 32), d, stream, (uint32_t)seed,
             (uint32_t)(seed >> 32), o0, o1);
-  uint64_t r = ((uint64_t)o1 << 32) | o0;
+  return ((uint64_t)o1 << 32) | o0;
+}
+// A draw's word mapped to [lo, hi] by multiply-high.
+__host__ __device__ __forceinline__ uint64_t zg_draw_map(uint64_t r, uint64_t lo, uint64_t hi) {
   uint64_t range = hi - lo + 1;
   if (range == 0) return r;
   return lo + zg_mulhi64(r, range);
+}
+// Draw d of `sample` in [lo, hi].
+__host__ __device__ __forceinline__ uint64_t zg_draw(uint64_t seed, uint32_t stream, uint64_t sample,
+                                                     uint32_t d, uint64_t lo, uint64_t hi) {
+  return zg_draw_map(zg_draw_word(seed, stream, sample, d), lo, hi);
 }
 
 // 192-bit unsigned numerator.

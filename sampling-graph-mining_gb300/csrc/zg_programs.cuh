@@ -30,8 +30,12 @@ struct Ctx {
   uint32_t nd;
   zg_sample_trace* tr;  // debug only
   uint32_t sectors;     // debug only: access model, 32-byte sectors
-  __device__ __forceinline__ uint64_t draw(uint64_t lo, uint64_t hi) {
-    uint64_t v = zg_draw(seed, stream, sample, nd, lo, hi);
+  __device__ __forceinline__ uint64_t draw(uint64_t lo, uint64_t hi) { return take(word(nd), lo, hi); }
+  // The Philox word of draw k, computable before the range it maps to is known (so the integer
+  // work overlaps the loads that determine the range); take() maps the next draw's word.
+  __device__ __forceinline__ uint64_t word(uint32_t k) const { return zg_draw_word(seed, stream, sample, k); }
+  __device__ __forceinline__ uint64_t take(uint64_t w, uint64_t lo, uint64_t hi) {
+    uint64_t v = zg_draw_map(w, lo, hi);
     if (tr && nd < ZG_MAX_DRAWS) {
       tr->lo[nd] = lo;
       tr->hi[nd] = hi;
@@ -279,8 +283,10 @@ __device__ void prog_triangle(const ZgDevGraph& g, Ctx& c, Res& r) {
     r.fail = true;
     return;
   }
+  const uint64_t w1 = c.word(1);  // the second draw's Philox work overlaps the first loads
   uint64_t e0 = c.draw(0, g.m - 1);
   uint4 q = ZG_LDG(&g.rec[e0]);
+  uint32_t endx = ZG_LDG(&g.off32[q.x + 1]), endy = ZG_LDG(&g.off32[q.y + 1]);
   uint64_t S = (uint64_t)q.z + q.w;
   if (DBG) c.sectors += 1 + model_anchor(g, q.x) + model_anchor(g, q.y);
   if (S == 0) {
@@ -288,15 +294,10 @@ __device__ void prog_triangle(const ZgDevGraph& g, Ctx& c, Res& r) {
     return;
   }
   if (DBG) c.sectors += 1;
-  uint64_t r1 = c.draw(0, S - 1);
-  uint32_t anchor = q.x, other = q.y, suf = q.z;
-  if (r1 >= q.z) {
-    r1 -= q.z;
-    anchor = q.y;
-    other = q.x;
-    suf = q.w;
-  }
-  uint32_t idx = ZG_LDG(&g.off32[anchor + 1]) - (uint32_t)suf + (uint32_t)r1;
+  uint64_t r1 = c.take(w1, 0, S - 1);
+  const bool on_y = r1 >= q.z;  // the conditional edge hangs off dst
+  const uint32_t other = on_y ? q.x : q.y;
+  uint32_t idx = on_y ? endy - q.w + (uint32_t)(r1 - q.z) : endx - q.z + (uint32_t)r1;
   uint2 e1 = ZG_LDG(&g.adj_e[idx]);
   uint32_t a1 = 1 + (e1.x == q.x || e1.x == q.y);
   res_mul(r, g.m);
@@ -364,6 +365,7 @@ __device__ void prog_four_clique(const ZgDevGraph& g, Ctx& c, Res& r) {
     r.fail = true;
     return;
   }
+  const uint64_t w1 = c.word(1), w2 = c.word(2);  // Philox work of the later draws, up front
   uint64_t e0 = c.draw(0, g.m - 1);
   uint4 q = ZG_LDG(&g.rec[e0]);
   uint64_t S1 = (uint64_t)q.z + q.w;
@@ -373,7 +375,7 @@ __device__ void prog_four_clique(const ZgDevGraph& g, Ctx& c, Res& r) {
     return;
   }
   if (DBG) c.sectors += 1;
-  uint64_t r1 = c.draw(0, S1 - 1);
+  uint64_t r1 = c.take(w1, 0, S1 - 1);
   const uint32_t va = q.x, vb = q.y;
   uint32_t endA = ZG_LDG(&g.off32[va + 1]), endB = ZG_LDG(&g.off32[vb + 1]);
   const bool s1b = r1 >= q.z;  // the first conditional edge hangs off b
@@ -404,7 +406,7 @@ __device__ void prog_four_clique(const ZgDevGraph& g, Ctx& c, Res& r) {
     return;
   }
   if (DBG) c.sectors += 1;
-  uint64_t r2 = c.draw(0, S2 - 1);
+  uint64_t r2 = c.take(w2, 0, S2 - 1);
   int s2;
   uint32_t pos2;
   if (r2 < lenA) {
@@ -426,8 +428,7 @@ __device__ void prog_four_clique(const ZgDevGraph& g, Ctx& c, Res& r) {
   if (a1 != 1 || dup) return;  // three vertices: a triangle was sampled (FourClique.cpp:224-226)
   // closure: the 3 vertex pairs not sampled, all with edge id >= id2 + 1.  Sampled pairs are
   // (a,b), (anchor of e1, c) and (anchor of e2, d).  The reference checks the pairs in slot order
-  // up to the first miss (the debug access model follows that); production issues all three
-  // look-ups at once.
+  // up to the first miss (the debug access model follows that).
   const int s1 = s1b ? 1 : 0;
   uint32_t mv2 = e2.y + 1;
   auto vslot = [&](int i) { return i == 0 ? va : i == 1 ? vb : i == 2 ? vc : vd; };
@@ -445,11 +446,17 @@ __device__ void prog_four_clique(const ZgDevGraph& g, Ctx& c, Res& r) {
     uint32_t x0 = s1b ? va : vb;             // the pair (not-anchor-of-e1, c)
     uint32_t x1 = vslot(s2 == 0 ? 1 : 0);    // the two pairs (?, d) other than e2's own
     uint32_t x2 = vslot(s2 == 2 ? 1 : 2);
-    EdgeProbe p0 = edge_candidate(g, x0, vc), p1 = edge_candidate(g, x1, vd), p2 = edge_candidate(g, x2, vd);
-    ok = p0.cand != ZG_HASH_EMPTY && p1.cand != ZG_HASH_EMPTY && p2.cand != ZG_HASH_EMPTY;
-    if (ok)
-      ok = edge_confirm(g, p0) >= (int64_t)mv2 && edge_confirm(g, p1) >= (int64_t)mv2 &&
-           edge_confirm(g, p2) >= (int64_t)mv2;
+    // the pair closing the first two edges fails most often: look it up first, the other two
+    // only when it exists
+    EdgeProbe p0 = edge_candidate(g, x0, vc);
+    ok = p0.cand != ZG_HASH_EMPTY;
+    if (ok) {
+      EdgeProbe p1 = edge_candidate(g, x1, vd), p2 = edge_candidate(g, x2, vd);
+      ok = p1.cand != ZG_HASH_EMPTY && p2.cand != ZG_HASH_EMPTY;
+      if (ok)
+        ok = edge_confirm(g, p0) >= (int64_t)mv2 && edge_confirm(g, p1) >= (int64_t)mv2 &&
+             edge_confirm(g, p2) >= (int64_t)mv2;
+    }
   }
   r.hit = ok;
   if (DBG && ok) {
@@ -464,6 +471,7 @@ __device__ void prog_four_clique(const ZgDevGraph& g, Ctx& c, Res& r) {
 // ---- FourChain: applications/FourChain.cpp:24-124 ----------------------------------------
 template <bool DBG>
 __device__ void prog_four_chain(const ZgDevGraph& g, Ctx& c, Res& r) {
+  const uint64_t w2 = c.word(2), w3 = c.word(3);  // Philox work of the later draws, up front
   uint64_t sel = c.draw(1, 3);
   res_mul(r, 3);
   if (g.m == 0) {
@@ -487,7 +495,7 @@ __device__ void prog_four_chain(const ZgDevGraph& g, Ctx& c, Res& r) {
       return;
     }
     if (DBG) c.sectors += 1;
-    uint64_t r1 = c.draw(0, S1 - 1);
+    uint64_t r1 = c.take(w2, 0, S1 - 1);
     uint32_t anchor = a, suf = q.z;
     if (r1 >= q.z) {
       r1 -= q.z;
@@ -524,7 +532,7 @@ __device__ void prog_four_chain(const ZgDevGraph& g, Ctx& c, Res& r) {
       return;
     }
     if (DBG) c.sectors += 1;
-    uint64_t r2 = c.draw(0, S2 - 1);
+    uint64_t r2 = c.take(w3, 0, S2 - 1);
     uint2 e2 = ZG_LDG(&g.adj_e[lbn + (uint32_t)r2]);
     a2 = 1 + (e2.x == nw);
     res_mul(r, S2);
@@ -540,7 +548,7 @@ __device__ void prog_four_chain(const ZgDevGraph& g, Ctx& c, Res& r) {
       return;
     }
     if (DBG) c.sectors += 1;
-    uint64_t r1 = c.draw(0, S1 - 1);
+    uint64_t r1 = c.take(w2, 0, S1 - 1);
     uint2 e1 = ZG_LDG(&g.adj_e[ZG_LDG(&g.off32[a + 1]) - (uint32_t)q.z + (uint32_t)r1]);
     a1 = 1 + (e1.x == a);
     res_mul(r, S1);
@@ -552,7 +560,7 @@ __device__ void prog_four_chain(const ZgDevGraph& g, Ctx& c, Res& r) {
       return;
     }
     if (DBG) c.sectors += 1;
-    uint64_t r2 = c.draw(0, S2 - 1);
+    uint64_t r2 = c.take(w3, 0, S2 - 1);
     uint2 e2 = ZG_LDG(&g.adj_e[ZG_LDG(&g.off32[b + 1]) - (uint32_t)q.w + (uint32_t)r2]);
     a2 = 1 + (e2.x == b);
     res_mul(r, S2);
