@@ -45,6 +45,12 @@ extern "C" {
 #define ZG_PROG_FOUR_CHAIN    4  /* applications/FourChain.cpp:24-124                           */
 #define ZG_PROG_CHAIN         5  /* applications/ChainMining.cpp:240-84 (param = order k)       */
 #define ZG_PROG_PATTERN       6  /* SamplerGenerator<Empty>::estimate, src/SamplerGenerator.cpp */
+/* No counterpart in the reference: FourClique's draws, but a sample counts only if it followed the
+ * clique's canonical path (e0 the smallest of the six edge ids; e1 the smallest edge joining e0's
+ * endpoints to the other two vertices; e2 the smallest edge id above e1 at the fourth vertex), so
+ * every 4-clique is counted exactly once: unbiased, where the reference's estimator counts only
+ * cliques whose three smallest edges grow connectedly (60 % of them for random edge ids). */
+#define ZG_PROG_FOUR_CLIQUE_UNBIASED 7
 
 /* ---- exact counters: naive_implementation/<Counter>.cpp --------------------------- */
 #define ZG_EXACT_TRIANGLE     1  /* TriangleCounting.cpp            */

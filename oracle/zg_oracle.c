@@ -338,6 +338,59 @@ static double prog_four_clique(zgo_ctx* c) {
   return 0;
 }
 
+/* The edge id of (x, y), any id, or -1 (a scan of the shorter edge-id-ordered list). */
+static int64_t find_edge_id(zgo_ctx* c, uint32_t x, uint32_t y) {
+  const zgo_graph* g = c->g;
+  uint64_t dx = g->off[x + 1] - g->off[x], dy = g->off[y + 1] - g->off[y];
+  c->sectors += 2 + zgo_model_search(dx < dy ? dx : dy);
+  uint32_t v = dx <= dy ? x : y, t = dx <= dy ? y : x;
+  for (uint64_t idx = g->off[v]; idx < g->off[v + 1]; ++idx)
+    if (g->adj_nbr[idx] == t) return (int64_t)g->adj_eid[idx];
+  return -1;
+}
+
+/* The unbiased 4-clique estimator (no counterpart in the reference): FourClique's draws; the three
+ * unsampled pairs must be edges (any id), looked up in the order (the other of a and b, c), then the
+ * two pairs at d in slot order, up to the first missing one; and the sample must be the clique's
+ * canonical path: id0 the smallest of the six ids, id1 the smallest of the four edges joining
+ * {a, b} to {c, d}, id2 the smallest id above id1 among the edges at d.  Each 4-clique has exactly
+ * one canonical path, which the draws reach with positive probability, so E[estimate] = #4-cliques. */
+static double prog_four_clique_unbiased(zgo_ctx* c) {
+  zgo_sub sg; sub_init(&sg);
+  double p = 1;
+  zgo_edge e0, e1, e2;
+  double t = prim_sample_edge(c, &e0);
+  if (t < 0) return -1;
+  p *= t; sub_add_edge(&sg, e0);
+  t = prim_cond_sample(c, sg.e, sg.ne, sg.v, sg.nv, &e1);
+  if (t < 0) return -1;
+  p *= t; sub_add_edge(&sg, e1);
+  t = prim_cond_sample(c, sg.e, sg.ne, sg.v, sg.nv, &e2);
+  if (t < 0) return -1;
+  p *= t; sub_add_edge(&sg, e2);
+  if (sg.nv == 3) return 0;
+  const uint32_t* v = sg.v; /* a, b, c, d in insertion order */
+  int s1 = e1.src == v[0] ? 0 : 1;
+  int s2 = e2.src == v[0] ? 0 : (e2.src == v[1] ? 1 : 2);
+  int x0 = 1 - s1, x1 = s2 == 0 ? 1 : 0, x2 = s2 == 2 ? 1 : 2;
+  int64_t h0 = find_edge_id(c, v[x0], v[2]);
+  if (h0 < 0) return 0;
+  int64_t h1 = find_edge_id(c, v[x1], v[3]);
+  if (h1 < 0) return 0;
+  int64_t h2 = find_edge_id(c, v[x2], v[3]);
+  if (h2 < 0) return 0;
+  uint64_t id0 = e0.eid, id1 = e1.eid, id2 = e2.eid;
+  uint64_t d[3];
+  d[s2] = id2;
+  d[x1] = (uint64_t)h1;
+  d[x2] = (uint64_t)h2;
+  if ((uint64_t)h0 < id0 || (uint64_t)h1 < id0 || (uint64_t)h2 < id0) return 0;
+  if ((uint64_t)h0 < id1 || d[0] < id1 || d[1] < id1) return 0;
+  for (int i = 0; i < 3; ++i)
+    if (d[i] > id1 && d[i] < id2) return 0;
+  return 1. / p;
+}
+
 /* applications/ThreeChain.cpp:315-330 */
 static double prog_three_chain(zgo_ctx* c) {
   zgo_sub sg; sub_init(&sg);
@@ -613,6 +666,7 @@ static uint32_t prog_den_log2(const zgo_program* p) {
   switch (p->kind) {
     case ZG_PROG_TRIANGLE: return 1;
     case ZG_PROG_FOUR_CLIQUE: return 2;
+    case ZG_PROG_FOUR_CLIQUE_UNBIASED: return 2;
     case ZG_PROG_THREE_CHAIN: return 1;
     case ZG_PROG_FOUR_CHAIN: return 2;
     case ZG_PROG_CHAIN: return p->param - 2;
@@ -652,6 +706,7 @@ int zgo_sample(const zgo_graph* g, const zgo_program* p, uint64_t seed, uint32_t
   switch (p->kind) {
     case ZG_PROG_TRIANGLE: r = prog_triangle(&c); break;
     case ZG_PROG_FOUR_CLIQUE: r = prog_four_clique(&c); break;
+    case ZG_PROG_FOUR_CLIQUE_UNBIASED: r = prog_four_clique_unbiased(&c); break;
     case ZG_PROG_THREE_CHAIN: r = prog_three_chain(&c); break;
     case ZG_PROG_FOUR_CHAIN: r = prog_four_chain(&c); break;
     case ZG_PROG_CHAIN: r = prog_chain(&c, (int)p->param); break;

@@ -72,7 +72,7 @@ static uint32_t pair_bit_host(uint32_t i, uint32_t j, uint32_t pv) {
 
 extern "C" int zg_program_create(int kind, uint32_t param, zg_program** out) {
   if (!out) return zg_set_error(ZG_ERR_INVALID_ARG, "null output"), ZG_ERR_INVALID_ARG;
-  if (kind < ZG_PROG_TRIANGLE || kind > ZG_PROG_CHAIN)
+  if ((kind < ZG_PROG_TRIANGLE || kind > ZG_PROG_CHAIN) && kind != ZG_PROG_FOUR_CLIQUE_UNBIASED)
     return zg_set_error(ZG_ERR_UNSUPPORTED_ESTIMATOR, "unknown program kind %d", kind), ZG_ERR_UNSUPPORTED_ESTIMATOR;
   if (kind == ZG_PROG_CHAIN && (param < 3 || param > ZG_MAX_LIST))
     return zg_set_error(ZG_ERR_INVALID_ARG, "chain order %u outside [3, %d]", param, ZG_MAX_LIST),
@@ -136,7 +136,8 @@ extern "C" int zg_program_info(const zg_program* p, uint32_t* num_unique, uint32
   uint32_t cc = 0, vv = 0;
   switch (p->kind) {
     case ZG_PROG_TRIANGLE: cc = 1; vv = 3; break;
-    case ZG_PROG_FOUR_CLIQUE: cc = 2; vv = 4; break;
+    case ZG_PROG_FOUR_CLIQUE:
+    case ZG_PROG_FOUR_CLIQUE_UNBIASED: cc = 2; vv = 4; break;
     case ZG_PROG_THREE_CHAIN: cc = 1; vv = 3; break;
     case ZG_PROG_FOUR_CHAIN: cc = 2; vv = 4; break;
     case ZG_PROG_CHAIN: cc = p->param - 2; vv = p->param; break;

@@ -109,6 +109,7 @@ __device__ __forceinline__ void batch_item(const BatchQuery& sq, uint32_t chunk,
       switch (sq.pp.kind) {
         case ZG_PROG_TRIANGLE: prog_triangle<false>(sq.g, c, r); break;
         case ZG_PROG_FOUR_CLIQUE: prog_four_clique<false>(sq.g, c, r); break;
+        case ZG_PROG_FOUR_CLIQUE_UNBIASED: prog_four_clique<false, true>(sq.g, c, r); break;
         case ZG_PROG_THREE_CHAIN: prog_three_chain<false>(sq.g, c, r); break;
         case ZG_PROG_FOUR_CHAIN: prog_four_chain<false>(sq.g, c, r); break;
         default: prog_chain<false>(sq.g, (int)sq.pp.param, c, r); break;  // ZG_PROG_CHAIN
@@ -234,6 +235,7 @@ uint32_t den_of(int kind, uint32_t param, const zg_program* prog) {
   switch (kind) {
     case ZG_PROG_TRIANGLE: return 1;
     case ZG_PROG_FOUR_CLIQUE: return 2;
+    case ZG_PROG_FOUR_CLIQUE_UNBIASED: return 2;
     case ZG_PROG_THREE_CHAIN: return 1;
     case ZG_PROG_FOUR_CHAIN: return 2;
     case ZG_PROG_CHAIN: return param - 2;
@@ -478,7 +480,7 @@ extern "C" int zg_batch_submit(zg_batch* b, const zg_batch_query* q, uint32_t nq
   for (uint32_t i = 0; i < nq; ++i) {
     const zg_batch_query& x = q[i];
     if (x.n == 0) return zg_set_error(ZG_ERR_INVALID_ARG, "query %u: zero estimators", i), ZG_ERR_INVALID_ARG;
-    bool builtin = x.kind >= ZG_PROG_TRIANGLE && x.kind <= ZG_PROG_CHAIN;
+    bool builtin = (x.kind >= ZG_PROG_TRIANGLE && x.kind <= ZG_PROG_CHAIN) || x.kind == ZG_PROG_FOUR_CLIQUE_UNBIASED;
     bool pattern = x.kind == ZG_PROG_PATTERN && x.program && x.program->kind == ZG_PROG_PATTERN;
     if (!builtin && !pattern && x.kind != ZG_QUERY_THREE_MOTIF)
       return zg_set_error(ZG_ERR_UNSUPPORTED_ESTIMATOR, "query %u: kind %d%s", i, x.kind,
@@ -490,7 +492,8 @@ extern "C" int zg_batch_submit(zg_batch* b, const zg_batch_query* q, uint32_t nq
   int rc = ZG_OK;
   for (uint32_t i = 0; i < nq && rc == ZG_OK; ++i) {
     const zg_batch_query& x = q[i];
-    if (x.kind >= ZG_PROG_TRIANGLE && x.kind <= ZG_PROG_CHAIN) rc = zg_program_create(x.kind, x.param, &own[i]);
+    if ((x.kind >= ZG_PROG_TRIANGLE && x.kind <= ZG_PROG_CHAIN) || x.kind == ZG_PROG_FOUR_CLIQUE_UNBIASED)
+      rc = zg_program_create(x.kind, x.param, &own[i]);
     if (rc == ZG_OK) {
       if (x.pred_op) rc = batch_filtered(b, x.pred_op, x.t0, x.t1, s, graphs, &graphs[i]);
       else graphs[i] = b->base;

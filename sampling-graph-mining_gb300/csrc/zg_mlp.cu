@@ -447,7 +447,8 @@ __global__ void k_deg_stats(ZgDevGraph g, DegStats* __restrict__ out) {
 int pattern_slot(const zg_program* p) {
   switch (p->kind) {
     case ZG_PROG_TRIANGLE: return 0;
-    case ZG_PROG_FOUR_CLIQUE: return 1;
+    case ZG_PROG_FOUR_CLIQUE:
+    case ZG_PROG_FOUR_CLIQUE_UNBIASED: return 1;
     case ZG_PROG_THREE_CHAIN: return 2;
     case ZG_PROG_FOUR_CHAIN:
     case ZG_PROG_CHAIN: return 3;

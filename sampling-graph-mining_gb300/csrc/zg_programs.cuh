@@ -356,10 +356,60 @@ __device__ void prog_three_chain(const ZgDevGraph& g, Ctx& c, Res& r) {
   }
 }
 
+// ---- the canonical-path test of the unbiased 4-clique program (no counterpart in the reference)
+// Vertices by slot: 0 = a, 1 = b (e0's ends), 2 = c (e1's new end, e1 hangs off slot s1), 3 = d
+// (e2's new end, e2 hangs off slot s2).  The three unsampled pairs must be edges (any id; looked
+// up in the order (the other of a and b, c), then the two pairs at d in slot order, up to the first
+// missing one, the debug access model counting each look-up), and the sample must be the clique's
+// canonical path: id0 the smallest of the six ids, id1 the
+// smallest of the four edges joining {a, b} to {c, d}, id2 the smallest id above id1 at d.
+template <bool DBG>
+__device__ __forceinline__ bool canonical_four_clique(const ZgDevGraph& g, Ctx& c, uint32_t va, uint32_t vb,
+                                                      uint32_t vc, uint32_t vd, int s1, int s2, uint32_t id0,
+                                                      uint32_t id1, uint32_t id2) {
+  auto vslot = [&](int i) { return i == 0 ? va : i == 1 ? vb : i == 2 ? vc : vd; };
+  // the unsampled pairs in slot order: (1 - s1, 2), then the two (x, 3) with x != s2
+  const int x0 = 1 - s1, x1 = s2 == 0 ? 1 : 0, x2 = s2 == 2 ? 1 : 2;
+  int64_t h0, h1 = -1, h2 = -1;
+  if (DBG) {
+    h0 = edge_confirm(g, edge_candidate(g, vslot(x0), vc));
+    c.sectors += model_close(g, vslot(x0), vc);
+    if (h0 >= 0) {
+      h1 = edge_confirm(g, edge_candidate(g, vslot(x1), vd));
+      c.sectors += model_close(g, vslot(x1), vd);
+    }
+    if (h0 >= 0 && h1 >= 0) {
+      h2 = edge_confirm(g, edge_candidate(g, vslot(x2), vd));
+      c.sectors += model_close(g, vslot(x2), vd);
+    }
+  } else {
+    EdgeProbe p0 = edge_candidate(g, vslot(x0), vc);
+    if (p0.cand == ZG_HASH_EMPTY) return false;
+    EdgeProbe p1 = edge_candidate(g, vslot(x1), vd), p2 = edge_candidate(g, vslot(x2), vd);
+    if (p1.cand == ZG_HASH_EMPTY || p2.cand == ZG_HASH_EMPTY) return false;
+    h0 = edge_confirm(g, p0);
+    h1 = edge_confirm(g, p1);
+    h2 = edge_confirm(g, p2);
+  }
+  if (h0 < 0 || h1 < 0 || h2 < 0) return false;
+  const uint32_t i_c = (uint32_t)h0, i_x1 = (uint32_t)h1, i_x2 = (uint32_t)h2;
+  // ids of the pairs at d by slot: the sampled one (s2) and the two looked up
+  const uint32_t d0 = s2 == 0 ? id2 : (x1 == 0 ? i_x1 : i_x2);
+  const uint32_t d1 = s2 == 1 ? id2 : (x1 == 1 ? i_x1 : i_x2);
+  const uint32_t d2 = s2 == 2 ? id2 : (x1 == 2 ? i_x1 : i_x2);
+  // (i) e0 is the smallest (e1, e2 are larger by construction)
+  if (i_c < id0 || i_x1 < id0 || i_x2 < id0) return false;
+  // (ii) e1 is the smallest of {a, b} x {c, d}: the other {a, b}-c edge and both {a, b}-d edges
+  if (i_c < id1 || d0 < id1 || d1 < id1) return false;
+  // (iii) no edge at d with an id strictly between id1 and id2
+  if ((d0 > id1 && d0 < id2) || (d1 > id1 && d1 < id2) || (d2 > id1 && d2 < id2)) return false;
+  return true;
+}
+
 // ---- FourClique: applications/FourClique.cpp:176-234 -------------------------------------
 // Vertices in insertion order a (e0.src), b (e0.dst), c (e1's new end), d (e2's new end); all
 // state in scalars (no dynamically indexed arrays, which would live in local memory).
-template <bool DBG>
+template <bool DBG, bool UNBIASED = false>
 __device__ void prog_four_clique(const ZgDevGraph& g, Ctx& c, Res& r) {
   if (g.m == 0) {
     r.fail = true;
@@ -426,40 +476,44 @@ __device__ void prog_four_clique(const ZgDevGraph& g, Ctx& c, Res& r) {
   res_mul(r, S2);
   if (a2 == 2) r.shift++;
   if (a1 != 1 || dup) return;  // three vertices: a triangle was sampled (FourClique.cpp:224-226)
-  // closure: the 3 vertex pairs not sampled, all with edge id >= id2 + 1.  Sampled pairs are
-  // (a,b), (anchor of e1, c) and (anchor of e2, d).  The reference checks the pairs in slot order
-  // up to the first miss (the debug access model follows that).
-  const int s1 = s1b ? 1 : 0;
-  uint32_t mv2 = e2.y + 1;
-  auto vslot = [&](int i) { return i == 0 ? va : i == 1 ? vb : i == 2 ? vc : vd; };
-  bool ok = true;
-  if (DBG) {
-    for (int i = 0; i < 4; ++i)
-      for (int j = i + 1; j < 4; ++j) {
-        bool sampled = (i == 0 && j == 1) || (i == s1 && j == 2) || (i == s2 && j == 3);
-        if (!sampled && ok) {
-          ok = edge_after(g, vslot(i), vslot(j), mv2);
-          c.sectors += model_close(g, vslot(i), vslot(j));
-        }
-      }
+  if (UNBIASED) {
+    r.hit = canonical_four_clique<DBG>(g, c, va, vb, vc, vd, s1b ? 1 : 0, s2, (uint32_t)e0, e1.y, e2.y);
   } else {
-    uint32_t x0 = s1b ? va : vb;             // the pair (not-anchor-of-e1, c)
-    uint32_t x1 = vslot(s2 == 0 ? 1 : 0);    // the two pairs (?, d) other than e2's own
-    uint32_t x2 = vslot(s2 == 2 ? 1 : 2);
-    // the pair closing the first two edges fails most often: look it up first, the other two
-    // only when it exists
-    EdgeProbe p0 = edge_candidate(g, x0, vc);
-    ok = p0.cand != ZG_HASH_EMPTY;
-    if (ok) {
-      EdgeProbe p1 = edge_candidate(g, x1, vd), p2 = edge_candidate(g, x2, vd);
-      ok = p1.cand != ZG_HASH_EMPTY && p2.cand != ZG_HASH_EMPTY;
-      if (ok)
-        ok = edge_confirm(g, p0) >= (int64_t)mv2 && edge_confirm(g, p1) >= (int64_t)mv2 &&
-             edge_confirm(g, p2) >= (int64_t)mv2;
+    // closure: the 3 vertex pairs not sampled, all with edge id >= id2 + 1.  Sampled pairs are
+    // (a,b), (anchor of e1, c) and (anchor of e2, d).  The reference checks the pairs in slot order
+    // up to the first miss (the debug access model follows that).
+    const int s1 = s1b ? 1 : 0;
+    uint32_t mv2 = e2.y + 1;
+    auto vslot = [&](int i) { return i == 0 ? va : i == 1 ? vb : i == 2 ? vc : vd; };
+    bool ok = true;
+    if (DBG) {
+      for (int i = 0; i < 4; ++i)
+        for (int j = i + 1; j < 4; ++j) {
+          bool sampled = (i == 0 && j == 1) || (i == s1 && j == 2) || (i == s2 && j == 3);
+          if (!sampled && ok) {
+            ok = edge_after(g, vslot(i), vslot(j), mv2);
+            c.sectors += model_close(g, vslot(i), vslot(j));
+          }
+        }
+    } else {
+      uint32_t x0 = s1b ? va : vb;             // the pair (not-anchor-of-e1, c)
+      uint32_t x1 = vslot(s2 == 0 ? 1 : 0);    // the two pairs (?, d) other than e2's own
+      uint32_t x2 = vslot(s2 == 2 ? 1 : 2);
+      // the pair closing the first two edges fails most often: look it up first, the other two
+      // only when it exists
+      EdgeProbe p0 = edge_candidate(g, x0, vc);
+      ok = p0.cand != ZG_HASH_EMPTY;
+      if (ok) {
+        EdgeProbe p1 = edge_candidate(g, x1, vd), p2 = edge_candidate(g, x2, vd);
+        ok = p1.cand != ZG_HASH_EMPTY && p2.cand != ZG_HASH_EMPTY;
+        if (ok)
+          ok = edge_confirm(g, p0) >= (int64_t)mv2 && edge_confirm(g, p1) >= (int64_t)mv2 &&
+               edge_confirm(g, p2) >= (int64_t)mv2;
+      }
     }
+    r.hit = ok;
   }
-  r.hit = ok;
-  if (DBG && ok) {
+  if (DBG && r.hit) {
     double p = 1.0;
     p = dmul(p, ddiv(1.0, u2d(g.m)));
     p = dmul(p, ddiv(1.0 * a1, u2d(S1)));

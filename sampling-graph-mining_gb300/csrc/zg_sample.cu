@@ -20,6 +20,7 @@ __device__ __forceinline__ void run_program(const ZgDevGraph& g, const ZgProgPar
   switch (pp.kind) {
     case ZG_PROG_TRIANGLE: prog_triangle<DBG>(g, c, r); break;
     case ZG_PROG_FOUR_CLIQUE: prog_four_clique<DBG>(g, c, r); break;
+    case ZG_PROG_FOUR_CLIQUE_UNBIASED: prog_four_clique<DBG, true>(g, c, r); break;
     case ZG_PROG_THREE_CHAIN: prog_three_chain<DBG>(g, c, r); break;
     case ZG_PROG_FOUR_CHAIN: prog_four_chain<DBG>(g, c, r); break;
     case ZG_PROG_CHAIN: prog_chain<DBG>(g, (int)pp.param, c, r); break;
@@ -41,6 +42,7 @@ __global__ void __launch_bounds__(kBlock, MINB) k_sample(ZgDevGraph g, ZgProgPar
     res_init(r);
     if (KIND == ZG_PROG_TRIANGLE) prog_triangle<false>(g, c, r);
     else if (KIND == ZG_PROG_FOUR_CLIQUE) prog_four_clique<false>(g, c, r);
+    else if (KIND == ZG_PROG_FOUR_CLIQUE_UNBIASED) prog_four_clique<false, true>(g, c, r);
     else if (KIND == ZG_PROG_THREE_CHAIN) prog_three_chain<false>(g, c, r);
     else if (KIND == ZG_PROG_FOUR_CHAIN) prog_four_chain<false>(g, c, r);
     else if (KIND == ZG_PROG_CHAIN) prog_chain<false>(g, (int)pp.param, c, r);
@@ -326,6 +328,7 @@ uint32_t den_for(const zg_program* p) {
   switch (p->kind) {
     case ZG_PROG_TRIANGLE: return 1;
     case ZG_PROG_FOUR_CLIQUE: return 2;
+    case ZG_PROG_FOUR_CLIQUE_UNBIASED: return 2;
     case ZG_PROG_THREE_CHAIN: return 1;
     case ZG_PROG_FOUR_CHAIN: return 2;
     case ZG_PROG_CHAIN: return p->param - 2;
@@ -374,6 +377,7 @@ SampleKernel kernel_for(int kind, int v) {
   switch (kind) {
     case ZG_PROG_TRIANGLE: return kernel_variant<ZG_PROG_TRIANGLE>(v);
     case ZG_PROG_FOUR_CLIQUE: return kernel_variant<ZG_PROG_FOUR_CLIQUE>(v);
+    case ZG_PROG_FOUR_CLIQUE_UNBIASED: return kernel_variant<ZG_PROG_FOUR_CLIQUE_UNBIASED>(v);
     case ZG_PROG_THREE_CHAIN: return kernel_variant<ZG_PROG_THREE_CHAIN>(v);
     case ZG_PROG_FOUR_CHAIN: return kernel_variant<ZG_PROG_FOUR_CHAIN>(v);
     case ZG_PROG_CHAIN: return kernel_variant<ZG_PROG_CHAIN>(v);
@@ -519,7 +523,7 @@ extern "C" int zg_run_async(const zg_graph* g, const zg_program* p, uint64_t n, 
 extern "C" int zg_set_variant(int kind, int variant) {
   if (variant < 0 || variant >= kVariants)
     return zg_set_error(ZG_ERR_INVALID_ARG, "launch variant %d outside [0, %d)", variant, kVariants), ZG_ERR_INVALID_ARG;
-  if (kind < ZG_PROG_TRIANGLE || kind > ZG_PROG_PATTERN)
+  if (kind < ZG_PROG_TRIANGLE || kind > ZG_PROG_FOUR_CLIQUE_UNBIASED)
     return zg_set_error(ZG_ERR_INVALID_ARG, "unknown program kind %d", kind), ZG_ERR_INVALID_ARG;
   variant_for(kind);  // initialise the table
   int d = current_device();
@@ -529,7 +533,7 @@ extern "C" int zg_set_variant(int kind, int variant) {
 }
 
 extern "C" int zg_get_variant(int kind, int* variant, int* min_blocks, int* grid) {
-  if (kind < ZG_PROG_TRIANGLE || kind > ZG_PROG_PATTERN)
+  if (kind < ZG_PROG_TRIANGLE || kind > ZG_PROG_FOUR_CLIQUE_UNBIASED)
     return zg_set_error(ZG_ERR_INVALID_ARG, "unknown program kind %d", kind), ZG_ERR_INVALID_ARG;
   int v = variant_for(kind);
   if (variant) *variant = v;

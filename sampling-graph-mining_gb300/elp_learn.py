@@ -34,6 +34,7 @@ PATTERNS = {
     "four_chain": (Z.PROG_FOUR_CHAIN, 0, None),
     "star5": (Z.PROG_PATTERN, 0, STAR),
     "house5": (Z.PROG_PATTERN, 0, HOUSE),
+    "four_clique_unbiased": (Z.PROG_FOUR_CLIQUE_UNBIASED, 0, None),
 }
 
 

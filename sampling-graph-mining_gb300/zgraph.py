@@ -29,6 +29,7 @@ ERRORS = {1: "INVALID_ARG", 2: "OOM", 3: "CUDA", 4: "INVALID_GRAPH", 5: "UNSUPPO
           6: "TIMEOUT", 7: "BOUND_NOT_MET", 8: "NO_DEVICE", 9: "OVERFLOW", 10: "TOO_LARGE"}
 
 PROG_TRIANGLE, PROG_FOUR_CLIQUE, PROG_THREE_CHAIN, PROG_FOUR_CHAIN, PROG_CHAIN, PROG_PATTERN = 1, 2, 3, 4, 5, 6
+PROG_FOUR_CLIQUE_UNBIASED = 7  # canonical-path 4-clique estimator (no counterpart in the reference)
 EXACT_TRIANGLE, EXACT_WEDGE, EXACT_THREE_PATH, EXACT_FIVE_STAR, EXACT_FOUR_CLIQUE = 1, 2, 3, 4, 5
 PRED_GE, PRED_LT, PRED_GT, PRED_LE, PRED_EQ, PRED_NE, PRED_RANGE = 1, 2, 3, 4, 5, 6, 7
 QUERY_THREE_MOTIF = 16

@@ -36,6 +36,7 @@ PROGRAMS = [
     ("cycle4", Z.PROG_PATTERN, 0, CYCLE4),
     ("chain5_pattern", Z.PROG_PATTERN, 0, CHAIN5),
     ("clique4_pattern", Z.PROG_PATTERN, 0, CLIQUE4),
+    ("four_clique_unbiased", Z.PROG_FOUR_CLIQUE_UNBIASED, 0, None),
 ]
 
 
@@ -264,3 +265,24 @@ def test_launch_variants_agree(graphs, name, kind, param, pattern):
     best, ms = p.tune(g, 1 << 18)
     assert 0 <= best < 6 and all(t > 0 for t in ms)
     assert p.variant()["variant"] == best
+
+
+def test_unbiased_four_clique_counters_and_accuracy():
+    """The canonical-path 4-clique program: exact sums equal the oracle's, and its estimate lands
+    within 4 standard errors of the exact count where the reference's program is biased low."""
+    import math
+    e = Z.gen_rmat(11, 16, seed=12)
+    g = Z.Graph.from_edges(e, 1 << 11)
+    og = O.OracleGraph(e, 1 << 11)
+    n = 1 << 20
+    c = Z.Program(Z.PROG_FOUR_CLIQUE_UNBIASED).run(g, n, 17)
+    oc = O.run(og, O.OracleProgram(Z.PROG_FOUR_CLIQUE_UNBIASED), n, 17)
+    assert (c.hits, c.fails) == (oc.hits, oc.fails)
+    assert [int(x) for x in c.sum_num] == [int(x) for x in oc.sum_num]
+    ex = g.exact_count(Z.EXACT_FOUR_CLIQUE)
+    big = Z.Program(Z.PROG_FOUR_CLIQUE_UNBIASED).run(g, 1 << 28, 3)
+    se = math.sqrt(max(big.sum_w2 / big.samples - big.estimate ** 2, 0) / big.samples)
+    assert abs(big.estimate - ex) < 4 * se, (big.estimate, ex, se)
+    assert se < 0.01 * ex
+    ref = Z.Program(Z.PROG_FOUR_CLIQUE).run(g, 1 << 28, 3)
+    assert ref.estimate < 0.8 * ex  # the reference's estimator misses the non-canonical cliques
