@@ -384,6 +384,12 @@ int zg_mlp_predict(const zg_mlp* net, const float* X, uint32_t n_rows, float* Y)
 int zg_graph_features(const zg_graph* g, const zg_program* p, uint64_t pilot_samples,
                       uint64_t seed, void* cuda_stream, float* features);
 
+/* ---- measurement ------------------------------------------------------------ */
+/* Read bandwidth (GB/s) of a device buffer of `bytes` read `reps` times by one persistent grid,
+ * timed with CUDA events: below the 129 MB L2 it measures L2, well above it HBM.  The L2 view of
+ * the roofline for graphs that nearly fit in L2 (no counterpart in the reference). */
+int zg_read_bandwidth(uint64_t bytes, uint32_t reps, void* cuda_stream, double* gbs);
+
 /* ---- exact counts ---------------------------------------------------------- */
 /* out[0..1]: 128-bit little-endian count.  kind: ZG_EXACT_*. */
 int zg_exact_count(const zg_graph* g, int kind, void* cuda_stream, uint64_t out[2]);

@@ -148,3 +148,54 @@ extern "C" int zg_program_info(const zg_program* p, uint32_t* num_unique, uint32
   if (vertices) *vertices = vv;
   return ZG_OK;
 }
+
+// ---- bandwidth probe: the L2 view of the roofline ------------------------------------------
+namespace {
+__global__ void k_read_probe(const uint4* __restrict__ buf, uint64_t n16, uint32_t reps, uint4* __restrict__ sink) {
+  uint4 acc = make_uint4(0, 0, 0, 0);
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint32_t r = 0; r < reps; ++r)
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n16; i += stride) {
+      uint4 v = __ldcg(&buf[i]);  // cached in L2 only
+      acc.x ^= v.x;
+      acc.y ^= v.y;
+      acc.z ^= v.z;
+      acc.w ^= v.w;
+    }
+  if ((acc.x ^ acc.y ^ acc.z ^ acc.w) == 0x9E3779B9u) sink[threadIdx.x] = acc;  // keeps the loads live
+}
+}  // namespace
+
+// Read bandwidth of a device buffer of `bytes` read `reps` times by one persistent grid (CUDA
+// events): a buffer well below the 129 MB L2 measures L2 bandwidth, one well above it HBM.
+extern "C" int zg_read_bandwidth(uint64_t bytes, uint32_t reps, void* cuda_stream, double* gbs) {
+  if (!gbs || bytes < 16 || reps == 0) return zg_set_error(ZG_ERR_INVALID_ARG, "zg_read_bandwidth: bad argument"), ZG_ERR_INVALID_ARG;
+  cudaStream_t s = (cudaStream_t)cuda_stream;
+  uint64_t n16 = bytes / 16;
+  uint4 *buf = nullptr, *sink = nullptr;
+  cudaError_t e;
+  if ((e = cudaMalloc(&buf, n16 * 16)) || (e = cudaMalloc(&sink, 256 * 16))) {
+    if (buf) cudaFree(buf);
+    cudaGetLastError();
+    return zg_set_error(ZG_ERR_OOM, "zg_read_bandwidth: %s", cudaGetErrorString(e)), ZG_ERR_OOM;
+  }
+  cudaMemsetAsync(buf, 1, n16 * 16, s);
+  int grid = 4 * zg_num_sms();
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  k_read_probe<<<grid, 256, 0, s>>>(buf, n16, 1, sink);  // warm the cache
+  cudaEventRecord(e0, s);
+  k_read_probe<<<grid, 256, 0, s>>>(buf, n16, reps, sink);
+  cudaEventRecord(e1, s);
+  e = cudaEventSynchronize(e1);
+  float ms = 0;
+  if (e == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(buf);
+  cudaFree(sink);
+  if (e != cudaSuccess) return zg_check_cuda(e, "zg_read_bandwidth");
+  *gbs = ms > 0 ? (double)n16 * 16 * reps / (ms / 1000.0) / 1e9 : 0.0;
+  return ZG_OK;
+}

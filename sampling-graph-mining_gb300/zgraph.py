@@ -163,6 +163,7 @@ def lib():
             "zg_batch_filtered_graph": ([P, I32, I64, I64, P, C.POINTER(P)], I32),
             "zg_batch_tune": ([P, P, U32, P, C.POINTER(I32), P], I32),
             "zg_batch_elapsed_ms": ([P, C.POINTER(C.c_float)], I32),
+            "zg_read_bandwidth": ([U64, U32, P, C.POINTER(D)], I32),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -353,6 +354,14 @@ class Graph:
             self.free()
         except Exception:
             pass
+
+
+def read_bandwidth(nbytes, reps=200, cuda_stream=None):
+    """zg_read_bandwidth: GB/s of repeated reads of an nbytes device buffer (L2 below 129 MB)."""
+    init()
+    out = C.c_double(0)
+    check(lib().zg_read_bandwidth(nbytes, reps, cuda_stream, C.byref(out)))
+    return out.value
 
 
 # ---- batched mixed queries ----------------------------------------------------------------
