@@ -535,91 +535,65 @@ __device__ void prog_four_chain(const ZgDevGraph& g, Ctx& c, Res& r) {
   uint64_t e0 = c.draw(0, g.m - 1);
   res_mul(r, g.m);
   uint4 q = ZG_LDG(&g.rec[e0]);
-  uint32_t a = q.x, b = q.y;
-  uint64_t S1, S2;
-  uint32_t a1 = 1, a2 = 1;
-  bool ok;
+  const uint32_t a = q.x, b = q.y;
   if (DBG) c.sectors += 1;
-  if (sel != 3) {
-    // edges [e0], vertices [a, b]
-    S1 = (uint64_t)q.z + q.w;
-    if (DBG) c.sectors += model_anchor(g, a) + model_anchor(g, b);
-    if (S1 == 0) {
-      r.fail = true;
-      return;
-    }
-    if (DBG) c.sectors += 1;
-    uint64_t r1 = c.take(w2, 0, S1 - 1);
-    uint32_t anchor = a, suf = q.z;
-    if (r1 >= q.z) {
-      r1 -= q.z;
-      anchor = b;
-      suf = q.w;
-    }
-    uint32_t idx1 = ZG_LDG(&g.off32[anchor + 1]) - (uint32_t)suf + (uint32_t)r1;
-    uint2 e1 = ZG_LDG(&g.adj_e[idx1]);
-    a1 = 1 + (e1.x == a || e1.x == b);
-    res_mul(r, S1);
-    if (a1 == 2) r.shift++;
-    // the vertex of e1 not shared with e0 (FourChain.cpp:44-54)
-    uint32_t nw;
-    if (a == anchor) nw = e1.x;
-    else if (a == e1.x) nw = anchor;
-    else if (b == anchor) nw = e1.x;
-    else nw = anchor;
-    uint4 q1 = ZG_LDG(&g.rec[e1.y]);
-    uint32_t sufn = (q1.x == nw) ? q1.z : q1.w;  // entries after e1 in nw's list
-    uint32_t endn = ZG_LDG(&g.off32[nw + 1]);
-    uint32_t lbn;
-    if (sel == 1) {
-      // edges [e0, e1]: min_valid = id1 + 1
-      lbn = endn - (uint32_t)sufn;
-    } else {
-      // edges [e0]: min_valid = id0 + 1, at or before e1's own slot in nw's list
-      uint32_t pos1 = endn - (uint32_t)sufn - 1;
-      lbn = lb_eid(g.adj_e, ZG_LDG(&g.off32[nw]), pos1 + 1, (uint32_t)e0 + 1, 0u, e1.y);
-    }
-    S2 = (uint64_t)(endn - lbn);
-    if (DBG) c.sectors += model_anchor(g, nw);
-    if (S2 == 0) {
-      r.fail = true;
-      return;
-    }
-    if (DBG) c.sectors += 1;
-    uint64_t r2 = c.take(w3, 0, S2 - 1);
-    uint2 e2 = ZG_LDG(&g.adj_e[lbn + (uint32_t)r2]);
-    a2 = 1 + (e2.x == nw);
-    res_mul(r, S2);
-    if (a2 == 2) r.shift++;
-    ok = !(nw == a || nw == b) && !(e2.x == a || e2.x == b);
-    if (sel == 2) ok = ok && !(e2.y >= e1.y);
-  } else {
-    // vertices [a]: e1 from a's list; then vertices [b]: e2 from b's list; edges [e0]
-    S1 = q.z;
-    if (DBG) c.sectors += model_anchor(g, a);
-    if (S1 == 0) {
-      r.fail = true;
-      return;
-    }
-    if (DBG) c.sectors += 1;
-    uint64_t r1 = c.take(w2, 0, S1 - 1);
-    uint2 e1 = ZG_LDG(&g.adj_e[ZG_LDG(&g.off32[a + 1]) - (uint32_t)q.z + (uint32_t)r1]);
-    a1 = 1 + (e1.x == a);
-    res_mul(r, S1);
-    if (a1 == 2) r.shift++;
-    S2 = q.w;
-    if (DBG) c.sectors += model_anchor(g, b);
-    if (S2 == 0) {
-      r.fail = true;
-      return;
-    }
-    if (DBG) c.sectors += 1;
-    uint64_t r2 = c.take(w3, 0, S2 - 1);
-    uint2 e2 = ZG_LDG(&g.adj_e[ZG_LDG(&g.off32[b + 1]) - (uint32_t)q.w + (uint32_t)r2]);
-    a2 = 1 + (e2.x == b);
-    res_mul(r, S2);
-    if (a2 == 2) r.shift++;
+  // The three programs share one chain of dependent loads (edge record, anchor offset, e1,
+  // second anchor's offset, e2) so a warp whose lanes drew different programs walks it once.
+  //   sel 1, 2: vertices [a, b] give e1; its far end nw gives e2 (edges [e0, e1] resp. [e0])
+  //   sel 3:    vertices [a] give e1; vertices [b] give e2 (edges [e0])
+  const bool split = sel == 3;
+  const uint64_t S1 = split ? (uint64_t)q.z : (uint64_t)q.z + q.w;
+  if (DBG) c.sectors += model_anchor(g, a) + (split ? 0 : model_anchor(g, b));
+  if (S1 == 0) {
+    r.fail = true;
+    return;
+  }
+  if (DBG) c.sectors += 1;
+  uint64_t r1 = c.take(w2, 0, S1 - 1);
+  uint32_t anchor = a, suf = q.z;
+  if (!split && r1 >= q.z) {
+    r1 -= q.z;
+    anchor = b;
+    suf = q.w;
+  }
+  const uint2 e1 = ZG_LDG(&g.adj_e[ZG_LDG(&g.off32[anchor + 1]) - suf + (uint32_t)r1]);
+  const uint32_t a1 = 1 + (e1.x == a || (!split && e1.x == b));
+  res_mul(r, S1);
+  if (a1 == 2) r.shift++;
+  // the second step's anchor: b, or the vertex of e1 not shared with e0 (FourChain.cpp:44-54)
+  uint32_t v2;
+  if (split) v2 = b;
+  else if (a == anchor) v2 = e1.x;
+  else if (a == e1.x) v2 = anchor;
+  else if (b == anchor) v2 = e1.x;
+  else v2 = anchor;
+  const uint32_t end2 = ZG_LDG(&g.off32[v2 + 1]);
+  uint32_t lb2 = end2 - q.w;  // sel 3: b's entries after e0
+  if (!split) {
+    const uint4 q1 = ZG_LDG(&g.rec[e1.y]);
+    const uint32_t suf1 = (q1.x == v2) ? q1.z : q1.w;  // entries after e1 in v2's list
+    lb2 = end2 - suf1;                                // sel 1: min_valid = id1 + 1
+    if (sel == 2)  // min_valid = id0 + 1, at or before e1's own slot in v2's list
+      lb2 = lb_eid(g.adj_e, ZG_LDG(&g.off32[v2]), lb2, (uint32_t)e0 + 1, 0u, e1.y);
+  }
+  const uint64_t S2 = (uint64_t)(end2 - lb2);
+  if (DBG) c.sectors += model_anchor(g, v2);
+  if (S2 == 0) {
+    r.fail = true;
+    return;
+  }
+  if (DBG) c.sectors += 1;
+  const uint64_t r2 = c.take(w3, 0, S2 - 1);
+  const uint2 e2 = ZG_LDG(&g.adj_e[lb2 + (uint32_t)r2]);
+  const uint32_t a2 = 1 + (e2.x == v2);
+  res_mul(r, S2);
+  if (a2 == 2) r.shift++;
+  bool ok;
+  if (split) {
     ok = !(b == a || b == e1.x) && !(e2.x == a || e2.x == e1.x);
+  } else {
+    ok = !(v2 == a || v2 == b) && !(e2.x == a || e2.x == b);
+    if (sel == 2) ok = ok && !(e2.y >= e1.y);
   }
   r.hit = ok;
   if (DBG && ok) {
