@@ -366,7 +366,7 @@ __device__ void prog_three_chain(const ZgDevGraph& g, Ctx& c, Res& r) {
 template <bool DBG>
 __device__ __forceinline__ bool canonical_four_clique(const ZgDevGraph& g, Ctx& c, uint32_t va, uint32_t vb,
                                                       uint32_t vc, uint32_t vd, int s1, int s2, uint32_t id0,
-                                                      uint32_t id1, uint32_t id2) {
+                                                      uint32_t id1, uint32_t id2, const EdgeProbe& pc) {
   auto vslot = [&](int i) { return i == 0 ? va : i == 1 ? vb : i == 2 ? vc : vd; };
   // the unsampled pairs in slot order: (1 - s1, 2), then the two (x, 3) with x != s2
   const int x0 = 1 - s1, x1 = s2 == 0 ? 1 : 0, x2 = s2 == 2 ? 1 : 2;
@@ -383,7 +383,7 @@ __device__ __forceinline__ bool canonical_four_clique(const ZgDevGraph& g, Ctx& 
       c.sectors += model_close(g, vslot(x2), vd);
     }
   } else {
-    EdgeProbe p0 = edge_candidate(g, vslot(x0), vc);
+    const EdgeProbe& p0 = pc;  // the caller's look-up of (slot x0, c)
     if (p0.cand == ZG_HASH_EMPTY) return false;
     EdgeProbe p1 = edge_candidate(g, vslot(x1), vd), p2 = edge_candidate(g, vslot(x2), vd);
     if (p1.cand == ZG_HASH_EMPTY || p2.cand == ZG_HASH_EMPTY) return false;
@@ -436,6 +436,18 @@ __device__ void prog_four_clique(const ZgDevGraph& g, Ctx& c, Res& r) {
   res_mul(r, g.m);
   res_mul(r, S1);
   if (a1 == 2) r.shift++;
+  // Every hit of either program is a 4-clique and so contains the pair (x0, c), x0 the end of e0
+  // that e1 does not hang off.  Its two buckets are read before the second step: when neither
+  // holds its fingerprint the pair is absent and the sample is a miss, unless the second step has
+  // no candidate at all (then it fails, as below).  With entries after e1 left in the anchor's own
+  // list that cannot happen, and the sample ends here; the counters are those of the full path.
+  const uint32_t x0 = s1b ? va : vb;
+  const uint32_t own = (s1b ? endB : endA) - (idx1 + 1);  // the anchor's entries after e1
+  EdgeProbe p0{0ull, ZG_HASH_EMPTY};
+  if (!DBG) {
+    p0 = edge_candidate(g, x0, vc);
+    if (p0.cand == ZG_HASH_EMPTY && own != 0) return;
+  }
   // second conditional step: anchors [a, b, c], min_valid = id1 + 1
   uint32_t mv = e1.y + 1;
   uint4 q1 = ZG_LDG(&g.rec[e1.y]);
@@ -455,6 +467,7 @@ __device__ void prog_four_clique(const ZgDevGraph& g, Ctx& c, Res& r) {
     r.fail = true;
     return;
   }
+  if (!DBG && p0.cand == ZG_HASH_EMPTY) return;  // (x0, c) absent: a miss
   if (DBG) c.sectors += 1;
   uint64_t r2 = c.take(w2, 0, S2 - 1);
   int s2;
@@ -477,7 +490,7 @@ __device__ void prog_four_clique(const ZgDevGraph& g, Ctx& c, Res& r) {
   if (a2 == 2) r.shift++;
   if (a1 != 1 || dup) return;  // three vertices: a triangle was sampled (FourClique.cpp:224-226)
   if (UNBIASED) {
-    r.hit = canonical_four_clique<DBG>(g, c, va, vb, vc, vd, s1b ? 1 : 0, s2, (uint32_t)e0, e1.y, e2.y);
+    r.hit = canonical_four_clique<DBG>(g, c, va, vb, vc, vd, s1b ? 1 : 0, s2, (uint32_t)e0, e1.y, e2.y, p0);
   } else {
     // closure: the 3 vertex pairs not sampled, all with edge id >= id2 + 1.  Sampled pairs are
     // (a,b), (anchor of e1, c) and (anchor of e2, d).  The reference checks the pairs in slot order
@@ -496,20 +509,14 @@ __device__ void prog_four_clique(const ZgDevGraph& g, Ctx& c, Res& r) {
           }
         }
     } else {
-      uint32_t x0 = s1b ? va : vb;             // the pair (not-anchor-of-e1, c)
-      uint32_t x1 = vslot(s2 == 0 ? 1 : 0);    // the two pairs (?, d) other than e2's own
+      // (x0, c) has a candidate (p0, read above); the two pairs (?, d) other than e2's own
+      uint32_t x1 = vslot(s2 == 0 ? 1 : 0);
       uint32_t x2 = vslot(s2 == 2 ? 1 : 2);
-      // the pair closing the first two edges fails most often: look it up first, the other two
-      // only when it exists
-      EdgeProbe p0 = edge_candidate(g, x0, vc);
-      ok = p0.cand != ZG_HASH_EMPTY;
-      if (ok) {
-        EdgeProbe p1 = edge_candidate(g, x1, vd), p2 = edge_candidate(g, x2, vd);
-        ok = p1.cand != ZG_HASH_EMPTY && p2.cand != ZG_HASH_EMPTY;
-        if (ok)
-          ok = edge_confirm(g, p0) >= (int64_t)mv2 && edge_confirm(g, p1) >= (int64_t)mv2 &&
-               edge_confirm(g, p2) >= (int64_t)mv2;
-      }
+      EdgeProbe p1 = edge_candidate(g, x1, vd), p2 = edge_candidate(g, x2, vd);
+      ok = p1.cand != ZG_HASH_EMPTY && p2.cand != ZG_HASH_EMPTY;
+      if (ok)
+        ok = edge_confirm(g, p0) >= (int64_t)mv2 && edge_confirm(g, p1) >= (int64_t)mv2 &&
+             edge_confirm(g, p2) >= (int64_t)mv2;
     }
     r.hit = ok;
   }
