@@ -36,7 +36,7 @@ int zg_num_sms() {
   return sms;
 }
 
-extern "C" int zg_version(void) { return 1; }
+extern "C" int zg_version(void) { return 2; }
 
 extern "C" const char* zg_last_error(void) { return g_err; }
 

@@ -56,24 +56,21 @@ __device__ __forceinline__ void motif_sample(const ZgDevGraph& g, Ctx& c, Res& r
     return;
   }
   uint64_t e0 = c.draw(0, g.m - 1);
-  uint4 q = ZG_LDG(&g.rec[e0]);
+  uint4 q, qp;
+  edge_rec(g, e0, q, qp);
   uint64_t S = (uint64_t)q.z + q.w;
   if (S == 0) {
     r.fail = true;
     return;
   }
   uint64_t r1 = c.draw(0, S - 1);
-  uint32_t anchor = q.x, other = q.y, suf = q.z;
-  if (r1 >= q.z) {
-    r1 -= q.z;
-    anchor = q.y;
-    other = q.x;
-    suf = q.w;
-  }
+  const bool on_y = r1 >= q.z;
+  if (on_y) r1 -= q.z;
+  const uint32_t other = on_y ? q.x : q.y, base = after_edge(g, q, qp, on_y);
   res_mul(r, g.m);
   res_mul(r, S);
   r.hit = true;
-  uint2 e1 = ZG_LDG(&g.adj_e[ZG_LDG(&g.off32[anchor + 1]) - (uint32_t)suf + (uint32_t)r1]);
+  uint2 e1 = ZG_LDG(&g.adj_e[base + (uint32_t)r1]);
   uint32_t a1 = 1 + (e1.x == q.x || e1.x == q.y);
   if (a1 == 2) r.shift = 1;
   rt.hit = a1 == 1 && edge_after(g, other, e1.x, e1.y + 1);

@@ -61,7 +61,7 @@ __device__ __forceinline__ bool lower(const ZgDevGraph& g, uint32_t a, uint32_t 
 
 __global__ void k_orient(ZgDevGraph g, unsigned long long* __restrict__ keys, unsigned long long* __restrict__ outdeg) {
   for (uint64_t e = blockIdx.x * (uint64_t)kB + threadIdx.x; e < g.m; e += (uint64_t)gridDim.x * kB) {
-    uint4 r = g.rec[e];
+    uint4 r = zg_rec_e(g, e);
     uint32_t a = r.x, b = r.y;
     if (!lower(g, a, b)) {
       uint32_t t = a;
@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(kB) k_degree_terms(ZgDevGraph g, int kind, U12
   uint64_t tid = blockIdx.x * (uint64_t)kB + threadIdx.x, stride = (uint64_t)gridDim.x * kB;
   if (kind == ZG_EXACT_THREE_PATH) {
     for (uint64_t e = tid; e < g.m; e += stride) {
-      uint4 r = g.rec[e];
+      uint4 r = zg_rec_e(g, e);
       add128w(acc, (unsigned __int128)(deg(g, r.x) - 1) * (deg(g, r.y) - 1));
     }
   } else {

@@ -73,7 +73,7 @@ int bits_for(uint64_t maxval) {
 // Validate the COO (src/Graph.cpp:454 asserts src != dst), count degrees, emit half-edges.
 __global__ void k_validate_count(const uint2* __restrict__ coo, uint64_t m, uint32_t nv,
                                  unsigned long long* __restrict__ deg, uint32_t* __restrict__ keys,
-                                 unsigned long long* __restrict__ vals, uint4* __restrict__ rec,
+                                 unsigned long long* __restrict__ vals, void* __restrict__ rec, uint32_t wide,
                                  unsigned int* __restrict__ bad) {
   for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < m;
        e += (uint64_t)gridDim.x * blockDim.x) {
@@ -88,24 +88,44 @@ __global__ void k_validate_count(const uint2* __restrict__ coo, uint64_t m, uint
     keys[2 * e + 1] = c.y;
     vals[2 * e] = (unsigned long long)c.y | ((unsigned long long)e << 32);
     vals[2 * e + 1] = (unsigned long long)c.x | ((unsigned long long)e << 32);
-    rec[e] = make_uint4(c.x, c.y, 0u, 0u);
+    if (wide) {
+      ((ZgRec*)rec)[e].e = make_uint4(c.x, c.y, 0u, 0u);
+      ((ZgRec*)rec)[e].p = make_uint4(0u, 0u, 0u, 0u);
+    } else {
+      ((uint4*)rec)[e] = make_uint4(c.x, c.y, 0u, 0u);
+    }
   }
 }
 
-// Suffix counts + (v:nbr) keys for the neighbour sort.
+// Per edge and endpoint: entries after it in the endpoint's list (wide records: also its own slot
+// and the entries before it); (v:nbr) keys for the neighbour sort.
 __global__ void k_suffix(const uint32_t* __restrict__ vkeys, const uint2* __restrict__ adj_e,
-                         uint64_t n2, const int64_t* __restrict__ off, uint4* __restrict__ rec,
+                         uint64_t n2, const int64_t* __restrict__ off, void* __restrict__ rec, uint32_t wide,
                          unsigned long long* __restrict__ nkeys, uint32_t* __restrict__ nvals) {
   for (uint64_t g = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; g < n2;
        g += (uint64_t)gridDim.x * blockDim.x) {
     uint32_t v = vkeys[g];
     uint2 a = adj_e[g];
     uint32_t suf = (uint32_t)(off[v + 1] - 1 - (int64_t)g);
-    uint4* r = &rec[a.y];
-    if (r->x == v)
-      r->z = suf;
-    else
-      r->w = suf;
+    if (wide) {
+      uint32_t pre = (uint32_t)((int64_t)g - off[v]);
+      ZgRec* r = &((ZgRec*)rec)[a.y];
+      if (r->e.x == v) {
+        r->e.z = suf;
+        r->p.x = (uint32_t)g;
+        r->p.z = pre;
+      } else {
+        r->e.w = suf;
+        r->p.y = (uint32_t)g;
+        r->p.w = pre;
+      }
+    } else {
+      uint4* r = &((uint4*)rec)[a.y];
+      if (r->x == v)
+        r->z = suf;
+      else
+        r->w = suf;
+    }
     if (nkeys) {
       nkeys[g] = ((unsigned long long)v << 32) | a.x;
       nvals[g] = a.y;
@@ -145,10 +165,10 @@ __device__ __forceinline__ bool cuckoo_try(unsigned long long* ent, uint32_t b, 
   return false;
 }
 
-__global__ void k_cuckoo_insert(const uint4* __restrict__ rec, uint64_t m, unsigned long long* ent, uint32_t bits,
+__global__ void k_cuckoo_insert(const ZgDevGraph d, uint64_t m, unsigned long long* ent, uint32_t bits,
                                 uint64_t seed, unsigned int* __restrict__ fail) {
   for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < m; e += (uint64_t)gridDim.x * blockDim.x) {
-    uint4 r = rec[e];
+    uint4 r = zg_rec_e(d, e);
     unsigned long long k = zg_edge_key(r.x, r.y);
     unsigned long long x = ((unsigned long long)zg_fingerprint(k, seed) << 32) | e;
     uint32_t from = 0xFFFFFFFFu;  // the bucket the carried entry was evicted from
@@ -166,7 +186,7 @@ __global__ void k_cuckoo_insert(const uint4* __restrict__ rec, uint64_t m, unsig
         break;
       }
       x = old;
-      uint4 ro = rec[(uint32_t)old];
+      uint4 ro = zg_rec_e(d, (uint32_t)old);
       k = zg_edge_key(ro.x, ro.y);
       from = vb;
     }
@@ -175,10 +195,10 @@ __global__ void k_cuckoo_insert(const uint4* __restrict__ rec, uint64_t m, unsig
 }
 
 // Every edge must be found in one of its two buckets (an insertion that gave up lost one).
-__global__ void k_cuckoo_check(const uint4* __restrict__ rec, uint64_t m, const unsigned long long* __restrict__ ent,
+__global__ void k_cuckoo_check(const ZgDevGraph d, uint64_t m, const unsigned long long* __restrict__ ent,
                                uint32_t bits, uint64_t seed, unsigned int* __restrict__ fail) {
   for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < m; e += (uint64_t)gridDim.x * blockDim.x) {
-    uint4 r = rec[e];
+    uint4 r = zg_rec_e(d, e);
     unsigned long long k = zg_edge_key(r.x, r.y);
     unsigned long long x = ((unsigned long long)zg_fingerprint(k, seed) << 32) | e;
     uint32_t bs[2] = {zg_bucket1(k, seed, bits), zg_bucket2(k, seed, bits)};
@@ -211,8 +231,8 @@ int build_hash(zg_graph* g, cudaStream_t s) {
         (ce = cudaMemsetAsync(fail.p, 0, sizeof(unsigned int), s)))
       return zg_check_cuda(ce, "hash memset");
     if (m) {
-      k_cuckoo_insert<<<grid_for(m, B), B, 0, s>>>(g->rec, m, g->hent, bits, seed, fail.as<unsigned int>());
-      k_cuckoo_check<<<grid_for(m, B), B, 0, s>>>(g->rec, m, g->hent, bits, seed, fail.as<unsigned int>());
+      k_cuckoo_insert<<<grid_for(m, B), B, 0, s>>>(g->d, m, g->hent, bits, seed, fail.as<unsigned int>());
+      k_cuckoo_check<<<grid_for(m, B), B, 0, s>>>(g->d, m, g->hent, bits, seed, fail.as<unsigned int>());
     }
     unsigned int hf = 0;
     if ((ce = cudaMemcpyAsync(&hf, fail.p, sizeof(hf), cudaMemcpyDeviceToHost, s)) || (ce = cudaStreamSynchronize(s)))
@@ -227,6 +247,25 @@ int build_hash(zg_graph* g, cudaStream_t s) {
   }
   zg_set_error(ZG_ERR_CUDA, "cuckoo table of %llu edges did not build", (unsigned long long)m);
   return ZG_ERR_CUDA;
+}
+
+// Record layout of the graphs built from now on (zg_set_record_layout).
+int g_record_layout = ZG_RECORDS_AUTO;
+
+// Wide records when the compact layout's sampling working set (records 16 B, edge-id adjacency
+// 16 B, cuckoo table about 10 B per edge, offsets) is more than twice the L2: such a graph is
+// served from HBM either way, and the wide record saves a dependent read and two sectors per step.
+// Near the L2 size the compact layout keeps more of the graph resident.
+bool wide_records(uint64_t m, uint32_t nv) {
+  if (g_record_layout == ZG_RECORDS_WIDE) return true;
+  if (g_record_layout == ZG_RECORDS_COMPACT) return false;
+  int dev = 0, l2 = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  const uint64_t hot = 42ull * m + 4ull * ((uint64_t)nv + 1);
+  return hot > 2ull * (uint64_t)l2;
 }
 
 // Builds a graph from a device COO (consumed: freed by the caller afterwards).
@@ -247,9 +286,11 @@ int build_graph(const uint2* d_coo, const uint32_t* d_w_in, uint64_t m, uint32_t
     return code;
   };
   uint64_t n2 = 2 * m;
+  g->wide = wide_records(m, nv);
+  const size_t rec_bytes = (g->wide ? sizeof(ZgRec) : sizeof(uint4)) * m;
   // adj_e and off32 share one allocation
   g->hot_bytes = sizeof(uint2) * n2 + sizeof(uint32_t) * ((size_t)nv + 1);
-  if ((rc = dev_alloc((char**)&g->hot, g->hot_bytes)) || (rc = dev_alloc(&g->rec, m)) ||
+  if ((rc = dev_alloc((char**)&g->hot, g->hot_bytes)) || (rc = dev_alloc((char**)&g->rec, rec_bytes)) ||
       (rc = dev_alloc(&g->off, (size_t)nv + 1)) || (!sampling_only && (rc = dev_alloc(&g->adj_n, n2))))
     return fail(rc);
   g->adj_e = (uint2*)g->hot;
@@ -261,7 +302,7 @@ int build_graph(const uint2* d_coo, const uint32_t* d_w_in, uint64_t m, uint32_t
       if (e != cudaSuccess) return fail(zg_check_cuda(e, "copy weights"));
     }
   }
-  g->bytes = sizeof(uint4) * m + (sizeof(int64_t) + sizeof(uint32_t)) * ((size_t)nv + 1) +
+  g->bytes = rec_bytes + (sizeof(int64_t) + sizeof(uint32_t)) * ((size_t)nv + 1) +
              (sampling_only ? 1 : 2) * sizeof(uint2) * n2 + (d_w_in ? sizeof(uint32_t) * m : 0);
   DevBuf deg, keys, keys2, vals, vals2, flags, tmp, nk, nk2, nv1, nv2;
   if ((rc = deg.alloc(sizeof(unsigned long long) * ((size_t)nv + 1))) ||
@@ -276,7 +317,7 @@ int build_graph(const uint2* d_coo, const uint32_t* d_w_in, uint64_t m, uint32_t
   if (m) {
     k_validate_count<<<grid_for(m, B), B, 0, s>>>(d_coo, m, nv, deg.as<unsigned long long>(),
                                                    keys.as<uint32_t>(), vals.as<unsigned long long>(),
-                                                   g->rec, flags.as<unsigned int>());
+                                                   g->rec, g->wide, flags.as<unsigned int>());
   }
   // offsets = exclusive scan of degrees (deg[nv] = 0 gives off[nv] = 2m)
   size_t tb = 0;
@@ -312,7 +353,7 @@ int build_graph(const uint2* d_coo, const uint32_t* d_w_in, uint64_t m, uint32_t
         ((rc = nk.alloc(sizeof(unsigned long long) * n2)) || (rc = nk2.alloc(sizeof(unsigned long long) * n2)) ||
          (rc = nv1.alloc(sizeof(uint32_t) * n2)) || (rc = nv2.alloc(sizeof(uint32_t) * n2))))
       return fail(rc);
-    k_suffix<<<grid_for(n2, B), B, 0, s>>>(keys2.as<uint32_t>(), g->adj_e, n2, g->off, g->rec,
+    k_suffix<<<grid_for(n2, B), B, 0, s>>>(keys2.as<uint32_t>(), g->adj_e, n2, g->off, g->rec, g->wide,
                                            nk.as<unsigned long long>(), nv1.as<uint32_t>());
     keys2.reset();
     if (!sampling_only) {
@@ -351,6 +392,8 @@ int build_graph(const uint2* d_coo, const uint32_t* d_w_in, uint64_t m, uint32_t
   k_off32<<<grid_for((uint64_t)nv + 1, B), B, 0, s>>>(g->off, (uint64_t)nv + 1, g->off32);
   g->d.m = m;
   g->d.rec = g->rec;
+  g->d.wide = g->wide;
+  g->d.off32 = g->off32;
   if ((rc = build_hash(g, s))) return fail(rc);
   ce = cudaGetLastError();
   if (ce != cudaSuccess) return fail(zg_check_cuda(ce, "graph build kernels"));
@@ -457,14 +500,14 @@ __global__ void k_select(uint64_t m, const uint32_t* __restrict__ w, int op, int
 }
 
 __global__ void k_compact(uint64_t m, const unsigned long long* __restrict__ flag,
-                          const unsigned long long* __restrict__ pos, const uint4* __restrict__ rec,
+                          const unsigned long long* __restrict__ pos, const ZgDevGraph src,
                           const uint32_t* __restrict__ w, uint2* __restrict__ coo_out,
                           uint32_t* __restrict__ w_out, unsigned long long* __restrict__ parent) {
   for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < m;
        e += (uint64_t)gridDim.x * blockDim.x) {
     if (!flag[e]) continue;
     unsigned long long p = pos[e];
-    uint4 r = rec[e];
+    uint4 r = zg_rec_e(src, e);
     coo_out[p] = make_uint2(r.x, r.y);
     if (w) w_out[p] = w[e];
     parent[p] = e;
@@ -509,7 +552,7 @@ int derive(bool sampling_only, const zg_graph* g, int mode, int op, int64_t t0, 
   }
   if (m)
     k_compact<<<grid_for(m, B), B, 0, s>>>(m, flag.as<unsigned long long>(), pos.as<unsigned long long>(),
-                                           g->rec, g->w, coo, w, parent);
+                                           g->d, g->w, coo, w, parent);
   if (shuffle_seed != ZG_NO_SHUFFLE) rc = permute(&coo, &w, &parent, kept, shuffle_seed, s);
   if (rc == ZG_OK) rc = build_graph(coo, w, kept, g->d.nv, s, out, sampling_only);
   if (rc == ZG_OK) {
@@ -608,6 +651,13 @@ extern "C" int zg_graph_permuted(const uint32_t* edges, uint64_t m, uint32_t num
   return rc;
 }
 
+extern "C" int zg_set_record_layout(int layout) {
+  if (layout < ZG_RECORDS_AUTO || layout > ZG_RECORDS_WIDE)
+    return zg_set_error(ZG_ERR_INVALID_ARG, "unknown record layout %d", layout), ZG_ERR_INVALID_ARG;
+  g_record_layout = layout;
+  return ZG_OK;
+}
+
 extern "C" int zg_graph_free(zg_graph* g) {
   if (!g) return ZG_OK;
   if (g->rec) cudaFree(g->rec);
@@ -628,6 +678,8 @@ extern "C" int zg_graph_get_meta(const zg_graph* g, zg_graph_meta* out) {
   out->num_edges = g->num_edges;
   out->max_degree = g->max_degree;
   out->device_bytes = g->bytes;
+  out->record_bytes = g->wide ? (uint32_t)sizeof(ZgRec) : (uint32_t)sizeof(uint4);
+  out->reserved = 0;
   return ZG_OK;
 }
 
@@ -644,17 +696,19 @@ extern "C" int zg_graph_download(const zg_graph* g, uint32_t* edges, uint32_t* w
   uint64_t m = g->d.m;
   cudaError_t ce = cudaSuccess;
   if ((edges || suffix) && m) {
-    std::vector<uint4> rec(m);
-    ce = cudaMemcpy(rec.data(), g->rec, sizeof(uint4) * m, cudaMemcpyDeviceToHost);
+    const uint64_t words = g->wide ? 8 : 4;  // 32-bit words per record
+    std::vector<uint32_t> rec(words * m);
+    ce = cudaMemcpy(rec.data(), g->rec, 4 * words * m, cudaMemcpyDeviceToHost);
     if (ce != cudaSuccess) return zg_check_cuda(ce, "download rec");
     for (uint64_t e = 0; e < m; ++e) {
+      const uint32_t* r = &rec[words * e];
       if (edges) {
-        edges[2 * e] = rec[e].x;
-        edges[2 * e + 1] = rec[e].y;
+        edges[2 * e] = r[0];
+        edges[2 * e + 1] = r[1];
       }
       if (suffix) {
-        suffix[2 * e] = rec[e].z;
-        suffix[2 * e + 1] = rec[e].w;
+        suffix[2 * e] = r[2];
+        suffix[2 * e + 1] = r[3];
       }
     }
   }

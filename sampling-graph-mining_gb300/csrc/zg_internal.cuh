@@ -1,21 +1,29 @@
 // zg_internal.cuh — shared device/host definitions of libzgraph_gpu.
 //
 // Device graph layout (all arrays in HBM, built by zg_graph.cu):
-//   rec[m]    uint4 (src, dst, suf_src, suf_dst): COO in edge-id order (edge id = position,
-//             src/Graph.cpp:295-306) plus, per endpoint, how many entries follow this edge in that
-//             endpoint's edge-id-ordered list.  suf gives the first conditional step's suffix
-//             size S without a search and locates the edge inside either list.
+//   rec[m]    one record per edge in edge-id order (edge id = position, src/Graph.cpp:295-306), in
+//             one of two layouts chosen when the graph is built (results are identical):
+//             compact, uint4 (src, dst, suf_src, suf_dst): the COO plus, per endpoint, how many
+//               entries follow this edge in that endpoint's edge-id-ordered list;
+//             wide, ZgRec (32 bytes, one sector): e = the compact record, p = (pos_src, pos_dst,
+//               pre_src, pre_dst), the index of the edge's own entry in adj_e within each
+//               endpoint's list and how many entries precede it there.
+//             A conditional step from an edge's endpoints needs S = suf_src + suf_dst and the
+//             entries' addresses pos + 1 .. pos + suf: the wide record gives both in one read, the
+//             compact one needs the endpoints' offsets (off32) as a second, dependent read.  The
+//             compact layout keeps graphs whose working set is near the L2 size resident; the wide
+//             one saves a dependent read and two sectors per step on graphs far larger than L2.
 //   off[V+1]  int64 offsets shared by both adjacency arrays (outgoing_adj_index).
 //   adj_e[2m] uint2 (nbr, edge_id) sorted by edge id per vertex (outgoing_adj_list order,
 //             asserted at src/Graph.cpp:324-334): the sampling order.
 //   adj_n[2m] uint2 (nbr, edge_id) sorted by (nbr, edge_id) per vertex (exports, exact counts).
 //   w[m]      uint32 edge data (Graph<VertexId>) or null.
-//   off32[V+1] the offsets as uint32 (2m < 2^32): what the sampling kernels read.
+//   off32[V+1] the offsets as uint32 (2m < 2^32), read by the compact layout's steps.
 //   hent[4B]  the edge set as a two-choice bucketed cuckoo table, B = 2^hbits buckets of 4
 //             entries (one 32-byte sector); entry = (fingerprint << 32) | edge id for the key
 //             (min(u,v) << 32) | max(u,v).  A closure check ("edge (x,y) exists with id >=
 //             min_valid") reads its two buckets together; a fingerprint match is confirmed
-//             against rec[edge id], so the answer is exact.
+//             against the record of that edge id, so the answer is exact.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -26,11 +34,17 @@
 #define ZG_STREAM_SHUFFLE 0xFFFFFFF0u
 #define ZG_STREAM_SUBSAMPLE 0xFFFFFFF1u
 
+struct __align__(32) ZgRec {
+  uint4 e;  // src, dst, suf_src, suf_dst
+  uint4 p;  // pos_src, pos_dst, pre_src, pre_dst
+};
+
 struct ZgDevGraph {
   uint32_t nv;
   uint32_t hbits;  // log2 of the cuckoo table's bucket count
   uint64_t m;
-  const uint4* rec;
+  const void* rec;  // ZgRec[m] when wide, else uint4[m]
+  uint32_t wide;
   const int64_t* off;
   const uint2* adj_e;
   const uint2* adj_n;
@@ -41,6 +55,13 @@ struct ZgDevGraph {
 };
 
 #define ZG_HASH_EMPTY 0xFFFFFFFFFFFFFFFFull
+
+#ifdef __CUDACC__
+// (src, dst, suf_src, suf_dst) of edge e, in either layout.
+__device__ __forceinline__ uint4 zg_rec_e(const ZgDevGraph& g, uint64_t e) {
+  return g.wide ? __ldg(&((const ZgRec*)g.rec)[e].e) : __ldg(&((const uint4*)g.rec)[e]);
+}
+#endif
 
 // splitmix64 finaliser: the cuckoo table's bucket hashes.
 __host__ __device__ __forceinline__ uint64_t zg_mix64(uint64_t z) {
@@ -65,7 +86,8 @@ __host__ __device__ __forceinline__ uint32_t zg_fingerprint(uint64_t key, uint64
 
 struct zg_graph {
   ZgDevGraph d;
-  uint4* rec;
+  void* rec;
+  uint32_t wide;
   int64_t* off;
   uint2* adj_e;
   uint2* adj_n;

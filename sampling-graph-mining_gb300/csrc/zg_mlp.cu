@@ -430,7 +430,7 @@ __global__ void k_deg_stats(ZgDevGraph g, DegStats* __restrict__ out) {
     }
   }
   for (uint64_t e = tid; e < g.m; e += stride) {
-    uint4 r = g.rec[e];
+    uint4 r = zg_rec_e(g, e);
     double du = (double)(g.off[r.x + 1] - g.off[r.x]), dv = (double)(g.off[r.y + 1] - g.off[r.y]);
     emin += fmin(du, dv);
     esum += du + dv;

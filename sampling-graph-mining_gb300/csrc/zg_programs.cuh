@@ -5,7 +5,8 @@
 // stream (seed, stream_id, sample index, draw index), so results do not depend on the launch
 // shape.  Each program restates one application estimate() (cited) on the device layout of
 // zg_internal.cuh:
-//   * the first conditional step reads its suffix sizes S from rec[] (no search);
+//   * a conditional step from an edge's endpoints reads its suffix sizes S and the entries'
+//     addresses from the edge's record (no search; see zg_internal.cuh for the two layouts);
 //   * later steps find lower bounds by interpolation search inside ranges the per-edge suffix
 //     counts already narrow;
 //   * closure checks (conditional_close, src/ZGraphInstance.cpp:372-407) look the edge up in the
@@ -117,6 +118,65 @@ __device__ __forceinline__ void ld_bucket(const unsigned long long* p, ulonglong
   asm("ld.global.nc.v4.u64 {%0, %1, %2, %3}, [%4];" : "=l"(lo.x), "=l"(lo.y), "=l"(hi.x), "=l"(hi.y) : "l"(p));
 }
 
+// One wide edge record (32 bytes, one sector) in a single 256-bit load.
+__device__ __forceinline__ void ld_rec(const ZgRec* r, uint4& e, uint4& p) {
+  unsigned long long a, b, c, d;
+  asm("ld.global.nc.v4.u64 {%0, %1, %2, %3}, [%4];" : "=l"(a), "=l"(b), "=l"(c), "=l"(d) : "l"(r));
+  e = make_uint4((uint32_t)a, (uint32_t)(a >> 32), (uint32_t)b, (uint32_t)(b >> 32));
+  p = make_uint4((uint32_t)c, (uint32_t)(c >> 32), (uint32_t)d, (uint32_t)(d >> 32));
+}
+
+// Edge e's record with both endpoints unknown: e = (src, dst, suf_src, suf_dst), p = (pos_src,
+// pos_dst, pre_src, pre_dst).  Wide layout: one read.  Compact: the record, then the endpoints'
+// offsets (the pre_* loads vanish where a caller does not use them).
+__device__ __forceinline__ void edge_rec(const ZgDevGraph& g, uint64_t e, uint4& q, uint4& p) {
+  if (g.wide) {
+    ld_rec(&((const ZgRec*)g.rec)[e], q, p);
+    return;
+  }
+  q = ZG_LDG(&((const uint4*)g.rec)[e]);
+  p.x = ZG_LDG(&g.off32[q.x + 1]) - q.z - 1;
+  p.y = ZG_LDG(&g.off32[q.y + 1]) - q.w - 1;
+  p.z = p.x - ZG_LDG(&g.off32[q.x]);
+  p.w = p.y - ZG_LDG(&g.off32[q.y]);
+}
+
+// The first entry after edge (q, p) in its src's (dst = false) or dst's list.  Compact layout:
+// one offset read, of the chosen endpoint only.
+__device__ __forceinline__ uint32_t after_edge(const ZgDevGraph& g, const uint4& q, const uint4& p, bool dst) {
+  if (g.wide) return (dst ? p.y : p.x) + 1;
+  return ZG_LDG(&g.off32[(dst ? q.y : q.x) + 1]) - (dst ? q.w : q.z);
+}
+
+// Edge e seen from its endpoint v (already known): entries after it in v's list and its own slot
+// there.  Compact layout: the record and v's end offset are read together.
+struct EdgeAt {
+  uint32_t suf, pos, pre;  // pre: wide layout only (see edge_at_start)
+};
+__device__ __forceinline__ EdgeAt edge_at(const ZgDevGraph& g, uint64_t e, uint32_t v) {
+  EdgeAt r;
+  if (g.wide) {
+    uint4 q, p;
+    ld_rec(&((const ZgRec*)g.rec)[e], q, p);
+    const bool s = q.x == v;
+    r.suf = s ? q.z : q.w;
+    r.pos = s ? p.x : p.y;
+    r.pre = s ? p.z : p.w;
+    return r;
+  }
+  const uint4 q = ZG_LDG(&((const uint4*)g.rec)[e]);
+  const uint32_t end = ZG_LDG(&g.off32[v + 1]);
+  r.suf = q.x == v ? q.z : q.w;
+  r.pos = end - r.suf - 1;
+  r.pre = 0;
+  return r;
+}
+// The first slot of v's list, for a step that searches it (compact layout: v's start offset, a
+// read independent of the record, issued only where a search needs it).
+__device__ __forceinline__ uint32_t edge_at_start(const ZgDevGraph& g, const EdgeAt& a, uint32_t v) {
+  return g.wide ? a.pos - a.pre : ZG_LDG(&g.off32[v]);
+}
+
 struct EdgeProbe {
   unsigned long long key, cand;
 };
@@ -150,7 +210,7 @@ __device__ __noinline__ int64_t edge_rescan(const ZgDevGraph& g, unsigned long l
   for (int i = 0; i < 8; ++i) {
     unsigned long long x = ZG_LDG(&g.hent[(i < 4 ? b1 : b2) + (i & 3)]);
     if (x == cand || (uint32_t)(x >> 32) != fp) continue;
-    uint4 q = ZG_LDG(&g.rec[(uint32_t)x]);
+    uint4 q = zg_rec_e(g, (uint32_t)x);
     if (zg_edge_key(q.x, q.y) == key) return (int64_t)(uint32_t)x;
   }
   return -1;
@@ -158,7 +218,7 @@ __device__ __noinline__ int64_t edge_rescan(const ZgDevGraph& g, unsigned long l
 
 __device__ __forceinline__ int64_t edge_confirm(const ZgDevGraph& g, const EdgeProbe& pr) {
   if (pr.cand == ZG_HASH_EMPTY) return -1;
-  uint4 r = ZG_LDG(&g.rec[(uint32_t)pr.cand]);
+  uint4 r = zg_rec_e(g, (uint32_t)pr.cand);
   if (zg_edge_key(r.x, r.y) == pr.key) return (int64_t)(uint32_t)pr.cand;
   return edge_rescan(g, pr.key, pr.cand);
 }
@@ -285,8 +345,8 @@ __device__ void prog_triangle(const ZgDevGraph& g, Ctx& c, Res& r) {
   }
   const uint64_t w1 = c.word(1);  // the second draw's Philox work overlaps the first loads
   uint64_t e0 = c.draw(0, g.m - 1);
-  uint4 q = ZG_LDG(&g.rec[e0]);
-  uint32_t endx = ZG_LDG(&g.off32[q.x + 1]), endy = ZG_LDG(&g.off32[q.y + 1]);
+  uint4 q, qp;
+  edge_rec(g, e0, q, qp);
   uint64_t S = (uint64_t)q.z + q.w;
   if (DBG) c.sectors += 1 + model_anchor(g, q.x) + model_anchor(g, q.y);
   if (S == 0) {
@@ -297,7 +357,7 @@ __device__ void prog_triangle(const ZgDevGraph& g, Ctx& c, Res& r) {
   uint64_t r1 = c.take(w1, 0, S - 1);
   const bool on_y = r1 >= q.z;  // the conditional edge hangs off dst
   const uint32_t other = on_y ? q.x : q.y;
-  uint32_t idx = on_y ? endy - q.w + (uint32_t)(r1 - q.z) : endx - q.z + (uint32_t)r1;
+  uint32_t idx = after_edge(g, q, qp, on_y) + (uint32_t)(on_y ? r1 - q.z : r1);
   uint2 e1 = ZG_LDG(&g.adj_e[idx]);
   uint32_t a1 = 1 + (e1.x == q.x || e1.x == q.y);
   res_mul(r, g.m);
@@ -322,7 +382,7 @@ __device__ void prog_three_chain(const ZgDevGraph& g, Ctx& c, Res& r) {
     return;
   }
   uint64_t e0 = c.draw(0, g.m - 1);
-  uint4 q = ZG_LDG(&g.rec[e0]);
+  uint4 q = zg_rec_e(g, e0);
   uint64_t S = (uint64_t)q.z + q.w;
   if (DBG) c.sectors += 1 + model_anchor(g, q.x) + model_anchor(g, q.y);
   if (S == 0) {
@@ -335,13 +395,14 @@ __device__ void prog_three_chain(const ZgDevGraph& g, Ctx& c, Res& r) {
   // (zg_graph_create rejects duplicate edges); the debug variant reads it and checks.
   uint32_t a1 = 1;
   if (DBG) {
-    uint32_t anchor = q.x, suf = q.z;
+    uint4 q2, qp;
+    edge_rec(g, e0, q2, qp);
+    uint32_t base = qp.x + 1;
     if (r1 >= q.z) {
       r1 -= q.z;
-      anchor = q.y;
-      suf = q.w;
+      base = qp.y + 1;
     }
-    uint2 e1 = ZG_LDG(&g.adj_e[ZG_LDG(&g.off32[anchor + 1]) - (uint32_t)suf + (uint32_t)r1]);
+    uint2 e1 = ZG_LDG(&g.adj_e[base + (uint32_t)r1]);
     a1 = 1 + (e1.x == q.x || e1.x == q.y);
   }
   res_mul(r, g.m);
@@ -417,7 +478,8 @@ __device__ void prog_four_clique(const ZgDevGraph& g, Ctx& c, Res& r) {
   }
   const uint64_t w1 = c.word(1), w2 = c.word(2);  // Philox work of the later draws, up front
   uint64_t e0 = c.draw(0, g.m - 1);
-  uint4 q = ZG_LDG(&g.rec[e0]);
+  uint4 q, qp;
+  edge_rec(g, e0, q, qp);
   uint64_t S1 = (uint64_t)q.z + q.w;
   if (DBG) c.sectors += 1 + model_anchor(g, q.x) + model_anchor(g, q.y);
   if (S1 == 0) {
@@ -427,9 +489,11 @@ __device__ void prog_four_clique(const ZgDevGraph& g, Ctx& c, Res& r) {
   if (DBG) c.sectors += 1;
   uint64_t r1 = c.take(w1, 0, S1 - 1);
   const uint32_t va = q.x, vb = q.y;
-  uint32_t endA = ZG_LDG(&g.off32[va + 1]), endB = ZG_LDG(&g.off32[vb + 1]);
   const bool s1b = r1 >= q.z;  // the first conditional edge hangs off b
-  uint32_t idx1 = (s1b ? endB - q.w + (uint32_t)(r1 - q.z) : endA - q.z + (uint32_t)r1);
+  const uint32_t r1o = (uint32_t)(s1b ? r1 - q.z : r1);  // its place among the anchor's entries after e0
+  const uint32_t suf_own = s1b ? q.w : q.z, suf_oth = s1b ? q.z : q.w;
+  const uint32_t base_own = after_edge(g, q, qp, s1b);  // the anchor's first entry after e0
+  const uint32_t idx1 = base_own + r1o;
   uint2 e1 = ZG_LDG(&g.adj_e[idx1]);
   const uint32_t vc = e1.x;
   uint32_t a1 = 1 + (vc == va || vc == vb);
@@ -442,7 +506,7 @@ __device__ void prog_four_clique(const ZgDevGraph& g, Ctx& c, Res& r) {
   // no candidate at all (then it fails, as below).  With entries after e1 left in the anchor's own
   // list that cannot happen, and the sample ends here; the counters are those of the full path.
   const uint32_t x0 = s1b ? va : vb;
-  const uint32_t own = (s1b ? endB : endA) - (idx1 + 1);  // the anchor's entries after e1
+  const uint32_t own = suf_own - r1o - 1;  // the anchor's entries after e1
   EdgeProbe p0{0ull, ZG_HASH_EMPTY};
   if (!DBG) {
     p0 = edge_candidate(g, x0, vc);
@@ -450,15 +514,16 @@ __device__ void prog_four_clique(const ZgDevGraph& g, Ctx& c, Res& r) {
   }
   // second conditional step: anchors [a, b, c], min_valid = id1 + 1
   uint32_t mv = e1.y + 1;
-  uint4 q1 = ZG_LDG(&g.rec[e1.y]);
-  uint32_t endC = ZG_LDG(&g.off32[vc + 1]);
-  uint32_t lbC = endC - ((q1.x == vc) ? q1.z : q1.w);
+  const EdgeAt ac = edge_at(g, e1.y, vc);
+  const uint32_t lbC = ac.pos + 1;  // c's entries after e1
+  const uint32_t endC = lbC + ac.suf;
   // the anchor's own list continues right after e1; the other endpoint's list needs a search
   // (that suffix holds edge ids in [id0 + 1, m - 1])
-  uint32_t lo = lb_eid(g.adj_e, s1b ? endA - q.z : endB - q.w, s1b ? endA : endB, mv, (uint32_t)e0 + 1,
-                       (uint32_t)(g.m - 1));
+  const uint32_t base_oth = after_edge(g, q, qp, !s1b);
+  const uint32_t end_own = base_own + suf_own, end_oth = base_oth + suf_oth;
+  uint32_t lo = lb_eid(g.adj_e, base_oth, end_oth, mv, (uint32_t)e0 + 1, (uint32_t)(g.m - 1));
   uint32_t lbA = s1b ? lo : idx1 + 1, lbB = s1b ? idx1 + 1 : lo;
-  uint64_t lenA = endA - lbA, lenB = endB - lbB;
+  uint64_t lenA = (s1b ? end_oth : end_own) - lbA, lenB = (s1b ? end_own : end_oth) - lbB;
   // when c coincides with a or b (duplicate edges) the reference lists only two vertices
   uint64_t lenC = a1 == 1 ? (uint64_t)(endC - lbC) : 0;
   uint64_t S2 = lenA + lenB + lenC;
@@ -541,7 +606,8 @@ __device__ void prog_four_chain(const ZgDevGraph& g, Ctx& c, Res& r) {
   }
   uint64_t e0 = c.draw(0, g.m - 1);
   res_mul(r, g.m);
-  uint4 q = ZG_LDG(&g.rec[e0]);
+  uint4 q, qp;
+  edge_rec(g, e0, q, qp);
   const uint32_t a = q.x, b = q.y;
   if (DBG) c.sectors += 1;
   // The three programs share one chain of dependent loads (edge record, anchor offset, e1,
@@ -557,13 +623,10 @@ __device__ void prog_four_chain(const ZgDevGraph& g, Ctx& c, Res& r) {
   }
   if (DBG) c.sectors += 1;
   uint64_t r1 = c.take(w2, 0, S1 - 1);
-  uint32_t anchor = a, suf = q.z;
-  if (!split && r1 >= q.z) {
-    r1 -= q.z;
-    anchor = b;
-    suf = q.w;
-  }
-  const uint2 e1 = ZG_LDG(&g.adj_e[ZG_LDG(&g.off32[anchor + 1]) - suf + (uint32_t)r1]);
+  const bool on_b = !split && r1 >= q.z;  // e1 hangs off b
+  if (on_b) r1 -= q.z;
+  const uint32_t anchor = on_b ? b : a;
+  const uint2 e1 = ZG_LDG(&g.adj_e[after_edge(g, q, qp, on_b) + (uint32_t)r1]);
   const uint32_t a1 = 1 + (e1.x == a || (!split && e1.x == b));
   res_mul(r, S1);
   if (a1 == 2) r.shift++;
@@ -574,14 +637,16 @@ __device__ void prog_four_chain(const ZgDevGraph& g, Ctx& c, Res& r) {
   else if (a == e1.x) v2 = anchor;
   else if (b == anchor) v2 = e1.x;
   else v2 = anchor;
-  const uint32_t end2 = ZG_LDG(&g.off32[v2 + 1]);
-  uint32_t lb2 = end2 - q.w;  // sel 3: b's entries after e0
-  if (!split) {
-    const uint4 q1 = ZG_LDG(&g.rec[e1.y]);
-    const uint32_t suf1 = (q1.x == v2) ? q1.z : q1.w;  // entries after e1 in v2's list
-    lb2 = end2 - suf1;                                // sel 1: min_valid = id1 + 1
+  uint32_t lb2, end2;
+  if (split) {
+    lb2 = after_edge(g, q, qp, true);  // sel 3: b's entries after e0
+    end2 = lb2 + q.w;
+  } else {
+    const EdgeAt a1v = edge_at(g, e1.y, v2);  // e1 in v2's list
+    lb2 = a1v.pos + 1;                          // sel 1: min_valid = id1 + 1
+    end2 = lb2 + a1v.suf;
     if (sel == 2)  // min_valid = id0 + 1, at or before e1's own slot in v2's list
-      lb2 = lb_eid(g.adj_e, ZG_LDG(&g.off32[v2]), lb2, (uint32_t)e0 + 1, 0u, e1.y);
+      lb2 = lb_eid(g.adj_e, edge_at_start(g, a1v, v2), lb2, (uint32_t)e0 + 1, 0u, e1.y);
   }
   const uint64_t S2 = (uint64_t)(end2 - lb2);
   if (DBG) c.sectors += model_anchor(g, v2);
@@ -636,7 +701,8 @@ __device__ void prog_chain(const ZgDevGraph& g, int order, Ctx& c, Res& r) {
   }
   uint64_t e0 = c.draw(0, g.m - 1);
   res_mul(r, g.m);
-  uint4 q = ZG_LDG(&g.rec[e0]);
+  uint4 q, qp;
+  edge_rec(g, e0, q, qp);
   uint32_t es[ZG_MAX_LIST], ed[ZG_MAX_LIST], ei[ZG_MAX_LIST];
   uint32_t vs[ZG_MAX_LIST];
   int ne = 1, nvtx = 2;
@@ -647,10 +713,10 @@ __device__ void prog_chain(const ZgDevGraph& g, int order, Ctx& c, Res& r) {
   vs[1] = q.y;
   uint32_t f[2] = {q.x, q.y};
   uint32_t fe[2], fl[2];
-  fe[0] = ZG_LDG(&g.off32[q.x + 1]);
-  fe[1] = ZG_LDG(&g.off32[q.y + 1]);
-  fl[0] = fe[0] - q.z;
-  fl[1] = fe[1] - q.w;
+  fl[0] = qp.x + 1;
+  fl[1] = qp.y + 1;
+  fe[0] = fl[0] + q.z;
+  fe[1] = fl[1] + q.w;
   Ext p;
   if (DBG) p = ext_from_double(ddiv(1.0, u2d(g.m)));
   if (DBG) c.sectors += 1;
@@ -688,11 +754,9 @@ __device__ void prog_chain(const ZgDevGraph& g, int order, Ctx& c, Res& r) {
     // frontier update (ChainMining.cpp:265-80); here src is a frontier vertex and e.x is new
     int upd = (f[0] == src) ? 0 : 1;
     f[upd] = e.x;
-    uint4 qe = ZG_LDG(&g.rec[e.y]);
-    uint32_t sufe = (qe.x == e.x) ? qe.z : qe.w;
-    fe[upd] = ZG_LDG(&g.off32[e.x + 1]);
-    uint32_t pos = fe[upd] - (uint32_t)sufe - 1;  // e's own slot in the new frontier's list
-    fl[upd] = lb_eid(g.adj_e, ZG_LDG(&g.off32[e.x]), pos + 1, mv, 0u, e.y);
+    const EdgeAt ae = edge_at(g, e.y, e.x);  // e in the new frontier's list
+    fe[upd] = ae.pos + 1 + ae.suf;
+    fl[upd] = lb_eid(g.adj_e, edge_at_start(g, ae, e.x), ae.pos + 1, mv, 0u, e.y);
   }
   r.hit = true;
   if (DBG) r.w = ext_to_double(ext_inv(p));
@@ -716,7 +780,8 @@ __device__ void prog_pattern(const ZgDevGraph& g, const ZgProgParams& pp, Ctx& c
   }
   uint64_t e0 = c.draw(0, g.m - 1);
   res_mul(r, g.m);
-  uint4 q = ZG_LDG(&g.rec[e0]);
+  uint4 q, qp;
+  edge_rec(g, e0, q, qp);
   const int MV = ZG_MAX_PATTERN_V + 1;
   uint32_t vs[MV];
   uint32_t vl[MV], ve[MV];
@@ -724,10 +789,10 @@ __device__ void prog_pattern(const ZgDevGraph& g, const ZgProgParams& pp, Ctx& c
   int nvtx = 2, ne = 1;
   vs[0] = q.x;
   vs[1] = q.y;
-  ve[0] = ZG_LDG(&g.off32[q.x + 1]);
-  ve[1] = ZG_LDG(&g.off32[q.y + 1]);
-  vl[0] = ve[0] - q.z;
-  vl[1] = ve[1] - q.w;
+  vl[0] = qp.x + 1;
+  vl[1] = qp.y + 1;
+  ve[0] = vl[0] + q.z;
+  ve[1] = vl[1] + q.w;
   es[0] = q.x;
   ed[0] = q.y;
   ei[0] = (uint32_t)e0;
@@ -768,11 +833,9 @@ __device__ void prog_pattern(const ZgDevGraph& g, const ZgProgParams& pp, Ctx& c
     ++ne;
     if (nbr_slot < 0) {
       vs[nvtx] = e.x;
-      uint4 qe = ZG_LDG(&g.rec[e.y]);
-      uint32_t sufe = (qe.x == e.x) ? qe.z : qe.w;
-      ve[nvtx] = ZG_LDG(&g.off32[e.x + 1]);
-      uint32_t pos = ve[nvtx] - (uint32_t)sufe - 1;
-      vl[nvtx] = lb_eid(g.adj_e, ZG_LDG(&g.off32[e.x]), pos + 1, mv, 0u, e.y);
+      const EdgeAt ae = edge_at(g, e.y, e.x);  // e in the new vertex's list
+      ve[nvtx] = ae.pos + 1 + ae.suf;
+      vl[nvtx] = lb_eid(g.adj_e, edge_at_start(g, ae, e.x), ae.pos + 1, mv, 0u, e.y);
       ++nvtx;
       if ((uint32_t)nvtx > pp.pv) return;
     }

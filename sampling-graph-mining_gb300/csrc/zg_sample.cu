@@ -28,11 +28,13 @@ __device__ __forceinline__ void run_program(const ZgDevGraph& g, const ZgProgPar
   }
 }
 
-// Production kernels: one specialisation per program and per register budget (MINB resident
-// blocks of 256 threads requested from the compiler); zg_tune picks the fastest per program.
-template <int KIND, int MINB>
+// Production kernels: one specialisation per program, per register budget (MINB resident blocks
+// of 256 threads requested from the compiler; zg_tune picks the fastest per program) and per record
+// layout (the layout tests of the record accessors fold away; each layout gets its own registers).
+template <int KIND, int MINB, bool WIDE>
 __global__ void __launch_bounds__(kBlock, MINB) k_sample(ZgDevGraph g, ZgProgParams pp, uint64_t n, uint64_t first,
                                                    uint64_t seed, uint32_t stream, ZgPartial* __restrict__ partials) {
+  g.wide = WIDE;
   Acc a;
   acc_init(a);
   uint64_t stride = (uint64_t)gridDim.x * kBlock;
@@ -124,7 +126,8 @@ __global__ void __launch_bounds__(kBlock) k_three_motif(ZgDevGraph g, uint64_t n
         r.fail = true;
       } else {
         uint64_t e0 = c.draw(0, g.m - 1);
-        uint4 q = ZG_LDG(&g.rec[e0]);
+        uint4 q, qp;
+        edge_rec(g, e0, q, qp);
         uint64_t S = (uint64_t)q.z + q.w;
         if (DBG) c.sectors += 1 + model_anchor(g, q.x) + model_anchor(g, q.y);
         if (S == 0) {
@@ -132,18 +135,14 @@ __global__ void __launch_bounds__(kBlock) k_three_motif(ZgDevGraph g, uint64_t n
         } else {
           if (DBG) c.sectors += 1;
           uint64_t r1 = c.draw(0, S - 1);
-          uint32_t anchor = q.x, other = q.y, suf = q.z;
-          if (r1 >= q.z) {
-            r1 -= q.z;
-            anchor = q.y;
-            other = q.x;
-            suf = q.w;
-          }
+          const bool on_y = r1 >= q.z;
+          if (on_y) r1 -= q.z;
+          const uint32_t other = on_y ? q.x : q.y;
           res_mul(r, g.m);
           res_mul(r, S);
           r.hit = true;
           if (i < n_tri) {
-            uint2 e1 = ZG_LDG(&g.adj_e[ZG_LDG(&g.off32[anchor + 1]) - (uint32_t)suf + (uint32_t)r1]);
+            uint2 e1 = ZG_LDG(&g.adj_e[after_edge(g, q, qp, on_y) + (uint32_t)r1]);
             uint32_t a1 = 1 + (e1.x == q.x || e1.x == q.y);
             if (a1 == 2) r.shift = 1;
             rt.hit = a1 == 1 && edge_after(g, other, e1.x, e1.y + 1);
@@ -361,35 +360,40 @@ constexpr int kVariants = 6;
 constexpr int kMinBlocks[kVariants] = {1, 2, 3, 4, 6, 8};
 typedef void (*SampleKernel)(ZgDevGraph, ZgProgParams, uint64_t, uint64_t, uint64_t, uint32_t, ZgPartial*);
 
-template <int KIND>
+template <int KIND, bool WIDE>
 SampleKernel kernel_variant(int v) {
   switch (v) {
-    case 0: return k_sample<KIND, 1>;
-    case 1: return k_sample<KIND, 2>;
-    case 2: return k_sample<KIND, 3>;
-    case 3: return k_sample<KIND, 4>;
-    case 4: return k_sample<KIND, 6>;
-    default: return k_sample<KIND, 8>;
+    case 0: return k_sample<KIND, 1, WIDE>;
+    case 1: return k_sample<KIND, 2, WIDE>;
+    case 2: return k_sample<KIND, 3, WIDE>;
+    case 3: return k_sample<KIND, 4, WIDE>;
+    case 4: return k_sample<KIND, 6, WIDE>;
+    default: return k_sample<KIND, 8, WIDE>;
   }
 }
 
-SampleKernel kernel_for(int kind, int v) {
+template <bool WIDE>
+SampleKernel kernel_for_layout(int kind, int v) {
   switch (kind) {
-    case ZG_PROG_TRIANGLE: return kernel_variant<ZG_PROG_TRIANGLE>(v);
-    case ZG_PROG_FOUR_CLIQUE: return kernel_variant<ZG_PROG_FOUR_CLIQUE>(v);
-    case ZG_PROG_FOUR_CLIQUE_UNBIASED: return kernel_variant<ZG_PROG_FOUR_CLIQUE_UNBIASED>(v);
-    case ZG_PROG_THREE_CHAIN: return kernel_variant<ZG_PROG_THREE_CHAIN>(v);
-    case ZG_PROG_FOUR_CHAIN: return kernel_variant<ZG_PROG_FOUR_CHAIN>(v);
-    case ZG_PROG_CHAIN: return kernel_variant<ZG_PROG_CHAIN>(v);
-    default: return kernel_variant<ZG_PROG_PATTERN>(v);
+    case ZG_PROG_TRIANGLE: return kernel_variant<ZG_PROG_TRIANGLE, WIDE>(v);
+    case ZG_PROG_FOUR_CLIQUE: return kernel_variant<ZG_PROG_FOUR_CLIQUE, WIDE>(v);
+    case ZG_PROG_FOUR_CLIQUE_UNBIASED: return kernel_variant<ZG_PROG_FOUR_CLIQUE_UNBIASED, WIDE>(v);
+    case ZG_PROG_THREE_CHAIN: return kernel_variant<ZG_PROG_THREE_CHAIN, WIDE>(v);
+    case ZG_PROG_FOUR_CHAIN: return kernel_variant<ZG_PROG_FOUR_CHAIN, WIDE>(v);
+    case ZG_PROG_CHAIN: return kernel_variant<ZG_PROG_CHAIN, WIDE>(v);
+    default: return kernel_variant<ZG_PROG_PATTERN, WIDE>(v);
   }
+}
+
+SampleKernel kernel_for(int kind, int v, bool wide) {
+  return wide ? kernel_for_layout<true>(kind, v) : kernel_for_layout<false>(kind, v);
 }
 
 // Per device: the variant each program kind uses and its occupancy grid.
 constexpr int kMaxDev = 64;
 std::mutex g_tune_mu;
 int g_variant[kMaxDev][8];
-int g_grid[kMaxDev][8][kVariants];
+int g_grid[kMaxDev][8][kVariants][2];
 bool g_tune_init[kMaxDev];
 // Defaults before tuning (register footprints measured with -Xptxas -v).
 constexpr int kDefaultVariant[8] = {3, 3, 2, 3, 2, 3, 3, 3};
@@ -412,15 +416,15 @@ int variant_for(int kind) {
   return g_variant[d][kind_slot(kind)];
 }
 
-int grid_for_variant(int kind, int v) {
+int grid_for_variant(int kind, int v, bool wide) {
   int d = current_device();
   std::lock_guard<std::mutex> lk(g_tune_mu);
-  int& g = g_grid[d][kind_slot(kind)][v];
-  if (!g) g = grid_of(kernel_for(kind, v));
+  int& g = g_grid[d][kind_slot(kind)][v][wide ? 1 : 0];
+  if (!g) g = grid_of(kernel_for(kind, v, wide));
   return g;
 }
 
-int grid_for_kind(int kind) { return grid_for_variant(kind, variant_for(kind)); }
+int grid_for_kind(int kind, bool wide) { return grid_for_variant(kind, variant_for(kind), wide); }
 
 int validate_run(const zg_graph* g, const zg_program* p) {
   if (!g || !p) return zg_set_error(ZG_ERR_INVALID_ARG, "null graph or program"), ZG_ERR_INVALID_ARG;
@@ -430,7 +434,7 @@ int validate_run(const zg_graph* g, const zg_program* p) {
 int launch_variant(const zg_graph* g, const zg_program* p, int v, uint64_t n, uint64_t first, uint64_t seed,
                    uint32_t stream_id, cudaStream_t s, ZgPartial* parts, int grid) {
   ZgProgParams pp = params_for(p);
-  SampleKernel k = kernel_for(p->kind, v);
+  SampleKernel k = kernel_for(p->kind, v, g->wide != 0);
   k<<<grid, kBlock, 0, s>>>(g->d, pp, n, first, seed, stream_id, parts);
   return ZG_OK;
 }
@@ -451,7 +455,7 @@ void zg_partial_to_counters(const void* partial, uint32_t den, zg_counters* out)
 double zg_exact_mean_host(const uint64_t s[5], uint32_t den, uint64_t n) { return exact_mean(s, den, n); }
 
 // Shared by the allocation-free entry points of other translation units.
-int zg_sample_grid(int kind) { return grid_for_kind(kind); }
+int zg_sample_grid(int kind, bool wide) { return grid_for_kind(kind, wide); }
 
 // Per-group estimates (device array out[n_groups]) on stream s.
 int zg_launch_groups(const zg_graph* g, const zg_program* p, uint64_t n_groups, uint32_t group, uint64_t first,
@@ -483,7 +487,7 @@ extern "C" int zg_run(const zg_graph* g, const zg_program* p, uint64_t n, uint64
   if (!out) return zg_set_error(ZG_ERR_INVALID_ARG, "null output"), ZG_ERR_INVALID_ARG;
   cudaStream_t s = (cudaStream_t)cuda_stream;
   uint64_t maxg = (n + kBlock - 1) / kBlock;
-  int grid = grid_for_kind(p->kind);
+  int grid = grid_for_kind(p->kind, g->wide != 0);
   if ((uint64_t)grid > maxg) grid = (int)(maxg ? maxg : 1);
   ZgPartial* parts = nullptr;
   ZG_CUDA(cudaMallocAsync((void**)&parts, sizeof(ZgPartial) * (grid + 1), s));
@@ -508,7 +512,7 @@ extern "C" int zg_run_async(const zg_graph* g, const zg_program* p, uint64_t n, 
   if (!d_result) return zg_set_error(ZG_ERR_INVALID_ARG, "null device result"), ZG_ERR_INVALID_ARG;
   cudaStream_t s = (cudaStream_t)cuda_stream;
   uint64_t maxg = (n + kBlock - 1) / kBlock;
-  int grid = grid_for_kind(p->kind);
+  int grid = grid_for_kind(p->kind, g->wide != 0);
   if ((uint64_t)grid > maxg) grid = (int)(maxg ? maxg : 1);
   ZgPartial* parts = nullptr;
   ZG_CUDA(cudaMallocAsync((void**)&parts, sizeof(ZgPartial) * grid, s));
@@ -538,7 +542,7 @@ extern "C" int zg_get_variant(int kind, int* variant, int* min_blocks, int* grid
   int v = variant_for(kind);
   if (variant) *variant = v;
   if (min_blocks) *min_blocks = kMinBlocks[v];
-  if (grid) *grid = grid_for_variant(kind, v);
+  if (grid) *grid = grid_for_variant(kind, v, false);
   return ZG_OK;
 }
 
@@ -551,7 +555,7 @@ extern "C" int zg_tune(const zg_graph* g, const zg_program* p, uint64_t probe_sa
   if (probe_samples == 0) probe_samples = 1ull << 22;
   cudaStream_t s = (cudaStream_t)cuda_stream;
   int grid_max = 0;
-  for (int v = 0; v < kVariants; ++v) grid_max = std::max(grid_max, grid_for_variant(p->kind, v));
+  for (int v = 0; v < kVariants; ++v) grid_max = std::max(grid_max, grid_for_variant(p->kind, v, g->wide != 0));
   ZgPartial* parts = nullptr;
   ZG_CUDA(cudaMallocAsync((void**)&parts, sizeof(ZgPartial) * (grid_max + 1), s));
   cudaEvent_t e0, e1;
@@ -562,7 +566,7 @@ extern "C" int zg_tune(const zg_graph* g, const zg_program* p, uint64_t probe_sa
   const int reps = 3;
   cudaError_t ce = cudaSuccess;
   for (int v = 0; v < kVariants && ce == cudaSuccess; ++v) {
-    int grid = grid_for_variant(p->kind, v);
+    int grid = grid_for_variant(p->kind, v, g->wide != 0);
     uint64_t maxg = (probe_samples + kBlock - 1) / kBlock;
     if ((uint64_t)grid > maxg) grid = (int)maxg;
     float vbest = 1e30f;

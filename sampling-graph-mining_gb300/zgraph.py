@@ -34,6 +34,7 @@ EXACT_TRIANGLE, EXACT_WEDGE, EXACT_THREE_PATH, EXACT_FIVE_STAR, EXACT_FOUR_CLIQU
 PRED_GE, PRED_LT, PRED_GT, PRED_LE, PRED_EQ, PRED_NE, PRED_RANGE = 1, 2, 3, 4, 5, 6, 7
 QUERY_THREE_MOTIF = 16
 GRAPH_SAMPLING_ONLY = 1
+RECORDS_AUTO, RECORDS_COMPACT, RECORDS_WIDE = 0, 1, 2
 BATCH_MAX_QUERIES, BATCH_MAX_CHUNKS = 65536, 65536
 NO_SHUFFLE = 0xFFFFFFFFFFFFFFFF
 MAX_DRAWS = 16
@@ -47,7 +48,8 @@ class ZgError(RuntimeError):
 
 class GraphMeta(C.Structure):
     _fields_ = [("num_vertices", C.c_uint32), ("weighted", C.c_uint32), ("num_local_edges", C.c_uint64),
-                ("num_edges", C.c_uint64), ("max_degree", C.c_uint64), ("device_bytes", C.c_uint64)]
+                ("num_edges", C.c_uint64), ("max_degree", C.c_uint64), ("device_bytes", C.c_uint64),
+                ("record_bytes", C.c_uint32), ("reserved", C.c_uint32)]
 
 
 class Counters(C.Structure):
@@ -114,7 +116,7 @@ def lib():
             "zg_version": ([], I32), "zg_init": ([I32], I32), "zg_last_error": ([], C.c_char_p),
             "zg_graph_create": ([P, U64, U32, P, P, C.POINTER(P)], I32),
             "zg_graph_permuted": ([P, U64, U32, P, U64, P, P, C.POINTER(P)], I32),
-            "zg_graph_free": ([P], I32),
+            "zg_graph_free": ([P], I32), "zg_set_record_layout": ([I32], I32),
             "zg_graph_get_meta": ([P, C.POINTER(GraphMeta)], I32),
             "zg_graph_set_meta": ([P, U64, U64], I32),
             "zg_graph_download": ([P, P, P, P, P, P, P], I32),
@@ -354,6 +356,12 @@ class Graph:
             self.free()
         except Exception:
             pass
+
+
+def set_record_layout(layout):
+    """zg_set_record_layout: per-edge record layout of the graphs built from now on
+    (RECORDS_AUTO, RECORDS_COMPACT or RECORDS_WIDE); estimates are identical under each."""
+    check(lib().zg_set_record_layout(layout))
 
 
 def read_bandwidth(nbytes, reps=200, cuda_stream=None):

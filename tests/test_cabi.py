@@ -27,7 +27,7 @@ def test_every_declared_symbol_is_exported():
 def test_struct_layouts():
     assert ctypes.sizeof(Z.Counters) == 8 * 3 + 4 * 2 + 8 * 5 + 8 * 4
     assert Z.TRACE_DTYPE.itemsize == 4 * 6 + 8 + 8 * 3 + 8 * 16 * 3
-    assert ctypes.sizeof(Z.GraphMeta) == 4 * 2 + 8 * 4
+    assert ctypes.sizeof(Z.GraphMeta) == 4 * 2 + 8 * 4 + 4 * 2
 
 
 def test_version_and_errors_without_device():

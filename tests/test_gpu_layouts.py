@@ -1,0 +1,108 @@
+"""The two per-edge record layouts (zg_set_record_layout): compact (16 bytes, steps read vertex
+offsets) and wide (32 bytes: each edge's slot and predecessor count in both endpoint lists).
+Every program, the fused 3-motif, batches, derived graphs and exports give identical results
+under both, sample for sample; the parity tests against the oracle run on the layout the
+automatic choice picks for their (small) graphs, so equality here carries them to the other."""
+import numpy as np
+import pytest
+
+import zgraph as Z
+
+pytestmark = pytest.mark.gpu
+
+STAR = (5, [(0, 1), (0, 2), (0, 3), (0, 4)])
+HOUSE = (5, [(0, 1), (0, 2), (1, 2), (1, 3), (2, 4), (3, 4)])
+TRI = (3, [(0, 1), (0, 2), (1, 2)])
+
+
+def _same(a, b, what):
+    assert (a.samples, a.hits, a.fails, a.overflow) == (b.samples, b.hits, b.fails, b.overflow), what
+    assert [int(x) for x in a.sum_num] == [int(x) for x in b.sum_num], what
+    assert a.estimate == b.estimate and a.sum_w == b.sum_w, what
+    assert abs(a.sum_w2 - b.sum_w2) <= 1e-12 * max(1.0, abs(b.sum_w2)), what
+
+
+def _build(layout, fn):
+    Z.set_record_layout(layout)
+    try:
+        return fn()
+    finally:
+        Z.set_record_layout(Z.RECORDS_AUTO)
+
+
+@pytest.fixture(scope="module")
+def pair():
+    Z.init(0)
+    e = Z.gen_rmat(12, 10, seed=17)
+    w = Z.gen_weights(len(e), 100, seed=4)
+    mk = lambda: Z.Graph.from_edges(e, 1 << 12, weights=w, shuffle_seed=5)  # noqa: E731
+    return _build(Z.RECORDS_COMPACT, mk), _build(Z.RECORDS_WIDE, mk)
+
+
+def test_meta_and_exports(pair):
+    c, wd = pair
+    assert c.meta().record_bytes == 16 and wd.meta().record_bytes == 32
+    assert wd.meta().device_bytes - c.meta().device_bytes == 16 * c.num_local_edges
+    dc, dw = c.download(), wd.download()
+    for k in ("edges", "weights", "offsets", "adj_e", "adj_n", "suffix"):
+        assert np.array_equal(dc[k], dw[k]), k
+
+
+PROGRAMS = [("triangle", Z.PROG_TRIANGLE, 0, None), ("four_clique", Z.PROG_FOUR_CLIQUE, 0, None),
+            ("four_clique_unbiased", Z.PROG_FOUR_CLIQUE_UNBIASED, 0, None),
+            ("three_chain", Z.PROG_THREE_CHAIN, 0, None), ("four_chain", Z.PROG_FOUR_CHAIN, 0, None),
+            ("chain5", Z.PROG_CHAIN, 5, None), ("chain7", Z.PROG_CHAIN, 7, None),
+            ("star5", Z.PROG_PATTERN, 0, STAR), ("house5", Z.PROG_PATTERN, 0, HOUSE),
+            ("triangle_pattern", Z.PROG_PATTERN, 0, TRI)]
+
+
+@pytest.mark.parametrize("name,kind,param,pat", PROGRAMS, ids=[p[0] for p in PROGRAMS])
+def test_programs_identical(pair, name, kind, param, pat):
+    c, wd = pair
+    p = Z.Program(kind, param, pat)
+    for n, seed, first in ((1 << 20, 3, 0), (77777, 9, 1 << 33)):
+        _same(p.run(c, n, seed, stream_id=4, first_sample=first), p.run(wd, n, seed, stream_id=4, first_sample=first),
+              (name, n))
+    tc, tw = p.run_debug(c, 4096, 11), p.run_debug(wd, 4096, 11)
+    for k in ("ndraws", "hit", "fail", "shift", "sectors", "w", "num", "lo", "hi", "val"):
+        assert np.array_equal(tc[k], tw[k]), (name, k)
+
+
+def test_three_motif_and_batch_identical(pair):
+    c, wd = pair
+    for a, b in zip(Z.run_three_motif(c, 1 << 20, 1 << 19, 7, 1, 2), Z.run_three_motif(wd, 1 << 20, 1 << 19, 7, 1, 2)):
+        _same(a, b, "three_motif")
+    qs = [{"kind": Z.PROG_TRIANGLE, "n": 300000, "seed": 1, "pred_op": Z.PRED_GE, "t0": 40},
+          {"kind": Z.QUERY_THREE_MOTIF, "n": 200000, "seed": 2},
+          {"kind": Z.PROG_FOUR_CHAIN, "n": 250000, "seed": 3, "first_sample": 99},
+          {"kind": Z.PROG_PATTERN, "program": Z.Program(Z.PROG_PATTERN, pattern=STAR), "n": 100000, "seed": 4}]
+    rc = _build(Z.RECORDS_COMPACT, lambda: Z.Batch(c, max_queries=8).run(qs))
+    rw = _build(Z.RECORDS_WIDE, lambda: Z.Batch(wd, max_queries=8).run(qs))
+    for q, (a, a2), (b, b2) in zip(qs, rc, rw):
+        _same(a, b, q)
+        _same(a2, b2, q)
+
+
+def test_derived_graphs_and_exact_counts(pair):
+    c, wd = pair
+    fc = _build(Z.RECORDS_COMPACT, lambda: c.filter(Z.PRED_LT, 50, shuffle_seed=8))
+    fw = _build(Z.RECORDS_WIDE, lambda: wd.filter(Z.PRED_LT, 50, shuffle_seed=8))
+    assert fc.meta().record_bytes == 16 and fw.meta().record_bytes == 32
+    assert np.array_equal(fc.download()["edges"], fw.download()["edges"])
+    p = Z.Program(Z.PROG_FOUR_CLIQUE)
+    _same(p.run(fc, 1 << 19, 5), p.run(fw, 1 << 19, 5), "filtered")
+    for kind in (Z.EXACT_TRIANGLE, Z.EXACT_WEDGE, Z.EXACT_FOUR_CLIQUE):
+        assert c.exact_count(kind) == wd.exact_count(kind), kind
+    e_c = _build(Z.RECORDS_COMPACT, lambda: Z.elp_plain(c, Z.Program(Z.PROG_TRIANGLE), 0.05, 0.95, 3))
+    e_w = _build(Z.RECORDS_WIDE, lambda: Z.elp_plain(wd, Z.Program(Z.PROG_TRIANGLE), 0.05, 0.95, 3))
+    assert e_c.n_required == e_w.n_required
+
+
+def test_device_generator_layouts():
+    Z.init(0)
+    gc = _build(Z.RECORDS_COMPACT, lambda: Z.Graph.gen_chung_lu(30000, 2.4, 10.0, seed=3, sampling_only=True))
+    gw = _build(Z.RECORDS_WIDE, lambda: Z.Graph.gen_chung_lu(30000, 2.4, 10.0, seed=3, sampling_only=True))
+    p = Z.Program(Z.PROG_FOUR_CHAIN)
+    _same(p.run(gc, 1 << 20, 2), p.run(gw, 1 << 20, 2), "chung-lu")
+    with pytest.raises(Z.ZgError):
+        Z.set_record_layout(3)
