@@ -610,8 +610,9 @@ __device__ void prog_four_chain(const ZgDevGraph& g, Ctx& c, Res& r) {
   edge_rec(g, e0, q, qp);
   const uint32_t a = q.x, b = q.y;
   if (DBG) c.sectors += 1;
-  // The three programs share one chain of dependent loads (edge record, anchor offset, e1,
-  // second anchor's offset, e2) so a warp whose lanes drew different programs walks it once.
+  // The three programs share one chain of dependent loads (edge record, [anchor offset,] e1,
+  // [e1's record and] the second anchor's offset, e2; bracketed reads: compact layout or some
+  // programs only) so a warp whose lanes drew different programs walks it once.
   //   sel 1, 2: vertices [a, b] give e1; its far end nw gives e2 (edges [e0, e1] resp. [e0])
   //   sel 3:    vertices [a] give e1; vertices [b] give e2 (edges [e0])
   const bool split = sel == 3;
