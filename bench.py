@@ -171,7 +171,7 @@ def cpu_baseline(wl, edges, nv, threads, target_s=12.0):
                          {k: round(v) for k, v in rates.items()})}
 
 
-def time_to_bound(Z, g, names, acc, eps=0.01, conf=0.95, cap=1 << 35, coverage_queries=40):
+def time_to_bound(Z, g, names, acc, eps=0.01, conf=0.95, cap=1 << 37, coverage_queries=40):
     """Time from query submission (graph resident) to an answer whose empirical 95 % half-width is
     <= 1 % of the estimate: plain ErrorProfile sizing vs the learned network, same judge (zg_query).
     For 4-cliques the unbiased canonical-path program runs: the reference's estimator is biased (it
