@@ -36,6 +36,36 @@ int zg_num_sms() {
   return sms;
 }
 
+namespace {
+std::mutex g_pool_mu;
+cudaMemPool_t g_pool[64];
+}  // namespace
+
+cudaError_t zg_malloc_async(void** p, size_t bytes, cudaStream_t s) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) return cudaMallocAsync(p, bytes, s);
+  cudaMemPool_t pool;
+  {
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    if (!g_pool[dev]) {
+      cudaMemPoolProps props = {};
+      props.allocType = cudaMemAllocationTypePinned;
+      props.location.type = cudaMemLocationTypeDevice;
+      props.location.id = dev;
+      if ((e = cudaMemPoolCreate(&g_pool[dev], &props)) != cudaSuccess) {
+        g_pool[dev] = nullptr;
+        return e;
+      }
+      uint64_t keep = 256ull << 20;
+      cudaMemPoolSetAttribute(g_pool[dev], cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    pool = g_pool[dev];
+  }
+  return cudaMallocFromPoolAsync(p, bytes, pool, s);
+}
+
 extern "C" int zg_version(void) { return 2; }
 
 extern "C" const char* zg_last_error(void) { return g_err; }

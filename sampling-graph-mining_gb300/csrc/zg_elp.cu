@@ -142,7 +142,7 @@ extern "C" int zg_run_groups(const zg_graph* g, const zg_program* p, uint64_t n_
     return zg_set_error(ZG_ERR_INVALID_ARG, "zg_run_groups: invalid argument"), ZG_ERR_INVALID_ARG;
   cudaStream_t s = (cudaStream_t)cuda_stream;
   double* d = nullptr;
-  ZG_CUDA(cudaMallocAsync((void**)&d, sizeof(double) * (n_groups ? n_groups : 1), s));
+  ZG_CUDA(zg_malloc_async((void**)&d, sizeof(double) * (n_groups ? n_groups : 1), s));
   int rc = zg_launch_groups(g, p, n_groups, group_size, first_sample, seed, stream_id, s, d);
   cudaError_t ce = cudaSuccess;
   if (rc == ZG_OK && n_groups)

@@ -221,3 +221,9 @@ int zg_check_cuda(cudaError_t e, const char* what);
   } while (0)
 
 int zg_num_sms();
+
+// Stream-ordered allocation of per-call scratch from the library's own memory pool on the current
+// device.  The pool keeps up to 256 MiB of freed blocks across synchronisations (the device's
+// default pool returns them at every synchronisation, and mapping them again cost ~0.1 ms per
+// call); free with cudaFreeAsync.
+cudaError_t zg_malloc_async(void** p, size_t bytes, cudaStream_t s);

@@ -470,7 +470,7 @@ extern "C" int zg_graph_features(const zg_graph* g, const zg_program* p, uint64_
   if (!g || !p || !f) return zg_set_error(ZG_ERR_INVALID_ARG, "zg_graph_features: null argument"), ZG_ERR_INVALID_ARG;
   cudaStream_t s = (cudaStream_t)cuda_stream;
   DegStats* d = nullptr;
-  ZG_CUDA(cudaMallocAsync((void**)&d, sizeof(DegStats), s));
+  ZG_CUDA(zg_malloc_async((void**)&d, sizeof(DegStats), s));
   cudaMemsetAsync(d, 0, sizeof(DegStats), s);
   k_deg_stats<<<zg_num_sms() * 4, 256, 0, s>>>(g->d, d);
   DegStats h;

@@ -490,7 +490,7 @@ extern "C" int zg_run(const zg_graph* g, const zg_program* p, uint64_t n, uint64
   int grid = grid_for_kind(p->kind, g->wide != 0);
   if ((uint64_t)grid > maxg) grid = (int)(maxg ? maxg : 1);
   ZgPartial* parts = nullptr;
-  ZG_CUDA(cudaMallocAsync((void**)&parts, sizeof(ZgPartial) * (grid + 1), s));
+  ZG_CUDA(zg_malloc_async((void**)&parts, sizeof(ZgPartial) * (grid + 1), s));
   launch_sample(g, p, n, first_sample, seed, stream_id, s, parts, grid);
   k_finalize<<<1, kBlock, 0, s>>>(parts, grid, parts + grid);
   ZgPartial h;
@@ -515,7 +515,7 @@ extern "C" int zg_run_async(const zg_graph* g, const zg_program* p, uint64_t n, 
   int grid = grid_for_kind(p->kind, g->wide != 0);
   if ((uint64_t)grid > maxg) grid = (int)(maxg ? maxg : 1);
   ZgPartial* parts = nullptr;
-  ZG_CUDA(cudaMallocAsync((void**)&parts, sizeof(ZgPartial) * grid, s));
+  ZG_CUDA(zg_malloc_async((void**)&parts, sizeof(ZgPartial) * grid, s));
   launch_sample(g, p, n, first_sample, seed, stream_id, s, parts, grid);
   k_finalize<<<1, kBlock, 0, s>>>(parts, grid, (ZgPartial*)d_result);
   cudaFreeAsync(parts, s);
@@ -557,7 +557,7 @@ extern "C" int zg_tune(const zg_graph* g, const zg_program* p, uint64_t probe_sa
   int grid_max = 0;
   for (int v = 0; v < kVariants; ++v) grid_max = std::max(grid_max, grid_for_variant(p->kind, v, g->wide != 0));
   ZgPartial* parts = nullptr;
-  ZG_CUDA(cudaMallocAsync((void**)&parts, sizeof(ZgPartial) * (grid_max + 1), s));
+  ZG_CUDA(zg_malloc_async((void**)&parts, sizeof(ZgPartial) * (grid_max + 1), s));
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -647,11 +647,11 @@ static int run_motif(const zg_graph* g, uint64_t n_chain, uint64_t n_tri, uint64
                  : std::min<int>(grid_of(k_three_motif<false>), (int)std::max<uint64_t>(1, (n + kBlock - 1) / kBlock));
   ZgPartial* parts = nullptr;
   zg_sample_trace *dtc = nullptr, *dtt = nullptr;
-  ZG_CUDA(cudaMallocAsync((void**)&parts, sizeof(ZgPartial) * (2 * grid + 2), s));
+  ZG_CUDA(zg_malloc_async((void**)&parts, sizeof(ZgPartial) * (2 * grid + 2), s));
   cudaError_t ce = cudaSuccess;
   if (dbg) {
-    ce = cudaMallocAsync((void**)&dtc, sizeof(zg_sample_trace) * (n_chain ? n_chain : 1), s);
-    if (ce == cudaSuccess) ce = cudaMallocAsync((void**)&dtt, sizeof(zg_sample_trace) * (n_tri ? n_tri : 1), s);
+    ce = zg_malloc_async((void**)&dtc, sizeof(zg_sample_trace) * (n_chain ? n_chain : 1), s);
+    if (ce == cudaSuccess) ce = zg_malloc_async((void**)&dtt, sizeof(zg_sample_trace) * (n_tri ? n_tri : 1), s);
     if (ce == cudaSuccess) ce = cudaMemsetAsync(dtc, 0, sizeof(zg_sample_trace) * (n_chain ? n_chain : 1), s);
     if (ce == cudaSuccess) ce = cudaMemsetAsync(dtt, 0, sizeof(zg_sample_trace) * (n_tri ? n_tri : 1), s);
   }
