@@ -228,11 +228,11 @@ int zg_run_noalloc(const zg_graph* g, const zg_program* p, uint64_t n, uint64_t 
                    uint64_t seed, uint32_t stream_id, void* cuda_stream, void* d_result);
 /* Autotuner (no counterpart in the reference, whose thread count comes from libnuma).  Each
  * program kind has ZG_VARIANTS launch shapes: the sampling kernel compiled for
- * min-blocks-per-SM 1, 2, 3, 4, 6, 8 (register caps 255/128/80/64/40/32) with a grid of
+ * min-blocks-per-SM 1, 2, 3, 4, 5, 6, 8 (register caps 255/128/80/64/48/40/32) with a grid of
  * occupancy x SM count.  zg_tune times every variant on g (probe_samples estimators, best of 3)
  * and keeps the fastest for this device and kind; ms_per_variant (may be NULL) receives
  * ZG_VARIANTS timings.  zg_set_variant / zg_get_variant fix or read the choice. */
-#define ZG_VARIANTS 6
+#define ZG_VARIANTS 7
 int zg_tune(const zg_graph* g, const zg_program* p, uint64_t probe_samples, void* cuda_stream,
             int* best_variant, float* ms_per_variant);
 int zg_set_variant(int kind, int variant);

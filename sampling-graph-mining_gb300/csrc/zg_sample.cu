@@ -355,9 +355,9 @@ int grid_of(K kernel) {
   return per_sm * zg_num_sms();
 }
 
-// Launch-shape variants: __launch_bounds__ min-blocks (register caps 255/128/80/64/40/32).
-constexpr int kVariants = 6;
-constexpr int kMinBlocks[kVariants] = {1, 2, 3, 4, 6, 8};
+// Launch-shape variants: __launch_bounds__ min-blocks (register caps 255/128/80/64/48/40/32).
+constexpr int kVariants = 7;
+constexpr int kMinBlocks[kVariants] = {1, 2, 3, 4, 5, 6, 8};
 typedef void (*SampleKernel)(ZgDevGraph, ZgProgParams, uint64_t, uint64_t, uint64_t, uint32_t, ZgPartial*);
 
 template <int KIND, bool WIDE>
@@ -367,7 +367,8 @@ SampleKernel kernel_variant(int v) {
     case 1: return k_sample<KIND, 2, WIDE>;
     case 2: return k_sample<KIND, 3, WIDE>;
     case 3: return k_sample<KIND, 4, WIDE>;
-    case 4: return k_sample<KIND, 6, WIDE>;
+    case 4: return k_sample<KIND, 5, WIDE>;
+    case 5: return k_sample<KIND, 6, WIDE>;
     default: return k_sample<KIND, 8, WIDE>;
   }
 }

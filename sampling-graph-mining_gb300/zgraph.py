@@ -38,6 +38,7 @@ RECORDS_AUTO, RECORDS_COMPACT, RECORDS_WIDE = 0, 1, 2
 BATCH_MAX_QUERIES, BATCH_MAX_CHUNKS = 65536, 65536
 NO_SHUFFLE = 0xFFFFFFFFFFFFFFFF
 MAX_DRAWS = 16
+VARIANTS = 7  # ZG_VARIANTS: launch shapes per program kind
 
 
 class ZgError(RuntimeError):
@@ -503,7 +504,7 @@ class Program:
         best = C.c_int(0)
         ms = (C.c_float * 8)()
         check(lib().zg_tune(graph.handle, self._h, probe_samples, cuda_stream, C.byref(best), ms))
-        return best.value, [float(ms[i]) for i in range(6)]
+        return best.value, [float(ms[i]) for i in range(VARIANTS)]
 
     def set_variant(self, variant):
         """zg_set_variant: fix this program kind's launch shape (0..ZG_VARIANTS-1)."""

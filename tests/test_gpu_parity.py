@@ -256,14 +256,14 @@ def test_launch_variants_agree(graphs, name, kind, param, pattern):
     g = Z.Graph.from_edges(e, nv)
     p = Z.Program(kind, param, pattern)
     base = None
-    for v in range(6):
+    for v in range(Z.VARIANTS):
         Z.check(L.zg_set_variant(kind, v))
         c = p.run(g, 1 << 19, 123)
         got = (c.samples, c.hits, c.fails, _sums(c))
         assert base is None or got == base, (name, v)
         base = got
     best, ms = p.tune(g, 1 << 18)
-    assert 0 <= best < 6 and all(t > 0 for t in ms)
+    assert 0 <= best < Z.VARIANTS and len(ms) == Z.VARIANTS and all(t > 0 for t in ms)
     assert p.variant()["variant"] == best
 
 
