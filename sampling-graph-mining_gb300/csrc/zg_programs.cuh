@@ -929,6 +929,62 @@ __device__ __forceinline__ void acc_add(Acc& a, const Res& r, uint32_t den) {
   a.sw2 = fma(w, w, a.sw2);
 }
 
+// One thread's 320-bit sum and variance term kept in shared memory (slot threadIdx.x of arrays
+// of BLOCK entries) instead of registers: a latency-bound sampling loop then fits a smaller
+// register budget, i.e. more resident warps and more loads in flight.  Each thread adds its hits
+// in the same order as with acc_add, so the results are identical.
+template <int BLOCK>
+struct AccSlots {
+  unsigned long long s[4][BLOCK];
+  double sw2[BLOCK];
+};
+
+template <int BLOCK>
+__device__ __forceinline__ void acc_slots_init(AccSlots<BLOCK>& sl) {
+  const int t = threadIdx.x;
+  sl.s[0][t] = sl.s[1][t] = sl.s[2][t] = sl.s[3][t] = 0;
+  sl.sw2[t] = 0.0;
+}
+
+template <int BLOCK>
+__device__ __forceinline__ void acc_add_slots(Acc& a, AccSlots<BLOCK>& sl, const Res& r, uint32_t den) {
+  a.samples++;
+  a.fails += r.fail;
+  if (!r.hit) return;
+  a.hits++;
+  a.ovf += r.ovf;
+  uint32_t sh = den - r.shift;  // < 64
+  uint64_t v0 = r.num.l[0] << sh;
+  uint64_t v1 = sh ? (r.num.l[1] << sh) | (r.num.l[0] >> (64 - sh)) : r.num.l[1];
+  uint64_t v2 = sh ? (r.num.l[2] << sh) | (r.num.l[1] >> (64 - sh)) : r.num.l[2];
+  uint64_t v3 = sh ? (r.num.l[2] >> (64 - sh)) : 0;
+  const int t = threadIdx.x;
+  unsigned long long s0 = sl.s[0][t], s1 = sl.s[1][t], s2 = sl.s[2][t], s3 = sl.s[3][t];
+  asm("add.cc.u64 %0, %0, %4;\n\t"
+      "addc.cc.u64 %1, %1, %5;\n\t"
+      "addc.cc.u64 %2, %2, %6;\n\t"
+      "addc.u64 %3, %3, %7;"
+      : "+l"(s0), "+l"(s1), "+l"(s2), "+l"(s3)
+      : "l"(v0), "l"(v1), "l"(v2), "l"(v3));
+  sl.s[0][t] = s0;
+  sl.s[1][t] = s1;
+  sl.s[2][t] = s2;
+  sl.s[3][t] = s3;
+  double w = u192_scaled_to_double(r.num, r.shift);
+  sl.sw2[t] = fma(w, w, sl.sw2[t]);
+}
+
+// The slots back into the thread's accumulator (after its loop).
+template <int BLOCK>
+__device__ __forceinline__ void acc_from_slots(Acc& a, const AccSlots<BLOCK>& sl) {
+  const int t = threadIdx.x;
+  a.s[0] = sl.s[0][t];
+  a.s[1] = sl.s[1][t];
+  a.s[2] = sl.s[2][t];
+  a.s[3] = sl.s[3][t];
+  a.sw2 = sl.sw2[t];
+}
+
 template <int BLOCK>
 __device__ void block_reduce_store(Acc& a, ZgPartial* out) {
   unsigned long long v[14];
