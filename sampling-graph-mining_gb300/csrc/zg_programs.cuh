@@ -521,6 +521,13 @@ __device__ void prog_four_clique(const ZgDevGraph& g, Ctx& c, Res& r) {
   // (that suffix holds edge ids in [id0 + 1, m - 1])
   const uint32_t base_oth = after_edge(g, q, qp, !s1b);
   const uint32_t end_own = base_own + suf_own, end_oth = base_oth + suf_oth;
+  if (!DBG && p0.cand == ZG_HASH_EMPTY) {
+    // a miss or a failure, nothing else: the step has a candidate unless c has no entries after
+    // e1 and the other endpoint's largest id after e0 (its list's last entry) is below id1 + 1
+    const bool any = (a1 == 1 && ac.suf != 0) || (suf_oth != 0 && ZG_LDG(&g.adj_e[end_oth - 1]).y >= mv);
+    r.fail = !any;
+    return;
+  }
   uint32_t lo = lb_eid(g.adj_e, base_oth, end_oth, mv, (uint32_t)e0 + 1, (uint32_t)(g.m - 1));
   uint32_t lbA = s1b ? lo : idx1 + 1, lbB = s1b ? idx1 + 1 : lo;
   uint64_t lenA = (s1b ? end_oth : end_own) - lbA, lenB = (s1b ? end_own : end_oth) - lbB;
@@ -532,7 +539,6 @@ __device__ void prog_four_clique(const ZgDevGraph& g, Ctx& c, Res& r) {
     r.fail = true;
     return;
   }
-  if (!DBG && p0.cand == ZG_HASH_EMPTY) return;  // (x0, c) absent: a miss
   if (DBG) c.sectors += 1;
   uint64_t r2 = c.take(w2, 0, S2 - 1);
   int s2;
