@@ -601,10 +601,17 @@ __device__ void prog_four_clique(const ZgDevGraph& g, Ctx& c, Res& r) {
 }
 
 // ---- FourChain: applications/FourChain.cpp:24-124 ----------------------------------------
+// sel_known: the program draw (1..3) when the caller has already drawn it, else 0.
 template <bool DBG>
-__device__ void prog_four_chain(const ZgDevGraph& g, Ctx& c, Res& r) {
+__device__ void prog_four_chain(const ZgDevGraph& g, Ctx& c, Res& r, uint32_t sel_known = 0) {
   const uint64_t w2 = c.word(2), w3 = c.word(3);  // Philox work of the later draws, up front
-  uint64_t sel = c.draw(1, 3);
+  uint64_t sel;
+  if (sel_known) {
+    sel = sel_known;
+    ++c.nd;
+  } else {
+    sel = c.draw(1, 3);
+  }
   res_mul(r, 3);
   if (g.m == 0) {
     r.fail = true;
