@@ -622,6 +622,24 @@ __device__ void prog_four_chain(const ZgDevGraph& g, Ctx& c, Res& r, uint32_t se
   uint4 q, qp;
   edge_rec(g, e0, q, qp);
   const uint32_t a = q.x, b = q.y;
+  if (!DBG && sel == 3) {
+    // vertices [a] give e1, vertices [b] give e2: both entries' addresses follow from e0's record,
+    // so their loads go out together (the same counters as the shared chain below)
+    const uint64_t S1 = q.z, S2 = q.w;
+    if (S1 == 0 || S2 == 0) {
+      r.fail = true;
+      return;
+    }
+    const uint64_t r1 = c.take(w2, 0, S1 - 1), r2 = c.take(w3, 0, S2 - 1);
+    const uint2 e1 = ZG_LDG(&g.adj_e[after_edge(g, q, qp, false) + (uint32_t)r1]);
+    const uint2 e2 = ZG_LDG(&g.adj_e[after_edge(g, q, qp, true) + (uint32_t)r2]);
+    res_mul(r, S1);
+    if (e1.x == a) r.shift++;
+    res_mul(r, S2);
+    if (e2.x == b) r.shift++;
+    r.hit = !(b == a || b == e1.x) && !(e2.x == a || e2.x == e1.x);
+    return;
+  }
   if (DBG) c.sectors += 1;
   // The three programs share one chain of dependent loads (edge record, [anchor offset,] e1,
   // [e1's record and] the second anchor's offset, e2; bracketed reads: compact layout or some
