@@ -288,13 +288,15 @@ int build_graph(const uint2* d_coo, const uint32_t* d_w_in, uint64_t m, uint32_t
   uint64_t n2 = 2 * m;
   g->wide = wide_records(m, nv);
   const size_t rec_bytes = (g->wide ? sizeof(ZgRec) : sizeof(uint4)) * m;
-  // adj_e and off32 share one allocation
-  g->hot_bytes = sizeof(uint2) * n2 + sizeof(uint32_t) * ((size_t)nv + 1);
+  // adj_e, 8 entries of slack (lb_eid_win's windows may read up to 7 entries past the last one),
+  // and off32 share one allocation
+  const size_t adj_bytes = sizeof(uint2) * (n2 + 8);
+  g->hot_bytes = adj_bytes + sizeof(uint32_t) * ((size_t)nv + 1);
   if ((rc = dev_alloc((char**)&g->hot, g->hot_bytes)) || (rc = dev_alloc((char**)&g->rec, rec_bytes)) ||
       (rc = dev_alloc(&g->off, (size_t)nv + 1)) || (!sampling_only && (rc = dev_alloc(&g->adj_n, n2))))
     return fail(rc);
   g->adj_e = (uint2*)g->hot;
-  g->off32 = (uint32_t*)((char*)g->hot + sizeof(uint2) * n2);
+  g->off32 = (uint32_t*)((char*)g->hot + adj_bytes);
   if (d_w_in) {
     if ((rc = dev_alloc(&g->w, m))) return fail(rc);
     if (m) {

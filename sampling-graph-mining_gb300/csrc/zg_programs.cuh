@@ -103,6 +103,66 @@ __device__ __forceinline__ uint32_t lb_eid(const uint2* __restrict__ adj, uint32
   return lo + below;
 }
 
+// The edge ids of adjacency entries s .. s+7 (s a multiple of 4: two 32-byte-aligned 256-bit
+// loads).  The build leaves 8 entries of slack after adj_e, so s < 2m never reads past it.
+__device__ __forceinline__ void ld_ids8(const uint2* adj, uint32_t s, uint32_t (&id)[8]) {
+  unsigned long long a0, a1, a2, a3, b0, b1, b2, b3;
+  asm("ld.global.nc.v4.u64 {%0, %1, %2, %3}, [%4];" : "=l"(a0), "=l"(a1), "=l"(a2), "=l"(a3) : "l"(adj + s));
+  asm("ld.global.nc.v4.u64 {%0, %1, %2, %3}, [%4];" : "=l"(b0), "=l"(b1), "=l"(b2), "=l"(b3) : "l"(adj + s + 4));
+  id[0] = (uint32_t)(a0 >> 32);
+  id[1] = (uint32_t)(a1 >> 32);
+  id[2] = (uint32_t)(a2 >> 32);
+  id[3] = (uint32_t)(a3 >> 32);
+  id[4] = (uint32_t)(b0 >> 32);
+  id[5] = (uint32_t)(b1 >> 32);
+  id[6] = (uint32_t)(b2 >> 32);
+  id[7] = (uint32_t)(b3 >> 32);
+}
+
+// lb_eid with a window of 8 entries (two sectors) read around each interpolated estimate: the
+// bound is found inside the window, or the window and every entry on its wrong side drop out, so
+// short lists take one dependent read.  Costs registers: used where warps run one search each.
+__device__ __forceinline__ uint32_t lb_eid_win(const uint2* __restrict__ adj, uint32_t lo, uint32_t hi, uint32_t key,
+                                               uint32_t vlo, uint32_t vhi) {
+  for (int it = 0; lo < hi; ++it) {
+    if (key <= vlo) return lo;
+    if (key > vhi) return hi;
+    const uint32_t n = hi - lo;
+    uint32_t c;
+    if (it < 8) {
+      float f = __fdividef((float)(key - vlo), (float)(vhi - vlo) + 1.0f);
+      uint32_t est = (uint32_t)(f * (float)n);
+      c = lo + (est < n ? est : n - 1);
+    } else {
+      c = lo + (n >> 1);
+    }
+    const uint32_t s = (c >= 3 ? c - 3 : 0u) & ~3u;  // window [s, s + 8) holds c
+    uint32_t id[8];
+    ld_ids8(adj, s, id);
+    const uint32_t wl = s > lo ? s : lo, wh = s + 8 < hi ? s + 8 : hi;  // its part of [lo, hi), not empty
+    uint32_t below = 0, idf = 0, idl = 0;
+#pragma unroll
+    for (uint32_t i = 0; i < 8; ++i) {
+      const uint32_t p = s + i;
+      below += p >= wl && p < wh && id[i] < key;
+      idf = p == wl ? id[i] : idf;
+      idl = p == wh - 1 ? id[i] : idl;
+    }
+    if (below == 0) {  // the bound is at or before the window
+      if (wl == lo) return lo;
+      hi = wl;
+      vhi = idf - 1;  // idf >= key > vlo >= 0
+    } else if (below == wh - wl) {  // the bound is after the window
+      if (wh == hi) return hi;
+      lo = wh;
+      vlo = idl + 1;
+    } else {
+      return wl + below;
+    }
+  }
+  return lo;
+}
+
 // Does edge (x,y) exist with edge id >= min_valid?  conditional_close's question
 // (src/ZGraphInstance.cpp:372-407): the pattern edges still to close join two sampled vertices,
 // so "found in some sampled vertex's list with id >= min_valid" is "edge (x,y) exists with such
@@ -678,7 +738,7 @@ __device__ void prog_four_chain(const ZgDevGraph& g, Ctx& c, Res& r, uint32_t se
     lb2 = a1v.pos + 1;                          // sel 1: min_valid = id1 + 1
     end2 = lb2 + a1v.suf;
     if (sel == 2)  // min_valid = id0 + 1, at or before e1's own slot in v2's list
-      lb2 = lb_eid(g.adj_e, edge_at_start(g, a1v, v2), lb2, (uint32_t)e0 + 1, 0u, e1.y);
+      lb2 = lb_eid_win(g.adj_e, edge_at_start(g, a1v, v2), lb2, (uint32_t)e0 + 1, 0u, e1.y);
   }
   const uint64_t S2 = (uint64_t)(end2 - lb2);
   if (DBG) c.sectors += model_anchor(g, v2);
