@@ -392,8 +392,9 @@ int zg_mlp_grad(const zg_mlp* net, const float* X, const float* Y, uint32_t n_ro
                 float* loss);
 /* Predictions for raw features, de-normalised: Y[n_rows][2]. */
 int zg_mlp_predict(const zg_mlp* net, const float* X, uint32_t n_rows, float* Y);
-/* The 16 features of a query: degree statistics of g (one device pass), the program's pattern
- * class, and a pilot run of pilot_samples estimators (0: 2^16). */
+/* The 16 features of a query: degree statistics of g (one device pass on the first call for g,
+ * then kept with the graph), the program's pattern class, and a pilot run of pilot_samples
+ * estimators (0: 2^16).  Not to be called for the same graph from two threads at once. */
 int zg_graph_features(const zg_graph* g, const zg_program* p, uint64_t pilot_samples,
                       uint64_t seed, void* cuda_stream, float* features);
 

@@ -99,6 +99,9 @@ struct zg_graph {
   uint64_t num_edges;   // Graph::num_edges metadata
   uint64_t max_degree;  // Graph::max_degree metadata
   uint64_t bytes;
+  // degree statistics of the learned profile's features (zg_graph_features), computed on first use
+  mutable bool deg_stats_ready;
+  mutable double deg_stats[7];  // s1, s2, s3, emin, esum, non-isolated vertices, max degree
 };
 
 // Program descriptor (host copy; device parameters are passed by value).

@@ -415,7 +415,10 @@ struct DegStats {
   unsigned long long nz, maxd;
 };
 
-__global__ void k_deg_stats(ZgDevGraph g, DegStats* __restrict__ out) {
+// Per-block degree statistics (no atomics: every block writes its own partial, summed on the host
+// in block order, so the features are reproducible bit for bit).
+constexpr int kStatBlock = 256;
+__global__ void __launch_bounds__(kStatBlock) k_deg_stats(ZgDevGraph g, DegStats* __restrict__ parts) {
   double s1 = 0, s2 = 0, s3 = 0, emin = 0, esum = 0;
   unsigned long long nz = 0, maxd = 0;
   uint64_t tid = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x, stride = (uint64_t)gridDim.x * blockDim.x;
@@ -435,13 +438,68 @@ __global__ void k_deg_stats(ZgDevGraph g, DegStats* __restrict__ out) {
     emin += fmin(du, dv);
     esum += du + dv;
   }
-  atomicAdd(&out->s1, s1);
-  atomicAdd(&out->s2, s2);
-  atomicAdd(&out->s3, s3);
-  atomicAdd(&out->emin, emin);
-  atomicAdd(&out->esum, esum);
-  atomicAdd(&out->nz, nz);
-  atomicMax(&out->maxd, maxd);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+    s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+    s3 += __shfl_xor_sync(0xffffffffu, s3, o);
+    emin += __shfl_xor_sync(0xffffffffu, emin, o);
+    esum += __shfl_xor_sync(0xffffffffu, esum, o);
+    nz += __shfl_xor_sync(0xffffffffu, nz, o);
+    maxd = max(maxd, __shfl_xor_sync(0xffffffffu, maxd, o));
+  }
+  __shared__ DegStats ws[kStatBlock / 32];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) ws[warp] = DegStats{s1, s2, s3, emin, esum, nz, maxd};
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    DegStats t = ws[0];
+    for (int w = 1; w < kStatBlock / 32; ++w) {
+      t.s1 += ws[w].s1;
+      t.s2 += ws[w].s2;
+      t.s3 += ws[w].s3;
+      t.emin += ws[w].emin;
+      t.esum += ws[w].esum;
+      t.nz += ws[w].nz;
+      t.maxd = max(t.maxd, ws[w].maxd);
+    }
+    parts[blockIdx.x] = t;
+  }
+}
+
+// The graph's degree statistics, computed once per graph (the graph is immutable).
+int deg_stats(const zg_graph* g, cudaStream_t s) {
+  if (g->deg_stats_ready) return ZG_OK;
+  const int grid = zg_num_sms() * 4;
+  DegStats* d = nullptr;
+  ZG_CUDA(zg_malloc_async((void**)&d, sizeof(DegStats) * grid, s));
+  k_deg_stats<<<grid, kStatBlock, 0, s>>>(g->d, d);
+  std::vector<DegStats> h(grid);
+  cudaError_t e = cudaMemcpyAsync(h.data(), d, sizeof(DegStats) * grid, cudaMemcpyDeviceToHost, s);
+  cudaFreeAsync(d, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) return zg_check_cuda(e, "graph features");
+  DegStats t = h[0];
+  for (int b = 1; b < grid; ++b) {
+    t.s1 += h[b].s1;
+    t.s2 += h[b].s2;
+    t.s3 += h[b].s3;
+    t.emin += h[b].emin;
+    t.esum += h[b].esum;
+    t.nz += h[b].nz;
+    t.maxd = std::max(t.maxd, h[b].maxd);
+  }
+  double* out = g->deg_stats;
+  out[0] = t.s1;
+  out[1] = t.s2;
+  out[2] = t.s3;
+  out[3] = t.emin;
+  out[4] = t.esum;
+  out[5] = (double)t.nz;
+  out[6] = (double)t.maxd;
+  g->deg_stats_ready = true;
+  return ZG_OK;
 }
 
 int pattern_slot(const zg_program* p) {
@@ -469,26 +527,19 @@ extern "C" int zg_graph_features(const zg_graph* g, const zg_program* p, uint64_
                                  void* cuda_stream, float* f) {
   if (!g || !p || !f) return zg_set_error(ZG_ERR_INVALID_ARG, "zg_graph_features: null argument"), ZG_ERR_INVALID_ARG;
   cudaStream_t s = (cudaStream_t)cuda_stream;
-  DegStats* d = nullptr;
-  ZG_CUDA(zg_malloc_async((void**)&d, sizeof(DegStats), s));
-  cudaMemsetAsync(d, 0, sizeof(DegStats), s);
-  k_deg_stats<<<zg_num_sms() * 4, 256, 0, s>>>(g->d, d);
-  DegStats h;
-  cudaError_t e = cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, s);
-  cudaFreeAsync(d, s);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-  if (e == cudaSuccess) e = cudaGetLastError();
-  if (e != cudaSuccess) return zg_check_cuda(e, "graph features");
-  double m = (double)g->d.m, nz = (double)(h.nz ? h.nz : 1);
+  int rc0 = deg_stats(g, s);
+  if (rc0) return rc0;
+  const double* h = g->deg_stats;
+  double m = (double)g->d.m, nz = h[5] > 0 ? h[5] : 1.0;
   for (int i = 0; i < IN; ++i) f[i] = 0.f;
   f[0] = lg2(m);
   f[1] = lg2(nz);
-  f[2] = lg2((double)h.maxd);
-  f[3] = lg2(h.s1 / nz);
-  f[4] = lg2(h.s2 / nz);
-  f[5] = lg2(h.s3 / nz);
-  f[6] = lg2(m > 0 ? h.esum / m : 0);
-  f[7] = lg2(m > 0 ? h.emin / m : 0);
+  f[2] = lg2(h[6]);
+  f[3] = lg2(h[0] / nz);
+  f[4] = lg2(h[1] / nz);
+  f[5] = lg2(h[2] / nz);
+  f[6] = lg2(m > 0 ? h[4] / m : 0);
+  f[7] = lg2(m > 0 ? h[3] / m : 0);
   f[8 + pattern_slot(p)] = 1.f;
   zg_counters c;
   if (pilot_samples == 0) pilot_samples = 1ull << 16;
