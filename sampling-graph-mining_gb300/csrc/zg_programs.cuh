@@ -241,15 +241,44 @@ struct EdgeProbe {
   unsigned long long key, cand;
 };
 
+// The key's first bucket is read first.  An entry sits in its second bucket only if its first
+// bucket was full when it got there (insertion tries the first bucket first, and a slot once
+// filled is never emptied), so a first bucket with an empty slot and no matching fingerprint
+// proves the edge absent after one sector; the second bucket is read only behind a full first one.
 __device__ __forceinline__ EdgeProbe edge_candidate(const ZgDevGraph& g, uint32_t x, uint32_t y) {
   EdgeProbe pr;
   pr.key = zg_edge_key(x, y);
-  uint64_t b1 = 4ull * zg_bucket1(pr.key, g.hseed, g.hbits), b2 = 4ull * zg_bucket2(pr.key, g.hseed, g.hbits);
-  ulonglong2 a0, a1, c0, c1;
-  ld_bucket(g.hent + b1, a0, a1);
-  ld_bucket(g.hent + b2, c0, c1);
-  uint32_t fp = zg_fingerprint(pr.key, g.hseed);
+  const uint32_t fp = zg_fingerprint(pr.key, g.hseed);
+  ulonglong2 a0, a1;
+  ld_bucket(g.hent + 4ull * zg_bucket1(pr.key, g.hseed, g.hbits), a0, a1);
   // an empty entry never matches: no fingerprint is 0xFFFFFFFF
+  unsigned long long e = ZG_HASH_EMPTY;
+  e = (uint32_t)(a1.y >> 32) == fp ? a1.y : e;
+  e = (uint32_t)(a1.x >> 32) == fp ? a1.x : e;
+  e = (uint32_t)(a0.y >> 32) == fp ? a0.y : e;
+  e = (uint32_t)(a0.x >> 32) == fp ? a0.x : e;
+  const bool full = a0.x != ZG_HASH_EMPTY && a0.y != ZG_HASH_EMPTY && a1.x != ZG_HASH_EMPTY && a1.y != ZG_HASH_EMPTY;
+  if (e == ZG_HASH_EMPTY && full) {
+    ulonglong2 c0, c1;
+    ld_bucket(g.hent + 4ull * zg_bucket2(pr.key, g.hseed, g.hbits), c0, c1);
+    e = (uint32_t)(c1.y >> 32) == fp ? c1.y : e;
+    e = (uint32_t)(c1.x >> 32) == fp ? c1.x : e;
+    e = (uint32_t)(c0.y >> 32) == fp ? c0.y : e;
+    e = (uint32_t)(c0.x >> 32) == fp ? c0.x : e;
+  }
+  pr.cand = e;
+  return pr;
+}
+
+// The same look-up with both buckets read at once (two sectors, one dependent step): for the
+// latency-bound 4-clique, whose early rejection waits on this look-up.
+__device__ __forceinline__ EdgeProbe edge_candidate_both(const ZgDevGraph& g, uint32_t x, uint32_t y) {
+  EdgeProbe pr;
+  pr.key = zg_edge_key(x, y);
+  const uint32_t fp = zg_fingerprint(pr.key, g.hseed);
+  ulonglong2 a0, a1, c0, c1;
+  ld_bucket(g.hent + 4ull * zg_bucket1(pr.key, g.hseed, g.hbits), a0, a1);
+  ld_bucket(g.hent + 4ull * zg_bucket2(pr.key, g.hseed, g.hbits), c0, c1);
   unsigned long long e = ZG_HASH_EMPTY;
   e = (uint32_t)(c1.y >> 32) == fp ? c1.y : e;
   e = (uint32_t)(c1.x >> 32) == fp ? c1.x : e;
@@ -569,7 +598,7 @@ __device__ void prog_four_clique(const ZgDevGraph& g, Ctx& c, Res& r) {
   const uint32_t own = suf_own - r1o - 1;  // the anchor's entries after e1
   EdgeProbe p0{0ull, ZG_HASH_EMPTY};
   if (!DBG) {
-    p0 = edge_candidate(g, x0, vc);
+    p0 = edge_candidate_both(g, x0, vc);
     if (p0.cand == ZG_HASH_EMPTY && own != 0) return;
   }
   // second conditional step: anchors [a, b, c], min_valid = id1 + 1
