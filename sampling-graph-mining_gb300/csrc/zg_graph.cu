@@ -209,12 +209,20 @@ __global__ void k_cuckoo_check(const ZgDevGraph d, uint64_t m, const unsigned lo
   }
 }
 
-// The cuckoo table of the graph's edges: buckets for a load of at most 0.8, up to 8 seeds, and the
-// table doubled after every 4 failed seeds.
+// The cuckoo table of the graph's edges: buckets for a load of at most 0.8 (0.5, see below), up to
+// 8 seeds, and the table doubled after every 4 failed seeds.
 int build_hash(zg_graph* g, cudaStream_t s) {
   const uint64_t m = g->d.m;
   uint32_t bits = 1;
+  // Load up to 0.8, or up to 0.5 for a graph far larger than L2 (wide records) whose table then
+  // stays within 4 GiB: such a graph is read from HBM either way, and with more first buckets
+  // holding an empty slot more absent edges are settled by one sector (edge_candidate).  Larger
+  // tables keep the 0.8 load: doubling one of tens of GB cost more in address translation than
+  // it saved (R-MAT scale 26: 709 -> 794 ms per batch; the 43 M-edge Chung-Lu batch: 74 -> 70 ms).
   while ((4ull << bits) * 4 < m * 5) ++bits;  // 4 * 2^bits slots >= m / 0.8
+  uint32_t roomy = 1;
+  while ((4ull << roomy) < m * 2) ++roomy;  // 4 * 2^roomy slots >= m / 0.5
+  if (g->wide && (8ull * (4ull << roomy)) <= (4ull << 30)) bits = roomy;
   DevBuf fail;
   int rc;
   if ((rc = fail.alloc(sizeof(unsigned int)))) return rc;
