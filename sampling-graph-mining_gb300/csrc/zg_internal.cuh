@@ -15,7 +15,8 @@
 //             one saves a dependent read and two sectors per step on graphs far larger than L2.
 //   off[V+1]  int64 offsets shared by both adjacency arrays (outgoing_adj_index).
 //   adj_e[2m] uint2 (nbr, edge_id) sorted by edge id per vertex (outgoing_adj_list order,
-//             asserted at src/Graph.cpp:324-334): the sampling order.
+//             asserted at src/Graph.cpp:324-334): the sampling order.  Followed by 8 entries of
+//             slack that the windowed search may read but never uses.
 //   adj_n[2m] uint2 (nbr, edge_id) sorted by (nbr, edge_id) per vertex (exports, exact counts).
 //   w[m]      uint32 edge data (Graph<VertexId>) or null.
 //   off32[V+1] the offsets as uint32 (2m < 2^32), read by the compact layout's steps.
@@ -94,7 +95,7 @@ struct zg_graph {
   uint32_t* w;
   uint32_t* off32;
   unsigned long long* hent;
-  void* hot;            // one allocation holding adj_e then off32 (read together by every program)
+  void* hot;            // one allocation: adj_e, 8 entries of slack (windowed searches), off32
   uint64_t hot_bytes;
   uint64_t num_edges;   // Graph::num_edges metadata
   uint64_t max_degree;  // Graph::max_degree metadata
