@@ -196,8 +196,7 @@ def time_to_bound(Z, g, names, acc, eps=0.01, conf=0.95, cap=1 << 37, coverage_q
     ex = acc["triangle"]["exact"] if "triangle" in acc else g.exact_count(1)
     inside, met = 0, 0
     for s in range(coverage_queries):
-        n, _, _ = Z.learned_budget(net, g, prog, eps, conf, seed=1000 + s)
-        q = Z.query(g, prog, eps, conf, n, 5000 + s, stream_id=0x60 + s, max_samples=cap)
+        q = Z.learned_query(net, g, prog, eps, conf, 1000 + s, 5000 + s, stream_id=0x60 + s, max_samples=cap)[0]
         met += q.bound_met
         inside += abs(q.estimate - ex) <= eps * ex
     out["coverage"] = {"pattern": "triangle", "queries": coverage_queries, "bound_met": met,
@@ -533,8 +532,7 @@ def large_time_to_bound(Z, g, eps=0.01, conf=0.95, cap=1 << 37):
                                    ("four_clique_unbiased", Z.PROG_FOUR_CLIQUE_UNBIASED, Z.EXACT_FOUR_CLIQUE)):
         prog = Z.Program(kind)
         t0 = time.perf_counter()
-        n, _, y = Z.learned_budget(net, g, prog, eps, conf, seed=77)
-        q = Z.query(g, prog, eps, conf, n, 4242, stream_id=0x71, max_samples=cap)
+        q, n = Z.learned_query(net, g, prog, eps, conf, 77, 4242, stream_id=0x71, max_samples=cap)
         dt = time.perf_counter() - t0
         r = {"n_sized": int(n), "samples": int(q.samples), "bound_met": int(q.bound_met),
              "rel_half_width": q.rel_half_width, "estimate": q.estimate, "seconds": dt}

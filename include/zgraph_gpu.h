@@ -397,6 +397,19 @@ int zg_mlp_predict(const zg_mlp* net, const float* X, uint32_t n_rows, float* Y)
  * estimators (0: 2^16).  Not to be called for the same graph from two threads at once. */
 int zg_graph_features(const zg_graph* g, const zg_program* p, uint64_t pilot_samples,
                       uint64_t seed, void* cuda_stream, float* features);
+/* Learned sizing (the learned counterpart of ErrorProfile::get_num_estimators,
+ * src/ErrorLatencyProfile.cpp:52-59): the query's features (zg_graph_features with pilot_samples),
+ * the network's prediction, and n = z^2 * 2^pred_cv2 / error^2, z the two-sided normal quantile
+ * of confidence, at least 2^16.  prediction (may be NULL) gets the network's two outputs. */
+int zg_elp_learned(const zg_mlp* net, const zg_graph* g, const zg_program* p, double error,
+                   double confidence, uint64_t pilot_samples, uint64_t seed, void* cuda_stream,
+                   uint64_t* n_required, float* prediction);
+/* zg_elp_learned (2^16-sample pilot from feature_seed), then zg_query from query_seed.  A budget
+ * above 2^30 samples runs in two looks: half of it first, then what the judge still needs, so an
+ * over-predicted budget costs at most half of it in extra samples.  n_required may be NULL. */
+int zg_query_learned(const zg_mlp* net, const zg_graph* g, const zg_program* p, double error,
+                     double confidence, uint64_t max_samples, uint64_t feature_seed, uint64_t query_seed,
+                     uint32_t stream_id, void* cuda_stream, uint64_t* n_required, zg_query_result* out);
 
 /* ---- measurement ------------------------------------------------------------ */
 /* Read bandwidth (GB/s) of a device buffer of `bytes` read `reps` times by one persistent grid,

@@ -387,19 +387,21 @@ extern "C" int zg_mlp_predict(const zg_mlp* p, const float* X, uint32_t n_rows, 
   std::vector<float> xn((size_t)n_rows * IN);
   for (uint32_t r = 0; r < n_rows; ++r)
     for (int k = 0; k < IN; ++k) xn[(size_t)r * IN + k] = (X[(size_t)r * IN + k] - p->norm[k]) / p->norm[IN + k];
-  float *dX = nullptr, *dY = nullptr;
-  cudaError_t e = cudaMalloc((void**)&dX, sizeof(float) * xn.size());
-  if (e == cudaSuccess) e = cudaMalloc((void**)&dY, sizeof(float) * n_rows * OUT);
-  if (e == cudaSuccess) e = cudaMemcpy(dX, xn.data(), sizeof(float) * xn.size(), cudaMemcpyHostToDevice);
+  // inputs and outputs in one block from the library's pool; stream-ordered on the legacy stream
+  const cudaStream_t s = 0;
+  float* d = nullptr;
+  cudaError_t e = zg_malloc_async((void**)&d, sizeof(float) * (xn.size() + (size_t)n_rows * OUT), s);
+  if (e != cudaSuccess) return zg_check_cuda(e, "zg_mlp_predict");
+  float *dX = d, *dY = d + xn.size();
+  e = cudaMemcpyAsync(dX, xn.data(), sizeof(float) * xn.size(), cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) {
     int grid = (int)std::min<uint32_t>((n_rows + 127) / 128, 1024);
-    k_mlp_predict<<<grid, 128>>>(dX, n_rows, p->master, dY);
-    e = cudaDeviceSynchronize();
+    k_mlp_predict<<<grid, 128, 0, s>>>(dX, n_rows, p->master, dY);
+    e = cudaGetLastError();
   }
-  if (e == cudaSuccess) e = cudaGetLastError();
-  if (e == cudaSuccess) e = cudaMemcpy(Y, dY, sizeof(float) * n_rows * OUT, cudaMemcpyDeviceToHost);
-  cudaFree(dX);
-  cudaFree(dY);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(Y, dY, sizeof(float) * n_rows * OUT, cudaMemcpyDeviceToHost, s);
+  cudaFreeAsync(d, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return zg_check_cuda(e, "zg_mlp_predict");
   for (uint32_t r = 0; r < n_rows; ++r)
     for (int o = 0; o < OUT; ++o)
@@ -551,4 +553,39 @@ extern "C" int zg_graph_features(const zg_graph* g, const zg_program* p, uint64_
   f[14] = lg2(((double)c.hits + 0.5) / n);
   f[15] = lg2(cv2 > 1e-12 ? cv2 : 1e-12);
   return ZG_OK;
+}
+
+// ---- learned sizing and the learned query ---------------------------------------------------
+extern "C" int zg_elp_learned(const zg_mlp* net, const zg_graph* g, const zg_program* p, double error,
+                              double confidence, uint64_t pilot_samples, uint64_t seed, void* cuda_stream,
+                              uint64_t* n_required, float* prediction) {
+  if (!net || !g || !p || !n_required)
+    return zg_set_error(ZG_ERR_INVALID_ARG, "zg_elp_learned: null argument"), ZG_ERR_INVALID_ARG;
+  if (!(error > 0) || !(confidence > 0 && confidence < 1))
+    return zg_set_error(ZG_ERR_INVALID_ARG, "zg_elp_learned: error %g / confidence %g", error, confidence),
+           ZG_ERR_INVALID_ARG;
+  float f[IN], y[OUT];
+  int rc = zg_graph_features(g, p, pilot_samples, seed, cuda_stream, f);
+  if (rc) return rc;
+  if ((rc = zg_mlp_predict(net, f, 1, y))) return rc;
+  const double z = zg_normal_quantile(1.0 - (1.0 - confidence) / 2.0);
+  const double n = z * z * exp2((double)y[0]) / (error * error);
+  const double lo = (double)(1ull << 16), hi = 1e18;
+  *n_required = n >= hi ? (uint64_t)hi : n <= lo ? (uint64_t)lo : (uint64_t)n;
+  if (prediction) {
+    prediction[0] = y[0];
+    prediction[1] = y[1];
+  }
+  return ZG_OK;
+}
+
+extern "C" int zg_query_learned(const zg_mlp* net, const zg_graph* g, const zg_program* p, double error,
+                                double confidence, uint64_t max_samples, uint64_t feature_seed, uint64_t query_seed,
+                                uint32_t stream_id, void* cuda_stream, uint64_t* n_required, zg_query_result* out) {
+  uint64_t n = 0;
+  int rc = zg_elp_learned(net, g, p, error, confidence, 0, feature_seed, cuda_stream, &n, nullptr);
+  if (rc) return rc;
+  if (n_required) *n_required = n;
+  const uint64_t first = n > (1ull << 30) ? n / 2 : n;  // two looks for a long budget
+  return zg_query(g, p, error, confidence, first, max_samples, query_seed, stream_id, cuda_stream, out);
 }

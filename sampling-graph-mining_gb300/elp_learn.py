@@ -126,12 +126,12 @@ def compare(net, graph, name, eps=0.01, conf=0.95, seed=5, max_samples=1 << 36):
                     "rel_half_width": q.rel_half_width, "estimate": q.estimate,
                     "seconds": time.perf_counter() - t0, "profile_ms": elp.profile_ms}
     t0 = time.perf_counter()
-    n, f, y = Z.learned_budget(net, graph, prog, eps, conf, seed)
-    q = Z.query(graph, prog, eps, conf, n, seed + 200, stream_id=0x52, max_samples=max_samples)
+    q, n = Z.learned_query(net, graph, prog, eps, conf, seed, seed + 200, stream_id=0x52, max_samples=max_samples)
+    dt = time.perf_counter() - t0
+    _, _, y = Z.learned_budget(net, graph, prog, eps, conf, seed)  # the prediction, for the report (untimed)
     out["learned"] = {"n_sized": int(n), "samples": int(q.samples), "bound_met": int(q.bound_met),
                       "rel_half_width": q.rel_half_width, "estimate": q.estimate,
-                      "seconds": time.perf_counter() - t0, "pred_log2_cv2": float(y[0]),
-                      "pred_log2_ns": float(y[1])}
+                      "seconds": dt, "pred_log2_cv2": float(y[0]), "pred_log2_ns": float(y[1])}
     return out
 
 

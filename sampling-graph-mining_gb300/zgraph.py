@@ -154,6 +154,9 @@ def lib():
             "zg_mlp_grad": ([P, P, P, U32, P, P], I32),
             "zg_mlp_predict": ([P, P, U32, P], I32),
             "zg_graph_features": ([P, P, U64, U64, P, P], I32),
+            "zg_elp_learned": ([P, P, P, D, D, U64, U64, P, C.POINTER(U64), P], I32),
+            "zg_query_learned": ([P, P, P, D, D, U64, U64, U64, U32, P, C.POINTER(U64), C.POINTER(QueryResult)],
+                                 I32),
             "zg_gen_rmat": ([U32, U32, D, D, D, U64, U64, P, C.POINTER(U64)], I32),
             "zg_gen_chung_lu": ([U32, D, D, U64, U64, P, C.POINTER(U64)], I32),
             "zg_gen_weights": ([U64, U32, U64, P], I32),
@@ -697,12 +700,24 @@ class Mlp:
 
 
 def learned_budget(mlp, graph, program, eps, conf, seed=1, pilot_samples=1 << 16):
-    """Learned ELP sizing: predicted per-sample relative variance -> n = z^2 * cv2 / eps^2."""
+    """zg_elp_learned: predicted per-sample relative variance -> n = z^2 * cv2 / eps^2.
+    Returns (n, features, prediction)."""
     f = features(graph, program, pilot_samples, seed)
-    y = mlp.predict(f[None, :])[0]
-    z = lib().zg_normal_quantile(1.0 - (1.0 - conf) / 2.0)
-    n = z * z * float(2.0 ** y[0]) / (eps * eps)
-    return max(int(n), 1 << 16), f, y
+    n = C.c_uint64(0)
+    y = np.zeros(2, np.float32)
+    check(lib().zg_elp_learned(mlp._h, graph.handle, program.handle, eps, conf, pilot_samples, seed, None,
+                               C.byref(n), _ptr(y)))
+    return int(n.value), f, y
+
+
+def learned_query(mlp, graph, program, eps, conf, seed, query_seed, stream_id=0, max_samples=0, cuda_stream=None):
+    """zg_query_learned: learned sizing (2^16-sample pilot from seed), then the judge from query_seed;
+    a budget above 2^30 samples runs in two looks (half first).  Returns (QueryResult, budget)."""
+    n = C.c_uint64(0)
+    out = QueryResult()
+    check(lib().zg_query_learned(mlp._h, graph.handle, program.handle, eps, conf, max_samples, seed, query_seed,
+                                 stream_id, cuda_stream, C.byref(n), C.byref(out)))
+    return out, int(n.value)
 
 
 def run_three_motif(graph, n_chain, n_tri, seed, stream_chain=0, stream_tri=1, cuda_stream=None):

@@ -95,6 +95,28 @@ def test_features_match_host():
     assert abs(f[14] - math.log2((c.hits + 0.5) / (1 << 16))) < 1e-5
 
 
+def test_learned_budget_and_query_entry_points():
+    """zg_elp_learned is the sizing formula on the network's prediction for the query's features;
+    zg_query_learned runs it and judges the answer, half of a long budget first."""
+    e = Z.gen_rmat(12, 10, seed=8)
+    g = Z.Graph.from_edges(e, 1 << 12)
+    net = Z.Mlp(5)
+    rng = np.random.default_rng(6)
+    net.train(rng.normal(size=(128, 16)).astype(np.float32), rng.normal(size=(128, 2)).astype(np.float32) + 6,
+              epochs=2, batch=32, lr=1e-3)
+    p = Z.Program(Z.PROG_TRIANGLE)
+    n, f, y = Z.learned_budget(net, g, p, 0.02, 0.95, seed=4)
+    y_ref = net.predict(f[None, :])[0]
+    assert np.allclose(y, y_ref, rtol=1e-6, atol=1e-6)
+    z = Z.lib().zg_normal_quantile(0.975)
+    assert n == max(int(z * z * 2.0 ** float(y_ref[0]) / 0.02 ** 2), 1 << 16)
+    q, n2 = Z.learned_query(net, g, p, 0.02, 0.95, 4, 77, stream_id=3, max_samples=1 << 32)
+    assert n2 == n and q.bound_met and q.rel_half_width <= 0.02
+    # the judge's first round ran the budget (below 2^30: one look), continued from the same stream
+    first = Z.query(g, p, 0.02, 0.95, n, 77, stream_id=3, max_samples=1 << 32)
+    assert (q.samples, q.estimate) == (first.samples, first.estimate)
+
+
 def test_learned_sizing_beats_plain_elp():
     """Trained on small synthetic graphs, the network sizes held-out queries far closer to what the
     empirical bound needs than ErrorProfile does; both deliver answers that meet the bound."""
