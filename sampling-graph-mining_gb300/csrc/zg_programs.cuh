@@ -565,7 +565,8 @@ __device__ void prog_four_clique(const ZgDevGraph& g, Ctx& c, Res& r) {
     r.fail = true;
     return;
   }
-  const uint64_t w1 = c.word(1), w2 = c.word(2);  // Philox work of the later draws, up front
+  const uint64_t w1 = c.word(1);  // the second draw's Philox work overlaps the first loads
+  // (the third draw's is done where it is needed: most samples end before it)
   uint64_t e0 = c.draw(0, g.m - 1);
   uint4 q, qp;
   edge_rec(g, e0, q, qp);
@@ -629,7 +630,7 @@ __device__ void prog_four_clique(const ZgDevGraph& g, Ctx& c, Res& r) {
     return;
   }
   if (DBG) c.sectors += 1;
-  uint64_t r2 = c.take(w2, 0, S2 - 1);
+  uint64_t r2 = c.take(c.word(2), 0, S2 - 1);
   int s2;
   uint32_t pos2;
   if (r2 < lenA) {
