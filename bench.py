@@ -349,18 +349,20 @@ def run_gb300(args):
             torch.distributed.destroy_process_group()
         return
     # algorithmic bytes per sample: access model from the debug kernel (2^16 samples)
-    model = {}
+    model, closures = {}, {}
     for j, p in enumerate(progs):
         tr = p.run_debug(g, 1 << 16, seed, stream_id=j + 1)
         model[names[j]] = float(tr["sectors"].mean()) * 32.0
+        closures[names[j]] = float(tr["closures"].mean())  # conditional_close look-ups per sample
     peak, peak_kind = peaks()
     kern = []
     for j, name in enumerate(names):
         t = per_prog[j] / args.steps / 1000.0
         ach = model[name] * n / t / 1e9
         kern.append({"kernel": "k_sample<%s>" % name, "ms": per_prog[j] / args.steps, "bytes_per_sample": model[name],
-                     "achieved_gbs": ach, "samples_per_s": n / t, "hits": int(res[j].hits),
-                     "estimate": res[j].estimate})
+                     "achieved_gbs": ach, "samples_per_s": n / t,
+                     "closure_checks_per_sample": closures[name], "closure_checks_per_s": closures[name] * n / t,
+                     "hits": int(res[j].hits), "estimate": res[j].estimate})
     dom = max(kern, key=lambda k: k["ms"])
     traffic = profile_traffic(n).get(dom["kernel"]) if args.workload == "rmat20" else None
     l2_gbs = l2_read_gbs(Z)

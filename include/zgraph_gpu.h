@@ -118,7 +118,8 @@ typedef struct zg_sample_trace {
   uint32_t fail;
   uint32_t shift;
   uint32_t sectors;        /* 32-byte sectors of the access model (algorithmic bytes / 32) */
-  uint32_t reserved;
+  uint32_t closures;       /* closure checks of the access model (conditional_close edge
+                              look-ups, up to the first missing edge)                   */
   double   w;              /* bit-exact reference value of estimate()               */
   uint64_t num[3];         /* 192-bit exact numerator                               */
   uint64_t lo[ZG_MAX_DRAWS];

@@ -15,7 +15,7 @@ REF_DIR = os.path.join(HERE, "_ref")
 
 MAX_DRAWS = 16
 TRACE_DTYPE = np.dtype([("ndraws", "<u4"), ("hit", "<u4"), ("fail", "<u4"), ("shift", "<u4"),
-                        ("sectors", "<u4"), ("reserved", "<u4"), ("w", "<f8"), ("num", "<u8", (3,)), ("lo", "<u8", (MAX_DRAWS,)),
+                        ("sectors", "<u4"), ("closures", "<u4"), ("w", "<f8"), ("num", "<u8", (3,)), ("lo", "<u8", (MAX_DRAWS,)),
                         ("hi", "<u8", (MAX_DRAWS,)), ("val", "<u8", (MAX_DRAWS,))])
 
 

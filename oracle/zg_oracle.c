@@ -156,6 +156,7 @@ typedef struct {
   u128 num_lo; uint64_t num_hi; /* 192-bit exact numerator */
   int overflow;
   uint32_t sectors; /* 32-byte sector access model (see zgo_model_*) */
+  uint32_t closures; /* closure checks of the access model */
 } zgo_ctx;
 
 /* Access model of the rebuilt kernels, in 32-byte sectors (the roofline's algorithmic bytes):
@@ -263,6 +264,7 @@ static int prim_close(zgo_ctx* c, const zgo_sub* sampled, const zgo_sub* wait) {
     {
       uint64_t dx = g->off[ws + 1] - g->off[ws], dy = g->off[wd + 1] - g->off[wd];
       c->sectors += 2 + zgo_model_search(dx < dy ? dx : dy);
+      c->closures++;
     }
     for (int j = 0; j < sampled->nv && !found; ++j) {
       uint32_t v = sampled->v[j];
@@ -343,6 +345,7 @@ static int64_t find_edge_id(zgo_ctx* c, uint32_t x, uint32_t y) {
   const zgo_graph* g = c->g;
   uint64_t dx = g->off[x + 1] - g->off[x], dy = g->off[y + 1] - g->off[y];
   c->sectors += 2 + zgo_model_search(dx < dy ? dx : dy);
+  c->closures++;
   uint32_t v = dx <= dy ? x : y, t = dx <= dy ? y : x;
   for (uint64_t idx = g->off[v]; idx < g->off[v + 1]; ++idx)
     if (g->adj_nbr[idx] == t) return (int64_t)g->adj_eid[idx];
@@ -678,7 +681,7 @@ static uint32_t prog_den_log2(const zgo_program* p) {
 static void ctx_init(zgo_ctx* c, const zgo_graph* g, uint64_t seed, uint32_t stream,
                      uint64_t sample, zg_sample_trace* tr) {
   c->g = g; c->seed = seed; c->stream = stream; c->sample = sample; c->nd = 0; c->tr = tr;
-  c->shift = 0; c->num_lo = 1; c->num_hi = 0; c->overflow = 0; c->sectors = 0;
+  c->shift = 0; c->num_lo = 1; c->num_hi = 0; c->overflow = 0; c->sectors = 0; c->closures = 0;
   memset(tr, 0, sizeof(*tr));
 }
 
@@ -686,6 +689,7 @@ static void ctx_finish(zgo_ctx* c, double r) {
   zg_sample_trace* tr = c->tr;
   tr->ndraws = c->nd;
   tr->sectors = c->sectors;
+  tr->closures = c->closures;
   if (r < 0) { tr->fail = 1; r = 0; }
   tr->w = r;
   tr->hit = r != 0;

@@ -31,6 +31,7 @@ struct Ctx {
   uint32_t nd;
   zg_sample_trace* tr;  // debug only
   uint32_t sectors;     // debug only: access model, 32-byte sectors
+  uint32_t closures;    // debug only: access model, closure checks
   __device__ __forceinline__ uint64_t draw(uint64_t lo, uint64_t hi) { return take(word(nd), lo, hi); }
   // The Philox word of draw k, computable before the range it maps to is known (so the integer
   // work overlaps the loads that determine the range); take() maps the next draw's word.
@@ -453,7 +454,10 @@ __device__ void prog_triangle(const ZgDevGraph& g, Ctx& c, Res& r) {
   res_mul(r, S);
   if (a1 == 2) r.shift = 1;
   bool closed = (a1 == 1) && edge_after(g, other, e1.x, e1.y + 1);
-  if (DBG) c.sectors += model_close(g, other, e1.x);
+  if (DBG) {
+    c.sectors += model_close(g, other, e1.x);
+    c.closures++;
+  }
   r.hit = closed;
   if (DBG && closed) {
     double p = 1.0;
@@ -524,13 +528,16 @@ __device__ __forceinline__ bool canonical_four_clique(const ZgDevGraph& g, Ctx& 
   if (DBG) {
     h0 = edge_confirm(g, edge_candidate(g, vslot(x0), vc));
     c.sectors += model_close(g, vslot(x0), vc);
+    c.closures++;
     if (h0 >= 0) {
       h1 = edge_confirm(g, edge_candidate(g, vslot(x1), vd));
       c.sectors += model_close(g, vslot(x1), vd);
+      c.closures++;
     }
     if (h0 >= 0 && h1 >= 0) {
       h2 = edge_confirm(g, edge_candidate(g, vslot(x2), vd));
       c.sectors += model_close(g, vslot(x2), vd);
+      c.closures++;
     }
   } else {
     const EdgeProbe& p0 = pc;  // the caller's look-up of (slot x0, c)
@@ -667,6 +674,7 @@ __device__ void prog_four_clique(const ZgDevGraph& g, Ctx& c, Res& r) {
           if (!sampled && ok) {
             ok = edge_after(g, vslot(i), vslot(j), mv2);
             c.sectors += model_close(g, vslot(i), vslot(j));
+            c.closures++;
           }
         }
     } else {

@@ -155,6 +155,7 @@ __global__ void __launch_bounds__(kBlock) k_sample_debug(ZgDevGraph g, ZgProgPar
     t->fail = r.fail;
     t->shift = r.hit ? r.shift : 0;
     t->sectors = c.sectors;
+    t->closures = c.closures;
     t->w = r.hit ? r.w : 0.0;
     t->num[0] = r.hit ? r.num.l[0] : 0;
     t->num[1] = r.hit ? r.num.l[1] : 0;
@@ -250,6 +251,7 @@ __global__ void __launch_bounds__(kBlock) k_three_motif(ZgDevGraph g, uint64_t n
         t->fail = r.fail;
         t->shift = r.hit ? r.shift : 0;
         t->sectors = c.sectors;
+        t->closures = c.closures;
         t->w = r.hit ? r.w : 0.0;
         t->num[0] = r.hit ? r.num.l[0] : 0;
         t->num[1] = r.hit ? r.num.l[1] : 0;
@@ -264,6 +266,7 @@ __global__ void __launch_bounds__(kBlock) k_three_motif(ZgDevGraph g, uint64_t n
           t->fail = 0;
           t->shift = rt.hit ? rt.shift : 0;
           t->sectors = tri_sectors;
+          t->closures = tri_sectors ? 1 : 0;
           t->w = rt.w;
           t->num[0] = rt.hit ? rt.num.l[0] : 0;
           t->num[1] = rt.hit ? rt.num.l[1] : 0;
@@ -283,6 +286,7 @@ __global__ void __launch_bounds__(kBlock) k_three_motif(ZgDevGraph g, uint64_t n
         t->fail = r.fail;
         t->shift = r.hit ? r.shift : 0;
         t->sectors = c.sectors;
+        t->closures = c.closures;
         t->w = r.hit ? r.w : 0.0;
         t->num[0] = r.hit ? r.num.l[0] : 0;
         t->num[1] = r.hit ? r.num.l[1] : 0;

@@ -96,7 +96,7 @@ class QueryResult(C.Structure):
 ELP_KEEP_OFFSET, ELP_SHUFFLE_OFFSET, ELP_FILTER_OFFSET, ELP_STREAM = 1, 2, 3, 0x454C5000
 
 TRACE_DTYPE = np.dtype([("ndraws", "<u4"), ("hit", "<u4"), ("fail", "<u4"), ("shift", "<u4"),
-                        ("sectors", "<u4"), ("reserved", "<u4"), ("w", "<f8"), ("num", "<u8", (3,)), ("lo", "<u8", (MAX_DRAWS,)),
+                        ("sectors", "<u4"), ("closures", "<u4"), ("w", "<f8"), ("num", "<u8", (3,)), ("lo", "<u8", (MAX_DRAWS,)),
                         ("hi", "<u8", (MAX_DRAWS,)), ("val", "<u8", (MAX_DRAWS,))])
 
 _lib = None

@@ -12,7 +12,7 @@ import zgraph as Z
 
 pytestmark = pytest.mark.gpu
 
-FIELDS = ("ndraws", "hit", "fail", "shift", "sectors", "num", "lo", "hi", "val")
+FIELDS = ("ndraws", "hit", "fail", "shift", "sectors", "closures", "num", "lo", "hi", "val")
 
 STAR = (5, [(0, 1), (0, 2), (0, 3), (0, 4)])                     # applications/FiveStar.cpp:18-26
 HOUSE = (5, [(0, 1), (0, 2), (1, 2), (1, 3), (2, 4), (3, 4)])     # applications/FiveHouse.cpp:18-27
