@@ -1058,14 +1058,15 @@ __device__ __forceinline__ void acc_add(Acc& a, const Res& r, uint32_t den) {
   a.sw2 = fma(w, w, a.sw2);
 }
 
-// One thread's 320-bit sum and variance term kept in shared memory (slot threadIdx.x of arrays
-// of BLOCK entries) instead of registers: a latency-bound sampling loop then fits a smaller
+// One thread's counters, 320-bit sum and variance term kept in shared memory (slot threadIdx.x of
+// arrays of BLOCK entries) instead of registers: a latency-bound sampling loop then fits a smaller
 // register budget, i.e. more resident warps and more loads in flight.  Each thread adds its hits
 // in the same order as with acc_add, so the results are identical.
 template <int BLOCK>
 struct AccSlots {
   unsigned long long s[4][BLOCK];
   double sw2[BLOCK];
+  uint32_t samples[BLOCK], hits[BLOCK], fails[BLOCK], ovf[BLOCK];
 };
 
 template <int BLOCK>
@@ -1073,21 +1074,22 @@ __device__ __forceinline__ void acc_slots_init(AccSlots<BLOCK>& sl) {
   const int t = threadIdx.x;
   sl.s[0][t] = sl.s[1][t] = sl.s[2][t] = sl.s[3][t] = 0;
   sl.sw2[t] = 0.0;
+  sl.samples[t] = sl.hits[t] = sl.fails[t] = sl.ovf[t] = 0;
 }
 
 template <int BLOCK>
 __device__ __forceinline__ void acc_add_slots(Acc& a, AccSlots<BLOCK>& sl, const Res& r, uint32_t den) {
-  a.samples++;
-  a.fails += r.fail;
+  const int t = threadIdx.x;
+  sl.samples[t]++;
+  sl.fails[t] += r.fail;
   if (!r.hit) return;
-  a.hits++;
-  a.ovf += r.ovf;
+  sl.hits[t]++;
+  sl.ovf[t] += r.ovf;
   uint32_t sh = den - r.shift;  // < 64
   uint64_t v0 = r.num.l[0] << sh;
   uint64_t v1 = sh ? (r.num.l[1] << sh) | (r.num.l[0] >> (64 - sh)) : r.num.l[1];
   uint64_t v2 = sh ? (r.num.l[2] << sh) | (r.num.l[1] >> (64 - sh)) : r.num.l[2];
   uint64_t v3 = sh ? (r.num.l[2] >> (64 - sh)) : 0;
-  const int t = threadIdx.x;
   unsigned long long s0 = sl.s[0][t], s1 = sl.s[1][t], s2 = sl.s[2][t], s3 = sl.s[3][t];
   asm("add.cc.u64 %0, %0, %4;\n\t"
       "addc.cc.u64 %1, %1, %5;\n\t"
@@ -1107,6 +1109,10 @@ __device__ __forceinline__ void acc_add_slots(Acc& a, AccSlots<BLOCK>& sl, const
 template <int BLOCK>
 __device__ __forceinline__ void acc_from_slots(Acc& a, const AccSlots<BLOCK>& sl) {
   const int t = threadIdx.x;
+  a.samples = sl.samples[t];
+  a.hits = sl.hits[t];
+  a.fails = sl.fails[t];
+  a.ovf = sl.ovf[t];
   a.s[0] = sl.s[0][t];
   a.s[1] = sl.s[1][t];
   a.s[2] = sl.s[2][t];
