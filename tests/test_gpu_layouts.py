@@ -64,7 +64,7 @@ def test_programs_identical(pair, name, kind, param, pat):
         _same(p.run(c, n, seed, stream_id=4, first_sample=first), p.run(wd, n, seed, stream_id=4, first_sample=first),
               (name, n))
     tc, tw = p.run_debug(c, 4096, 11), p.run_debug(wd, 4096, 11)
-    for k in ("ndraws", "hit", "fail", "shift", "sectors", "w", "num", "lo", "hi", "val"):
+    for k in ("ndraws", "hit", "fail", "shift", "sectors", "closures", "w", "num", "lo", "hi", "val"):
         assert np.array_equal(tc[k], tw[k]), (name, k)
 
 
@@ -106,3 +106,19 @@ def test_device_generator_layouts():
     _same(p.run(gc, 1 << 20, 2), p.run(gw, 1 << 20, 2), "chung-lu")
     with pytest.raises(Z.ZgError):
         Z.set_record_layout(3)
+
+
+def test_tiny_graphs_and_sample_counts():
+    """Empty, single-edge and isolated-vertex graphs, and sample counts that leave warps partly
+    filled (the 4-chain's grouped queues drain their leftovers): both layouts agree exactly."""
+    Z.init(0)
+    cases = [(np.zeros((0, 2), np.uint32), 4), (np.array([[0, 1]], np.uint32), 2),
+             (np.array([[5, 2], [2, 9], [9, 5]], np.uint32), 12),
+             (np.array([[0, 1], [1, 2], [2, 3], [3, 0], [0, 2], [4, 0]], np.uint32), 6)]
+    for e, nv in cases:
+        gc = _build(Z.RECORDS_COMPACT, lambda: Z.Graph.from_edges(e, nv))
+        gw = _build(Z.RECORDS_WIDE, lambda: Z.Graph.from_edges(e, nv))
+        for name, kind, param, pat in PROGRAMS:
+            p = Z.Program(kind, param, pat)
+            for n in (1, 31, 33, 1000):
+                _same(p.run(gc, n, 3, first_sample=n), p.run(gw, n, 3, first_sample=n), (len(e), name, n))
