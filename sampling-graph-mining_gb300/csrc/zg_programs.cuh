@@ -902,10 +902,148 @@ __device__ __forceinline__ uint32_t pair_bit(uint32_t i, uint32_t j, uint32_t pv
   return i * (2 * pv - i - 1) / 2 + (j - i - 1);
 }
 
+// prog_pattern for patterns of at most MV vertices and ME edges with every per-sample array in
+// registers: loops run to the compile-time bounds under guards, writes at a run-time position go
+// to every slot under a predicate, and the sampled edges are kept as the vertex slots of their
+// ends (4 bits each, packed) plus their edge ids.  Same draws, same tests in the same order as
+// prog_pattern (the canonicality test compares vertex slots: the vertices are distinct).
+template <int MV, int ME>
+__device__ void prog_pattern_small(const ZgDevGraph& g, const ZgProgParams& pp, Ctx& c, Res& r) {
+  uint64_t e0 = c.draw(0, g.m - 1);
+  res_mul(r, g.m);
+  uint4 q, qp;
+  edge_rec(g, e0, q, qp);
+  uint32_t vs[MV], vl[MV], ve[MV], ei[ME];
+#pragma unroll
+  for (int i = 0; i < MV; ++i) vs[i] = vl[i] = ve[i] = 0;
+#pragma unroll
+  for (int i = 0; i < ME; ++i) ei[i] = 0;
+  vs[0] = q.x;
+  vs[1] = q.y;
+  vl[0] = qp.x + 1;
+  vl[1] = qp.y + 1;
+  ve[0] = vl[0] + q.z;
+  ve[1] = vl[1] + q.w;
+  uint32_t es = 0u, ed = 1u;  // edge k's end slots at bits 4k..4k+3
+  ei[0] = (uint32_t)e0;
+  const uint32_t mv = (uint32_t)e0 + 1;
+  int nvtx = 2, ne = 1;
+#pragma unroll
+  for (int k = 1; k < ME; ++k) {
+    if ((uint32_t)k >= pp.pe) break;
+    uint64_t S = 0;
+#pragma unroll
+    for (int i = 0; i < MV; ++i) S += i < nvtx ? (uint64_t)(ve[i] - vl[i]) : 0ull;
+    if (S == 0) {
+      r.fail = true;
+      return;
+    }
+    uint64_t rr = c.draw(0, S - 1);
+    // the anchor slot: the first whose entries hold rr (prog_pattern's scan, unrolled)
+    int side = nvtx - 1;
+    uint32_t base = 0, src = 0;
+    bool done = false;
+#pragma unroll
+    for (int i = 0; i < MV - 1; ++i) {
+      const uint64_t len = (uint64_t)(ve[i] - vl[i]);
+      const bool here = !done && i < nvtx - 1 && rr < len;
+      if (!done && i < nvtx - 1 && !here) rr -= len;
+      if (here) side = i;
+      done = done || here || i >= nvtx - 1;
+    }
+#pragma unroll
+    for (int i = 0; i < MV; ++i)
+      if (i == side) {
+        base = vl[i];
+        src = vs[i];
+      }
+    uint2 e = ZG_LDG(&g.adj_e[base + (uint32_t)rr]);
+    int nbr_slot = -1;
+#pragma unroll
+    for (int i = 0; i < MV; ++i)
+      if (i < nvtx && vs[i] == e.x) nbr_slot = i;
+    res_mul(r, S);
+    if (nbr_slot >= 0) r.shift++;
+    // canonicality_check (src/SamplerGenerator.cpp:368-385) on vertex slots
+    const int ds = nbr_slot >= 0 ? nbr_slot : nvtx;  // the new edge's far end (a new slot if new)
+    if (ne > 1) {
+      bool found = false, canon = true;
+#pragma unroll
+      for (int i = 0; i < ME; ++i) {
+        if (i >= ne) break;
+        const int a = (int)((es >> (4 * i)) & 15u), b = (int)((ed >> (4 * i)) & 15u);
+        if (!found) {
+          if (side == a || side == b || ds == a || ds == b) found = true;
+        } else if (ei[i] >= e.y) {
+          canon = false;
+        }
+      }
+      if (!canon) return;
+    }
+    es |= (uint32_t)side << (4 * ne);
+    ed |= (uint32_t)ds << (4 * ne);
+#pragma unroll
+    for (int i = 0; i < ME; ++i)
+      if (i == ne) ei[i] = e.y;
+    ++ne;
+    if (nbr_slot < 0) {
+      if (nvtx >= MV) return;  // more vertices than the pattern (pv <= MV): not a hit
+      const EdgeAt ae = edge_at(g, e.y, e.x);  // e in the new vertex's list
+      const uint32_t nve = ae.pos + 1 + ae.suf;
+      const uint32_t nvl = lb_eid(g.adj_e, edge_at_start(g, ae, e.x), ae.pos + 1, mv, 0u, e.y);
+#pragma unroll
+      for (int i = 0; i < MV; ++i)
+        if (i == nvtx) {
+          vs[i] = e.x;
+          ve[i] = nve;
+          vl[i] = nvl;
+        }
+      ++nvtx;
+      if ((uint32_t)nvtx > pp.pv) return;
+    }
+  }
+  if ((uint32_t)nvtx != pp.pv) return;
+  // relabel by ascending vertex id (SamplerGenerator.cpp:493-527) and test the edge set
+  uint32_t rank[MV];
+#pragma unroll
+  for (int i = 0; i < MV; ++i) {
+    uint32_t rk = 0;
+#pragma unroll
+    for (int j = 0; j < MV; ++j) rk += (j < nvtx && vs[j] < vs[i]) ? 1u : 0u;
+    rank[i] = rk;
+  }
+  uint32_t mask = 0;
+#pragma unroll
+  for (int k = 0; k < ME; ++k) {
+    if (k >= ne) break;
+    const int a = (int)((es >> (4 * k)) & 15u), b = (int)((ed >> (4 * k)) & 15u);
+    uint32_t ri = 0, rj = 0;
+#pragma unroll
+    for (int i = 0; i < MV; ++i) {
+      if (i == a) ri = rank[i];
+      if (i == b) rj = rank[i];
+    }
+    mask |= 1u << pair_bit(ri, rj, pp.pv);
+  }
+  int lo = 0, hi = (int)pp.num_unique;
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (ZG_LDG(&pp.masks[mid]) < mask)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  r.hit = lo < (int)pp.num_unique && ZG_LDG(&pp.masks[lo]) == mask;
+}
+
 template <bool DBG>
 __device__ void prog_pattern(const ZgDevGraph& g, const ZgProgParams& pp, Ctx& c, Res& r) {
   if (g.m == 0) {
     r.fail = true;
+    return;
+  }
+  if (!DBG && pp.pv <= 5 && pp.pe <= 6) {  // 5-star, 5-house, triangle, ...: registers only
+    prog_pattern_small<5, 6>(g, pp, c, r);
     return;
   }
   uint64_t e0 = c.draw(0, g.m - 1);
