@@ -1143,13 +1143,13 @@ __device__ void prog_pattern(const ZgDevGraph& g, const ZgProgParams& pp, Ctx& c
 struct Acc {
   uint32_t samples, hits, fails, ovf;
   uint64_t s[4];
-  double sw, sw2;
+  double sw2;  // the mean's sum is the exact s[]; only the variance term is a double
 };
 
 __device__ __forceinline__ void acc_init(Acc& a) {
   a.samples = a.hits = a.fails = a.ovf = 0;
   a.s[0] = a.s[1] = a.s[2] = a.s[3] = 0;
-  a.sw = a.sw2 = 0.0;
+  a.sw2 = 0.0;
 }
 
 // num / 2^shift as a double truncated to 53 bits, built from integer operations only: GB300's
@@ -1270,39 +1270,36 @@ __device__ void block_reduce_store(Acc& a, ZgPartial* out) {
     v[4 + 2 * i] = (uint32_t)a.s[i];
     v[5 + 2 * i] = a.s[i] >> 32;
   }
-  double d0 = a.sw, d1 = a.sw2;
+  double d1 = a.sw2;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
 #pragma unroll
     for (int i = 0; i < 12; ++i) v[i] += __shfl_xor_sync(0xffffffffu, v[i], o);
-    d0 += __shfl_xor_sync(0xffffffffu, d0, o);
     d1 += __shfl_xor_sync(0xffffffffu, d1, o);
   }
   __shared__ unsigned long long sv[BLOCK / 32][12];
-  __shared__ double sd[BLOCK / 32][2];
+  __shared__ double sd[BLOCK / 32];
   int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (lane == 0) {
 #pragma unroll
     for (int i = 0; i < 12; ++i) sv[warp][i] = v[i];
-    sd[warp][0] = d0;
-    sd[warp][1] = d1;
+    sd[warp] = d1;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
     ZgPartial p;
     unsigned long long t[12] = {0};
-    double s0 = 0, s1 = 0;
+    double s1 = 0;
     for (int w = 0; w < BLOCK / 32; ++w) {
       for (int i = 0; i < 12; ++i) t[i] += sv[w][i];
-      s0 += sd[w][0];
-      s1 += sd[w][1];
+      s1 += sd[w];
     }
     p.samples = t[0];
     p.hits = t[1];
     p.fails = t[2];
     p.overflow = t[3];
     for (int i = 0; i < 8; ++i) p.lane[i] = t[4 + i];
-    p.sum_w = s0;
+    p.sum_w = 0.0;  // the counters take it from the exact sum
     p.sum_w2 = s1;
     *out = p;
   }
