@@ -324,7 +324,8 @@ def run_gb300(args):
         res = [Z.allgather_counters(r) for r in res]
 
     # end to end through the public API: calculate() per program, results read back each query
-    insts = [getattr(Z, c)(g, seed=seed + 7, stream_id=j + 11) for j, c in
+    # (each rank its own Philox streams, so the ranks draw different samples)
+    insts = [getattr(Z, c)(g, seed=seed + 7, stream_id=16 * rank + j + 11) for j, c in
              enumerate({"triangle": "TriangleCountingInstance", "four_clique": "FourCliqueCountingInstance",
                         "three_chain": "ThreeChainCountingInstance",
                         "four_chain": "FourChainCountingInstance"}[p] for p in names)]
