@@ -53,6 +53,22 @@ uint64_t zgo_draw(uint64_t seed, uint32_t stream, uint64_t sample, uint32_t d, u
   return lo + (uint64_t)(((u128)r * range) >> 64);
 }
 
+/* Estimator draw d of sample `sample`: two draws per Philox block, counter (sample_lo, sample_hi,
+ * d >> 1, stream), key (seed_lo, seed_hi); draw d takes the 64-bit word out1:out0 (d even) or
+ * out3:out2 (d odd), mapped to [lo, hi] by the multiply-high method.  (zgo_draw, one draw per
+ * block, stays for the graph shuffles and subsamples.) */
+uint64_t zgo_sample_draw(uint64_t seed, uint32_t stream, uint64_t sample, uint32_t d, uint64_t lo,
+                         uint64_t hi) {
+  uint32_t ctr[4] = {(uint32_t)sample, (uint32_t)(sample >> 32), d >> 1, stream};
+  uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+  uint32_t o[4];
+  zgo_philox4x32_10(ctr, key, o);
+  uint64_t r = (d & 1) ? (((uint64_t)o[3] << 32) | o[2]) : (((uint64_t)o[1] << 32) | o[0]);
+  uint64_t range = hi - lo + 1;
+  if (range == 0) return r;
+  return lo + (uint64_t)(((u128)r * range) >> 64);
+}
+
 /* ------------------------------------------------------------------------- */
 /* Graph: CSRConstructor::construct_bitmap_assisted_csr without its shuffle
  * (src/Graph.cpp:255-311): two half-edges per edge, appended in edge-id order, so every
@@ -174,7 +190,7 @@ static uint32_t zgo_model_search(uint64_t d) {
 }
 
 static uint64_t ctx_rand(zgo_ctx* c, uint64_t lo, uint64_t hi) {
-  uint64_t v = zgo_draw(c->seed, c->stream, c->sample, c->nd, lo, hi);
+  uint64_t v = zgo_sample_draw(c->seed, c->stream, c->sample, c->nd, lo, hi);
   if (c->nd < ZG_MAX_DRAWS) {
     c->tr->lo[c->nd] = lo; c->tr->hi[c->nd] = hi; c->tr->val[c->nd] = v;
   }

@@ -62,6 +62,8 @@ void zgo_program_free(zgo_program* p);
 void     zgo_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 uint64_t zgo_draw(uint64_t seed, uint32_t stream, uint64_t sample, uint32_t d,
                   uint64_t lo, uint64_t hi);
+uint64_t zgo_sample_draw(uint64_t seed, uint32_t stream, uint64_t sample, uint32_t d,
+                         uint64_t lo, uint64_t hi);
 
 /* One estimate() call for sample index `sample`; fills *tr (never NULL). Returns 0. */
 int zgo_sample(const zgo_graph* g, const zgo_program* p, uint64_t seed, uint32_t stream,

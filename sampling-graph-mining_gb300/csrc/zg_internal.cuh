@@ -135,9 +135,9 @@ struct ZgPartial {
 
 // ----------------------------------------------------------------------------------------
 // Philox4x32-10 (Salmon et al., SC'11); identical to the CPU oracle's.
-__host__ __device__ __forceinline__ void zg_philox(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
-                                                   uint32_t k0, uint32_t k1, uint32_t& o0,
-                                                   uint32_t& o1) {
+__host__ __device__ __forceinline__ void zg_philox4(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
+                                                    uint32_t k0, uint32_t k1, uint32_t& o0, uint32_t& o1,
+                                                    uint32_t& o2, uint32_t& o3) {
 #pragma unroll
   for (int r = 0; r < 10; ++r) {
     if (r) {
@@ -160,6 +160,14 @@ __host__ __device__ __forceinline__ void zg_philox(uint32_t c0, uint32_t c1, uin
   }
   o0 = c0;
   o1 = c1;
+  o2 = c2;
+  o3 = c3;
+}
+// The first two output words.
+__host__ __device__ __forceinline__ void zg_philox(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
+                                                   uint32_t k0, uint32_t k1, uint32_t& o0, uint32_t& o1) {
+  uint32_t o2, o3;
+  zg_philox4(c0, c1, c2, c3, k0, k1, o0, o1, o2, o3);
 }
 
 __host__ __device__ __forceinline__ uint64_t zg_mulhi64(uint64_t a, uint64_t b) {
@@ -177,6 +185,16 @@ __host__ __device__ __forceinline__ uint64_t zg_draw_word(uint64_t seed, uint32_
   zg_philox((uint32_t)sample, (uint32_t)(sample >> 32), d, stream, (uint32_t)seed,
             (uint32_t)(seed >> 32), o0, o1);
   return ((uint64_t)o1 << 32) | o0;
+}
+// The 64-bit word of an estimator's draw d: two draws per Philox block, counter (sample, d >> 1,
+// stream), key seed; draw d takes output words 1:0 (d even) or 3:2 (d odd).  A program's
+// consecutive draw pairs cost one Philox evaluation.  (Graph construction keeps zg_draw_word.)
+__host__ __device__ __forceinline__ uint64_t zg_sample_word(uint64_t seed, uint32_t stream, uint64_t sample,
+                                                            uint32_t d) {
+  uint32_t o0, o1, o2, o3;
+  zg_philox4((uint32_t)sample, (uint32_t)(sample >> 32), d >> 1, stream, (uint32_t)seed, (uint32_t)(seed >> 32),
+             o0, o1, o2, o3);
+  return (d & 1) ? (((uint64_t)o3 << 32) | o2) : (((uint64_t)o1 << 32) | o0);
 }
 // A draw's word mapped to [lo, hi] by multiply-high.
 __host__ __device__ __forceinline__ uint64_t zg_draw_map(uint64_t r, uint64_t lo, uint64_t hi) {

@@ -50,7 +50,7 @@ __device__ __forceinline__ void four_chain_grouped(const ZgDevGraph& g, uint64_t
     const uint64_t i = base + (uint64_t)k * stride + lane;
     const bool valid = i < n;
     if (!__ballot_sync(0xffffffffu, valid)) break;
-    const uint32_t sel = valid ? (uint32_t)zg_draw_map(zg_draw_word(seed, stream, first + i, 0), 1, 3) : 0u;
+    const uint32_t sel = valid ? (uint32_t)zg_draw_map(zg_sample_word(seed, stream, first + i, 0), 1, 3) : 0u;
     const unsigned m1 = __ballot_sync(0xffffffffu, sel == 1), m2 = __ballot_sync(0xffffffffu, sel == 2),
                    m3 = __ballot_sync(0xffffffffu, sel == 3);
     // every count is <= 31 before this round, so a queue of 64 never overflows
