@@ -173,7 +173,7 @@ def cpu_baseline(wl, edges, nv, threads, target_s=12.0):
 
 def time_to_bound(Z, g, names, acc, eps=0.01, conf=0.95, cap=1 << 37, coverage_queries=40):
     """Time from query submission (graph resident) to an answer whose empirical 95 % half-width is
-    <= 1 % of the estimate: plain ErrorProfile sizing vs the learned network, same judge (zg_query).
+    <= 1 % of the estimate: plain ErrorProfile sizing vs the learned network, same bound check (zg_query).
     For 4-cliques the unbiased canonical-path program runs: the reference's estimator is biased (it
     finds ~60 % of the cliques), so a tight interval around it is not an accuracy claim."""
     import elp_learn as EL
@@ -191,7 +191,7 @@ def time_to_bound(Z, g, names, acc, eps=0.01, conf=0.95, cap=1 << 37, coverage_q
             r[k]["rel_err_vs_exact"] = abs(r[k]["estimate"] - ex) / ex
         r["speedup_learned_over_plain"] = r["plain"]["seconds"] / r["learned"]["seconds"]
         out["patterns"][prog_name] = r
-    # delivered accuracy: triangle queries over independent seeds, learned sizing + judge
+    # delivered accuracy: triangle queries over independent seeds, learned sizing + bound check
     prog = Z.Program(1)
     ex = acc["triangle"]["exact"] if "triangle" in acc else g.exact_count(1)
     inside, met = 0, 0
@@ -524,7 +524,7 @@ def run_batch(args):
 
 def large_time_to_bound(Z, g, eps=0.01, conf=0.95, cap=1 << 37):
     """Triangle and (unbiased) 4-clique queries to 1 % at 95 % on the largest graph: learned-ELP
-    budget, then the empirical-CLT judge keeps sampling until the bound holds (or the cap)."""
+    budget, then the empirical-CLT bound check keeps sampling until the bound holds (or the cap)."""
     import elp_learn as EL
     model = os.path.join(ROOT, "sampling-graph-mining_gb300", "elp_mlp.npz")
     if not os.path.exists(model):

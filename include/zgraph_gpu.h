@@ -360,7 +360,7 @@ typedef struct zg_query_result {
   double   ms_total;
 } zg_query_result;
 /* A bounded query (no counterpart in the reference, whose ErrorProfile::run trusts its bound):
- * run n_initial estimators, judge the answer by its empirical CLT half-width, and keep sampling
+ * run n_initial estimators, check the answer's empirical CLT half-width, and keep sampling
  * fresh estimators until half_width <= error * estimate with at least 30 hits, or max_samples
  * (0: 2^40) is reached (then bound_met = 0). */
 int zg_query(const zg_graph* g, const zg_program* p, double error, double confidence,
@@ -406,7 +406,7 @@ int zg_elp_learned(const zg_mlp* net, const zg_graph* g, const zg_program* p, do
                    double confidence, uint64_t pilot_samples, uint64_t seed, void* cuda_stream,
                    uint64_t* n_required, float* prediction);
 /* zg_elp_learned (2^16-sample pilot from feature_seed), then zg_query from query_seed.  A budget
- * above 2^30 samples runs in two looks: half of it first, then what the judge still needs, so an
+ * above 2^30 samples runs in two looks: half of it first, then what the bound check still needs, so an
  * over-predicted budget costs at most half of it in extra samples.  n_required may be NULL. */
 int zg_query_learned(const zg_mlp* net, const zg_graph* g, const zg_program* p, double error,
                      double confidence, uint64_t max_samples, uint64_t feature_seed, uint64_t query_seed,

@@ -6,7 +6,7 @@
 //                    moving-average regression and the Chernoff-style bound, host side.
 //   zg_elp_solve     the host half alone (testable without a GPU).
 //   zg_time_profile  TimeProfile<E>::run (:25-47): doubling runs under a wall-clock budget.
-//   zg_query         run a budget, judge the answer by its empirical CLT half-width at the requested
+//   zg_query         run a budget, check the answer's empirical CLT half-width at the requested
 //                    confidence and keep sampling until the bound holds: the delivered error never
 //                    depends on how the budget was chosen.
 #include <math.h>
@@ -231,7 +231,7 @@ extern "C" int zg_time_profile(const zg_graph* g, const zg_program* p, uint32_t 
   return ZG_OK;
 }
 
-// Bounded query: sample n_initial estimators (the sizing step's budget), then judge the answer by
+// Bounded query: sample n_initial estimators (the sizing step's budget), then check the answer by
 // its CLT half-width z * sqrt(var / n) at `conf`; while it exceeds eps * estimate, extend with more
 // estimators (never reusing sample indices) sized from the current variance, up to max_samples.
 extern "C" int zg_query(const zg_graph* g, const zg_program* p, double eps, double conf, uint64_t n_initial,

@@ -4,7 +4,7 @@ network by the library's own CUDA kernels, and budget sizing.
 The network (zg_mlp_*) maps 16 query features (zg_graph_features: degree statistics of the
 graph, the pattern class, a 2^16-estimator pilot) to log2 of the per-sample relative variance
 Var(1/p) / E(1/p)^2 and log2 of the per-sample latency.  For a target error eps at confidence
-conf the budget is n = z^2 * cv2 / eps^2; zg_query then judges the answer by its empirical
+conf the budget is n = z^2 * cv2 / eps^2; zg_query then checks the answer against its empirical
 bound and keeps sampling if needed, so a wrong prediction costs time, never accuracy.
 
 Training rows come from the plain estimator on seeded synthetic graphs: R-MAT with a in
@@ -115,7 +115,7 @@ def train(X, Y, seed=3, epochs=400, batch=32, lr=2e-3):
 
 
 def compare(net, graph, name, eps=0.01, conf=0.95, seed=5, max_samples=1 << 36):
-    """Time to an answer that meets (eps, conf): plain ELP sizing vs learned sizing, same judge."""
+    """Time to an answer that meets (eps, conf): plain ELP sizing vs learned sizing, same bound check."""
     kind, param, pat = PATTERNS[name]
     prog = Z.Program(kind, param, pat)
     out = {"pattern": name}
@@ -162,7 +162,7 @@ def main():
     rep["heldout_rmse_log2_cv2"] = float(np.sqrt(np.mean((ph[:, 0] - Yh[:, 0]) ** 2)))
     rep["heldout_rmse_log2_ns"] = float(np.sqrt(np.mean((ph[:, 1] - Yh[:, 1]) ** 2)))
     rep["heldout_rmse_pilot_only"] = float(np.sqrt(np.mean((Xh[:, 15] - Yh[:, 0]) ** 2)))
-    # time to a 1 % / 95 % answer on the held-out graphs: learned vs plain sizing, same judge
+    # time to a 1 % / 95 % answer on the held-out graphs: learned vs plain sizing, same bound check
     rows = []
     for spec in specs[args.graphs:]:
         g = build_graph(spec)

@@ -569,7 +569,7 @@ def time_profile(graph, program, time_limit_ms, seed, stream_id=0):
 
 
 def query(graph, program, eps, conf, n_initial, seed, stream_id=0, max_samples=0, cuda_stream=None):
-    """zg_query: budgeted run judged by its empirical CLT bound, extended until the bound holds."""
+    """zg_query: budgeted run checked against its empirical CLT bound, extended until the bound holds."""
     out = QueryResult()
     check(lib().zg_query(graph.handle, program.handle, eps, conf, n_initial, max_samples, seed, stream_id,
                          cuda_stream, C.byref(out)))
@@ -711,7 +711,7 @@ def learned_budget(mlp, graph, program, eps, conf, seed=1, pilot_samples=1 << 16
 
 
 def learned_query(mlp, graph, program, eps, conf, seed, query_seed, stream_id=0, max_samples=0, cuda_stream=None):
-    """zg_query_learned: learned sizing (2^16-sample pilot from seed), then the judge from query_seed;
+    """zg_query_learned: learned sizing (2^16-sample pilot from seed), then the bound check from query_seed;
     a budget above 2^30 samples runs in two looks (half first).  Returns (QueryResult, budget)."""
     n = C.c_uint64(0)
     out = QueryResult()

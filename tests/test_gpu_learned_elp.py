@@ -97,7 +97,7 @@ def test_features_match_host():
 
 def test_learned_budget_and_query_entry_points():
     """zg_elp_learned is the sizing formula on the network's prediction for the query's features;
-    zg_query_learned runs it and judges the answer, half of a long budget first."""
+    zg_query_learned runs it and checks the answer's bound, half of a long budget first."""
     e = Z.gen_rmat(12, 10, seed=8)
     g = Z.Graph.from_edges(e, 1 << 12)
     net = Z.Mlp(5)
@@ -112,7 +112,7 @@ def test_learned_budget_and_query_entry_points():
     assert n == max(int(z * z * 2.0 ** float(y_ref[0]) / 0.02 ** 2), 1 << 16)
     q, n2 = Z.learned_query(net, g, p, 0.02, 0.95, 4, 77, stream_id=3, max_samples=1 << 32)
     assert n2 == n and q.bound_met and q.rel_half_width <= 0.02
-    # the judge's first round ran the budget (below 2^30: one look), continued from the same stream
+    # the first round of the bound check ran the budget (below 2^30: one look), continued from the same stream
     first = Z.query(g, p, 0.02, 0.95, n, 77, stream_id=3, max_samples=1 << 32)
     assert (q.samples, q.estimate) == (first.samples, first.estimate)
 
