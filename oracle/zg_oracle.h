@@ -3,8 +3,8 @@
  *
  * A plain-C restatement of jy-yuan/sampling-graph-mining's neighbour-sampling estimator
  * path, used to check libzgraph_gpu.so.  Only tests/, __graft_entry__.smoke() and
- * bench.py's cpu_baseline / --impl reference legs may load it, and only as the checker or
- * the timed CPU baseline; the product path never calls it.
+ * bench.py's cpu_baseline / --impl reference legs may load it, and only to check results or
+ * as the timed CPU baseline; the product path never calls it.
  *
  * Parity is pinned: tests/golden/ holds per-sample outcomes produced by the reference's own
  * sources (compiled by oracle/build_ref.sh against a replaying Random), and this restatement

@@ -86,7 +86,7 @@ extern "C" int zg_init(int device) {
   cudaDeviceProp prop;
   ZG_CUDA(cudaGetDeviceProperties(&prop, device));
   if (prop.major * 10 + prop.minor != 103) {
-    zg_set_error(ZG_ERR_NO_DEVICE, "device %d is sm_%d%d; this build targets sm_103a", device, prop.major,
+    zg_set_error(ZG_ERR_NO_DEVICE, "device %d is sm_%d%d; the library targets sm_103a", device, prop.major,
                  prop.minor);
     return ZG_ERR_NO_DEVICE;
   }
