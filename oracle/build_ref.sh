@@ -4,6 +4,8 @@
 #
 #   * src/*.cpp (except Random.cpp) + a replaying Random + single-rank MPI / one-node NUMA
 #     shims  ->  one driver .so per application (oracle/ref/app_*.cpp include the app source);
+#   * the same with the reference's own Random.cpp  ->  libzgtime_*.so, which time its
+#     calculate() (oracle/ref/time_app.cpp);
 #   * naive_implementation/*.cpp  ->  executables (with a zero-filling operator new[]);
 #   * tests/Test{Pattern,Pattern2,Subgraph,Regression}.cpp  ->  executables.
 #
@@ -32,6 +34,18 @@ wait
 
 for app in triangle four_clique three_chain four_chain chain pred_triangle three_motif pattern; do
   $CXX $FLAGS $INC -shared -o "$OUT/libzgref_$app.so" "$HERE/ref/app_$app.cpp" "$OUT"/obj/*.o -lm &
+done
+wait
+
+# timing drivers: the applications with the reference's own Random (mt19937) and OpenMP threads
+mkdir -p "$OUT/obj_time"
+$CXX $FLAGS $INC -c "$REF/src/Random.cpp" -o "$OUT/obj_time/Random.o"
+TIME_OBJS=$(ls "$OUT"/obj/*.o | grep -v -e replay_random.o -e zg_oracle.o)
+for pair in triangle:Triangle:TriangleCoutingInstance four_clique:FourClique:FourCliqueCountingInstance \
+            three_chain:ThreeChain:ThreeChainCountingInstance four_chain:FourChain:FourChainCountingInstance; do
+  app=${pair%%:*}; rest=${pair#*:}; file=${rest%%:*}; cls=${rest#*:}
+  $CXX $FLAGS $INC -DZGREF_APP_FILE="\"applications/$file.cpp\"" -DZGREF_APP_CLASS=$cls -shared \
+       -o "$OUT/libzgtime_$app.so" "$HERE/ref/time_app.cpp" $TIME_OBJS "$OUT/obj_time/Random.o" -lm &
 done
 wait
 
