@@ -76,6 +76,7 @@ extern "C" {
 
 typedef struct zg_graph zg_graph;     /* device-resident graph (opaque)   */
 typedef struct zg_program zg_program; /* estimator program (opaque)       */
+typedef struct zg_mlp zg_mlp;         /* learned-profile network (opaque) */
 
 /* Graph metadata.  num_edges / max_degree are the reference's Graph<E>::num_edges and
  * ::max_degree (include/Graph.hpp:155-158), which GraphSampler/GraphFilter rescale; the
@@ -289,6 +290,14 @@ int zg_batch_submit(zg_batch* b, const zg_batch_query* queries, uint32_t nq, voi
 /* Waits for the submitted batch; out[2i] receives query i's counters (ZG_QUERY_THREE_MOTIF:
  * out[2i] the 3-chain, out[2i+1] the triangle). */
 int zg_batch_wait(zg_batch* b, zg_counters* out);
+/* Learned sizing for a batch (no counterpart in the reference): every query with n == 0 gets the
+ * learned profile's budget for (error, confidence), from one pilot batch (pilot_samples per query,
+ * 0: 2^16, on the pilot stream zg_graph_features uses: first sample 0, stream ZG_ELP_STREAM + 1,
+ * the query's seed), the degree statistics of its graph (base or filtered) and one prediction for
+ * all of them; n as zg_elp_learned computes it.  Queries with n > 0 are left as they are; a 3-motif
+ * query needs its n.  Runs the batch (so not while one of its batches is pending). */
+int zg_batch_size_learned(zg_batch* b, const zg_mlp* net, zg_batch_query* queries, uint32_t nq,
+                          double error, double confidence, uint64_t pilot_samples, void* cuda_stream);
 /* Device time of the last waited batch (CUDA events around its graph launch), in ms. */
 int zg_batch_elapsed_ms(const zg_batch* b, float* ms);
 /* The cached filtered graph of a predicate (built if missing): what a filtered query samples. */
@@ -377,7 +386,6 @@ int zg_query(const zg_graph* g, const zg_program* p, double error, double confid
 #define ZG_MLP_FEATURES 16
 #define ZG_MLP_OUTPUTS  2
 #define ZG_MLP_PARAMS   5378
-typedef struct zg_mlp zg_mlp;
 int zg_mlp_num_params(void);
 int zg_mlp_create(uint64_t seed, zg_mlp** out);
 int zg_mlp_free(zg_mlp* net);

@@ -586,6 +586,56 @@ extern "C" int zg_batch_wait(zg_batch* b, zg_counters* out) {
   return ZG_OK;
 }
 
+extern "C" int zg_batch_size_learned(zg_batch* b, const zg_mlp* net, zg_batch_query* q, uint32_t nq, double error,
+                                     double confidence, uint64_t pilot_samples, void* cuda_stream) {
+  if (!b || !net || (nq && !q))
+    return zg_set_error(ZG_ERR_INVALID_ARG, "zg_batch_size_learned: null argument"), ZG_ERR_INVALID_ARG;
+  if (!(error > 0) || !(confidence > 0 && confidence < 1))
+    return zg_set_error(ZG_ERR_INVALID_ARG, "zg_batch_size_learned: error %g / confidence %g", error, confidence),
+           ZG_ERR_INVALID_ARG;
+  if (pilot_samples == 0) pilot_samples = 1ull << 16;
+  cudaStream_t s = (cudaStream_t)cuda_stream;
+  // the queries to size, as pilot queries: the pilot zg_graph_features would run for each
+  std::vector<uint32_t> idx;
+  std::vector<zg_batch_query> pilot;
+  for (uint32_t i = 0; i < nq; ++i) {
+    if (q[i].n != 0) continue;
+    if (q[i].kind == ZG_QUERY_THREE_MOTIF)
+      return zg_set_error(ZG_ERR_INVALID_ARG, "query %u: a 3-motif query needs its sample count", i),
+             ZG_ERR_INVALID_ARG;
+    zg_batch_query x = q[i];
+    x.n = pilot_samples;
+    x.first_sample = 0;
+    x.stream_id = ZG_ELP_STREAM + 1;
+    idx.push_back(i);
+    pilot.push_back(x);
+  }
+  if (idx.empty()) return ZG_OK;
+  const uint32_t k = (uint32_t)idx.size();
+  std::vector<zg_counters> c(2 * (size_t)k);
+  int rc = zg_batch_submit(b, pilot.data(), k, cuda_stream);
+  if (rc == ZG_OK) rc = zg_batch_wait(b, c.data());
+  if (rc) return rc;
+  // features: the query graph's degree statistics, the program class, the pilot
+  std::vector<float> X((size_t)k * ZG_MLP_FEATURES), Y((size_t)k * ZG_MLP_OUTPUTS);
+  std::vector<const zg_graph*> none;
+  for (uint32_t j = 0; j < k && rc == ZG_OK; ++j) {
+    const zg_batch_query& x = q[idx[j]];
+    const zg_graph* g = b->base;
+    if (x.pred_op) rc = batch_filtered(b, x.pred_op, x.t0, x.t1, s, none, &g);
+    zg_program* own = nullptr;
+    if (rc == ZG_OK && x.kind != ZG_PROG_PATTERN) rc = zg_program_create(x.kind, x.param, &own);
+    float* f = &X[(size_t)j * ZG_MLP_FEATURES];
+    if (rc == ZG_OK) rc = zg_degree_features(g, s, f);
+    if (rc == ZG_OK) zg_query_features(own ? own : x.program, c[2 * j], f);
+    if (own) zg_program_free(own);
+  }
+  if (rc == ZG_OK) rc = zg_mlp_predict(net, X.data(), k, Y.data());
+  if (rc) return rc;
+  for (uint32_t j = 0; j < k; ++j) q[idx[j]].n = zg_learned_n(Y[(size_t)j * ZG_MLP_OUTPUTS], error, confidence);
+  return ZG_OK;
+}
+
 extern "C" int zg_batch_tune(zg_batch* b, const zg_batch_query* q, uint32_t nq, void* cuda_stream, int* best_variant,
                              float* ms_per_variant) {
   if (!b || !q) return zg_set_error(ZG_ERR_INVALID_ARG, "zg_batch_tune: null argument"), ZG_ERR_INVALID_ARG;

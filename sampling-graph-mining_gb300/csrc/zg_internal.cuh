@@ -249,3 +249,10 @@ int zg_num_sms();
 // default pool returns them at every synchronisation, and mapping them again cost ~0.1 ms per
 // call); free with cudaFreeAsync.
 cudaError_t zg_malloc_async(void** p, size_t bytes, cudaStream_t s);
+
+// Learned-profile helpers shared by zg_mlp.cu and zg_batch.cu: the graph's eight degree features
+// (f[0..7], the rest zeroed), the program and pilot features (f[8..15]) from a pilot run's
+// counters, and the budget for a predicted log2 relative variance.
+int zg_degree_features(const zg_graph* g, cudaStream_t s, float* f);
+void zg_query_features(const zg_program* p, const zg_counters& c, float* f);
+uint64_t zg_learned_n(float pred_log2_cv2, double error, double confidence);

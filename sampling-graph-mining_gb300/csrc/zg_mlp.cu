@@ -525,12 +525,10 @@ float lg2(double x) { return (float)log2(x > 1e-300 ? x : 1e-300); }
 // pattern one-hot (triangle, 4-clique, 3-chain, 4-chain/k-chain, tree pattern, cyclic pattern),
 // and from a pilot run of pilot_samples estimators (stream ZG_ELP_STREAM + 1): log2 hit rate and
 // log2 per-sample relative variance.
-extern "C" int zg_graph_features(const zg_graph* g, const zg_program* p, uint64_t pilot_samples, uint64_t seed,
-                                 void* cuda_stream, float* f) {
-  if (!g || !p || !f) return zg_set_error(ZG_ERR_INVALID_ARG, "zg_graph_features: null argument"), ZG_ERR_INVALID_ARG;
-  cudaStream_t s = (cudaStream_t)cuda_stream;
-  int rc0 = deg_stats(g, s);
-  if (rc0) return rc0;
+// The graph part of the features (f[0..7]; the rest zeroed).
+int zg_degree_features(const zg_graph* g, cudaStream_t s, float* f) {
+  int rc = deg_stats(g, s);
+  if (rc) return rc;
   const double* h = g->deg_stats;
   double m = (double)g->d.m, nz = h[5] > 0 ? h[5] : 1.0;
   for (int i = 0; i < IN; ++i) f[i] = 0.f;
@@ -542,16 +540,38 @@ extern "C" int zg_graph_features(const zg_graph* g, const zg_program* p, uint64_
   f[5] = lg2(h[2] / nz);
   f[6] = lg2(m > 0 ? h[4] / m : 0);
   f[7] = lg2(m > 0 ? h[3] / m : 0);
+  return ZG_OK;
+}
+
+// The program and pilot parts: the pattern class one-hot and, from a pilot run's counters, the
+// hit rate and the per-sample relative variance.
+void zg_query_features(const zg_program* p, const zg_counters& c, float* f) {
   f[8 + pattern_slot(p)] = 1.f;
-  zg_counters c;
-  if (pilot_samples == 0) pilot_samples = 1ull << 16;
-  int rc = zg_run(g, p, pilot_samples, 0, seed, ZG_ELP_STREAM + 1, cuda_stream, &c);
-  if (rc) return rc;
   double n = (double)c.samples;
   double mean = c.estimate;
   double cv2 = (c.hits >= 2 && mean > 0) ? (c.sum_w2 / n) / (mean * mean) - 1.0 : n;
   f[14] = lg2(((double)c.hits + 0.5) / n);
   f[15] = lg2(cv2 > 1e-12 ? cv2 : 1e-12);
+}
+
+// The learned budget for a prediction: n = z^2 * 2^pred / error^2, at least 2^16.
+uint64_t zg_learned_n(float pred_log2_cv2, double error, double confidence) {
+  const double z = zg_normal_quantile(1.0 - (1.0 - confidence) / 2.0);
+  const double n = z * z * exp2((double)pred_log2_cv2) / (error * error);
+  const double lo = (double)(1ull << 16), hi = 1e18;
+  return n >= hi ? (uint64_t)hi : n <= lo ? (uint64_t)lo : (uint64_t)n;
+}
+
+extern "C" int zg_graph_features(const zg_graph* g, const zg_program* p, uint64_t pilot_samples, uint64_t seed,
+                                 void* cuda_stream, float* f) {
+  if (!g || !p || !f) return zg_set_error(ZG_ERR_INVALID_ARG, "zg_graph_features: null argument"), ZG_ERR_INVALID_ARG;
+  int rc = zg_degree_features(g, (cudaStream_t)cuda_stream, f);
+  if (rc) return rc;
+  zg_counters c;
+  if (pilot_samples == 0) pilot_samples = 1ull << 16;
+  rc = zg_run(g, p, pilot_samples, 0, seed, ZG_ELP_STREAM + 1, cuda_stream, &c);
+  if (rc) return rc;
+  zg_query_features(p, c, f);
   return ZG_OK;
 }
 
@@ -568,10 +588,7 @@ extern "C" int zg_elp_learned(const zg_mlp* net, const zg_graph* g, const zg_pro
   int rc = zg_graph_features(g, p, pilot_samples, seed, cuda_stream, f);
   if (rc) return rc;
   if ((rc = zg_mlp_predict(net, f, 1, y))) return rc;
-  const double z = zg_normal_quantile(1.0 - (1.0 - confidence) / 2.0);
-  const double n = z * z * exp2((double)y[0]) / (error * error);
-  const double lo = (double)(1ull << 16), hi = 1e18;
-  *n_required = n >= hi ? (uint64_t)hi : n <= lo ? (uint64_t)lo : (uint64_t)n;
+  *n_required = zg_learned_n(y[0], error, confidence);
   if (prediction) {
     prediction[0] = y[0];
     prediction[1] = y[1];

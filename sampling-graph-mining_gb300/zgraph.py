@@ -166,6 +166,7 @@ def lib():
             "zg_batch_free": ([P], I32),
             "zg_batch_submit": ([P, P, U32, P], I32),
             "zg_batch_wait": ([P, P], I32),
+            "zg_batch_size_learned": ([P, P, P, U32, D, D, U64, P], I32),
             "zg_batch_filtered_graph": ([P, I32, I64, I64, P, C.POINTER(P)], I32),
             "zg_batch_tune": ([P, P, U32, P, C.POINTER(I32), P], I32),
             "zg_batch_elapsed_ms": ([P, C.POINTER(C.c_float)], I32),
@@ -404,7 +405,7 @@ class Batch:
             arr[i].stream_id = q.get("stream_id", 0)
             arr[i].t0 = q.get("t0", 0)
             arr[i].t1 = q.get("t1", 0)
-            arr[i].n = q["n"]
+            arr[i].n = q.get("n", 0)
             arr[i].seed = q["seed"]
             arr[i].first_sample = q.get("first_sample", 0)
             prog = q.get("program")
@@ -429,6 +430,16 @@ class Batch:
     def run(self, qs, cuda_stream=None):
         self.submit(qs, cuda_stream)
         return self.wait()
+
+    def size_learned(self, mlp, qs, eps, conf, pilot_samples=1 << 16, cuda_stream=None):
+        """zg_batch_size_learned: the learned budget of every query without an "n" (one pilot
+        batch, one prediction); returns the queries with "n" filled in."""
+        qs = [dict(q) for q in qs]
+        arr, nq, keep = self.queries(qs)
+        check(lib().zg_batch_size_learned(self._h, mlp._h, arr, nq, eps, conf, pilot_samples, cuda_stream))
+        for i, q in enumerate(qs):
+            q["n"] = int(arr[i].n)
+        return qs
 
     def elapsed_ms(self):
         """Device time of the last waited batch (CUDA events around its graph launch)."""

@@ -149,3 +149,32 @@ def test_pattern_queries_and_first_sample(wgraph):
         p = q.get("program") or Z.Program(q["kind"])
         _same(c, p.run(gg, q["n"], q["seed"], stream_id=q.get("stream_id", 0),
                        first_sample=q.get("first_sample", 0)), q)
+
+
+def test_learned_sizing_of_a_batch(wgraph):
+    """zg_batch_size_learned fills the n of every query without one, from one pilot batch and one
+    prediction, equal (to the last bit of the pilot's variance term) to zg_elp_learned per query."""
+    rng = np.random.default_rng(12)
+    net = Z.Mlp(3)
+    net.train(rng.normal(size=(64, 16)).astype(np.float32), (rng.normal(size=(64, 2)) + 8).astype(np.float32),
+              epochs=2, batch=32, lr=1e-3)
+    star = Z.Program(Z.PROG_PATTERN, pattern=(5, [(0, 1), (0, 2), (0, 3), (0, 4)]))
+    qs = [{"kind": Z.PROG_TRIANGLE, "seed": 5},
+          {"kind": Z.PROG_TRIANGLE, "seed": 6, "pred_op": Z.PRED_GE, "t0": 40},
+          {"kind": Z.PROG_FOUR_CHAIN, "seed": 7, "n": 12345},
+          {"kind": Z.PROG_PATTERN, "program": star, "seed": 8},
+          {"kind": Z.PROG_THREE_CHAIN, "seed": 9, "stream_id": 3}]
+    b = Z.Batch(wgraph, max_queries=16)
+    sized = b.size_learned(net, qs, 0.02, 0.95)
+    assert sized[2]["n"] == 12345
+    for q, s in zip(qs, sized):
+        if "n" in q:
+            continue
+        gg = b.filtered_graph(q["pred_op"], q["t0"]) if q.get("pred_op") else wgraph
+        p = q.get("program") or Z.Program(q["kind"])
+        n, _, _ = Z.learned_budget(net, gg, p, 0.02, 0.95, seed=q["seed"])
+        assert abs(s["n"] - n) <= 1e-6 * n + 1, (q, s["n"], n)
+    res = b.run(sized)
+    assert all(c.samples == q["n"] for (c, _), q in zip(res, sized))
+    with pytest.raises(Z.ZgError):
+        b.size_learned(net, [{"kind": Z.QUERY_THREE_MOTIF, "seed": 1}], 0.02, 0.95)
