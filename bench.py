@@ -519,7 +519,31 @@ def run_batch(args):
                            for name, (c, _) in zip(["four_clique", "five_star", "five_house"], res)}
         if not args.no_time_to_bound:
             line["time_to_bound"] = large_time_to_bound(Z, g)
+    elif not args.no_time_to_bound:
+        line["learned_batch"] = learned_batch(Z, b, qs)
     print(json.dumps(line), flush=True)
+
+
+def learned_batch(Z, b, qs, eps=0.05, conf=0.95):
+    """The same queries to eps at conf: learned sizing of the whole batch (zg_batch_size_learned:
+    one pilot batch, one prediction; 3-motif queries keep their budgets), one batch, then top-up
+    batches for the answers whose empirical bound does not hold yet (Batch.bounded)."""
+    model = os.path.join(ROOT, "sampling-graph-mining_gb300", "elp_mlp.npz")
+    if not os.path.exists(model):
+        return {"skipped": "no trained network at %s" % model}
+    net = Z.Mlp.load(model)
+    lqs = [q if q["kind"] == Z.QUERY_THREE_MOTIF else {k: v for k, v in q.items() if k != "n"} for q in qs]
+    t0 = time.perf_counter()
+    sized = b.size_learned(net, lqs, eps, conf)
+    sizing_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    total, met, rounds = b.bounded(net, lqs, eps, conf)
+    wall = time.perf_counter() - t0
+    sized_q = [i for i, q in enumerate(lqs) if q["kind"] != Z.QUERY_THREE_MOTIF]
+    return {"eps": eps, "confidence": conf, "queries_sized": len(sized_q), "sizing_s": sizing_s,
+            "sized_samples": sum(sized[i]["n"] for i in sized_q),
+            "bounded_s": wall, "rounds": rounds, "samples": sum(total[i].samples for i in sized_q),
+            "bound_met": sum(1 for i in sized_q if met[i])}
 
 
 def large_time_to_bound(Z, g, eps=0.01, conf=0.95, cap=1 << 37):

@@ -178,3 +178,28 @@ def test_learned_sizing_of_a_batch(wgraph):
     assert all(c.samples == q["n"] for (c, _), q in zip(res, sized))
     with pytest.raises(Z.ZgError):
         b.size_learned(net, [{"kind": Z.QUERY_THREE_MOTIF, "seed": 1}], 0.02, 0.95)
+
+
+def test_bounded_batch_tops_up_until_the_bound_holds(wgraph):
+    """Batch.bounded: learned sizing, one batch, top-up batches on fresh sample indices for the
+    answers still outside the bound; each merged answer equals one run over all its samples."""
+    rng = np.random.default_rng(13)
+    net = Z.Mlp(4)
+    net.train(rng.normal(size=(64, 16)).astype(np.float32), (rng.normal(size=(64, 2)) + 2).astype(np.float32),
+              epochs=2, batch=32, lr=1e-3)  # predicts small variances: the top-ups do the work
+    qs = [{"kind": Z.PROG_TRIANGLE, "seed": 21, "stream_id": 2},
+          {"kind": Z.PROG_TRIANGLE, "seed": 22, "pred_op": Z.PRED_LT, "t0": 70},
+          {"kind": Z.PROG_THREE_CHAIN, "seed": 23, "first_sample": 1000},
+          {"kind": Z.PROG_FOUR_CHAIN, "seed": 24}]
+    b = Z.Batch(wgraph, max_queries=8)
+    total, met, rounds = b.bounded(net, qs, 0.05, 0.95, max_rounds=6)
+    assert all(met) and rounds >= 1
+    z = Z.lib().zg_normal_quantile(0.975)
+    for q, c in zip(qs, total):
+        var = max(c.sum_w2 / c.samples - c.estimate ** 2, 0.0)
+        assert z * (var / c.samples) ** 0.5 <= 0.05 * c.estimate
+        gg = b.filtered_graph(q["pred_op"], q["t0"]) if q.get("pred_op") else wgraph
+        one = Z.Program(q["kind"]).run(gg, c.samples, q["seed"], stream_id=q.get("stream_id", 0),
+                                       first_sample=q.get("first_sample", 0))
+        assert (one.samples, one.hits, one.fails) == (c.samples, c.hits, c.fails)
+        assert [int(x) for x in one.sum_num] == [int(x) for x in c.sum_num] and one.estimate == c.estimate
