@@ -298,6 +298,16 @@ int zg_batch_wait(zg_batch* b, zg_counters* out);
  * query needs its n.  Runs the batch (so not while one of its batches is pending). */
 int zg_batch_size_learned(zg_batch* b, const zg_mlp* net, zg_batch_query* queries, uint32_t nq,
                           double error, double confidence, uint64_t pilot_samples, void* cuda_stream);
+/* The batch counterpart of zg_query_learned (no counterpart in the reference): learned sizing of
+ * the queries without a sample count (zg_batch_size_learned), one batch, then further batches for
+ * the answers whose empirical CLT half-width is still above error * estimate (at least 30 hits),
+ * each topped up to what its observed variance needs (+10 %) on fresh sample indices and merged
+ * exactly (an answer equals one run over all its samples), for at most max_rounds batches (0: 4)
+ * and max_samples per query (0: 2^40).  3-motif queries run their given budgets once.  out: two
+ * zg_counters per query as zg_batch_wait; bound_met: one flag per query; *rounds_run may be NULL. */
+int zg_batch_bounded(zg_batch* b, const zg_mlp* net, const zg_batch_query* queries, uint32_t nq,
+                     double error, double confidence, uint32_t max_rounds, uint64_t max_samples,
+                     void* cuda_stream, zg_counters* out, uint32_t* bound_met, uint32_t* rounds_run);
 /* Device time of the last waited batch (CUDA events around its graph launch), in ms. */
 int zg_batch_elapsed_ms(const zg_batch* b, float* ms);
 /* The cached filtered graph of a predicate (built if missing): what a filtered query samples. */

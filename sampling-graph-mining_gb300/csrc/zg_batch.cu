@@ -16,6 +16,7 @@
 //     instantiated once and replayed by every submit: the kernels read the batch size from
 //     device memory, so one graph serves every batch up to the object's capacity.
 #include <algorithm>
+#include <math.h>
 #include <map>
 #include <tuple>
 #include <vector>
@@ -633,6 +634,102 @@ extern "C" int zg_batch_size_learned(zg_batch* b, const zg_mlp* net, zg_batch_qu
   if (rc == ZG_OK) rc = zg_mlp_predict(net, X.data(), k, Y.data());
   if (rc) return rc;
   for (uint32_t j = 0; j < k; ++j) q[idx[j]].n = zg_learned_n(Y[(size_t)j * ZG_MLP_OUTPUTS], error, confidence);
+  return ZG_OK;
+}
+
+double zg_exact_mean_host(const uint64_t s[5], uint32_t den, uint64_t n);
+
+namespace {
+double exact_mean_of(const zg_counters& c) { return zg_exact_mean_host(c.sum_num, c.den_log2, c.samples); }
+// a += c for two runs of one query over disjoint sample ranges (same den_log2): exact.
+void merge_into(zg_counters& a, const zg_counters& c) {
+  unsigned __int128 carry = 0;
+  for (int i = 0; i < 5; ++i) {
+    unsigned __int128 t = (unsigned __int128)a.sum_num[i] + c.sum_num[i] + carry;
+    a.sum_num[i] = (uint64_t)t;
+    carry = t >> 64;
+  }
+  a.samples += c.samples;
+  a.hits += c.hits;
+  a.fails += c.fails;
+  a.overflow |= c.overflow;
+  a.sum_w2 += c.sum_w2;
+  a.estimate = exact_mean_of(a);
+  a.sum_w = zg_exact_mean_host(a.sum_num, a.den_log2, 1);  // the exact sum, rounded once
+}
+}  // namespace
+
+extern "C" int zg_batch_bounded(zg_batch* b, const zg_mlp* net, const zg_batch_query* q, uint32_t nq, double error,
+                                double confidence, uint32_t max_rounds, uint64_t max_samples, void* cuda_stream,
+                                zg_counters* out, uint32_t* bound_met, uint32_t* rounds_run) {
+  if (!b || !net || (nq && (!q || !out || !bound_met)))
+    return zg_set_error(ZG_ERR_INVALID_ARG, "zg_batch_bounded: null argument"), ZG_ERR_INVALID_ARG;
+  if (max_rounds == 0) max_rounds = 4;
+  if (max_samples == 0) max_samples = 1ull << 40;
+  std::vector<zg_batch_query> sized(q, q + nq);
+  int rc = zg_batch_size_learned(b, net, sized.data(), nq, error, confidence, 0, cuda_stream);
+  if (rc) return rc;
+  const double z = zg_normal_quantile(1.0 - (1.0 - confidence) / 2.0);
+  std::vector<uint64_t> ran(nq, 0), want(nq);
+  std::vector<uint32_t> pending;
+  for (uint32_t i = 0; i < nq; ++i) {
+    want[i] = sized[i].n;
+    bound_met[i] = 0;
+    pending.push_back(i);
+    memset(&out[2 * i], 0, 2 * sizeof(zg_counters));
+  }
+  uint32_t rounds = 0;
+  std::vector<zg_batch_query> sub;
+  std::vector<zg_counters> res;
+  while (!pending.empty() && rounds < max_rounds) {
+    sub.clear();
+    for (uint32_t i : pending) {
+      zg_batch_query x = sized[i];
+      x.n = want[i];
+      x.first_sample = sized[i].first_sample + ran[i];  // fresh sample indices
+      sub.push_back(x);
+    }
+    res.assign(2 * sub.size(), zg_counters{});
+    if ((rc = zg_batch_submit(b, sub.data(), (uint32_t)sub.size(), cuda_stream)) ||
+        (rc = zg_batch_wait(b, res.data())))
+      return rc;
+    ++rounds;
+    std::vector<uint32_t> next;
+    for (size_t j = 0; j < pending.size(); ++j) {
+      const uint32_t i = pending[j];
+      if (sized[i].kind == ZG_QUERY_THREE_MOTIF) {  // its given budgets, once
+        out[2 * i] = res[2 * j];
+        out[2 * i + 1] = res[2 * j + 1];
+        continue;
+      }
+      if (ran[i] == 0) out[2 * i] = res[2 * j];
+      else merge_into(out[2 * i], res[2 * j]);
+      ran[i] += want[i];
+      const zg_counters& t = out[2 * i];
+      double need;
+      if (t.hits >= 30 && t.estimate > 0) {
+        const double n = (double)t.samples;
+        double var = t.sum_w2 / n - t.estimate * t.estimate;
+        if (var < 0) var = 0;
+        if (z * sqrt(var / n) <= error * t.estimate) {
+          bound_met[i] = 1;
+          continue;
+        }
+        need = z * z * var / (error * error * t.estimate * t.estimate) * 1.1;
+      } else {
+        need = 2.0 * (double)ran[i];
+      }
+      if (ran[i] >= max_samples) continue;
+      const double cap = (double)max_samples;
+      const uint64_t target = (uint64_t)(need < cap ? need : cap);
+      want[i] = target > ran[i] ? target - ran[i] : 0;
+      if (want[i] < ran[i] / 4 + 1) want[i] = ran[i] / 4 + 1;
+      if (want[i] > max_samples - ran[i]) want[i] = max_samples - ran[i];
+      next.push_back(i);
+    }
+    pending.swap(next);
+  }
+  if (rounds_run) *rounds_run = rounds;
   return ZG_OK;
 }
 

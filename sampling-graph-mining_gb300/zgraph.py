@@ -167,6 +167,7 @@ def lib():
             "zg_batch_submit": ([P, P, U32, P], I32),
             "zg_batch_wait": ([P, P], I32),
             "zg_batch_size_learned": ([P, P, P, U32, D, D, U64, P], I32),
+            "zg_batch_bounded": ([P, P, P, U32, D, D, U32, U64, P, P, P, C.POINTER(U32)], I32),
             "zg_batch_filtered_graph": ([P, I32, I64, I64, P, C.POINTER(P)], I32),
             "zg_batch_tune": ([P, P, U32, P, C.POINTER(I32), P], I32),
             "zg_batch_elapsed_ms": ([P, C.POINTER(C.c_float)], I32),
@@ -441,47 +442,22 @@ class Batch:
             q["n"] = int(arr[i].n)
         return qs
 
-    def bounded(self, mlp, qs, eps, conf, max_rounds=4, max_samples=1 << 40, pilot_samples=1 << 16):
-        """The batch counterpart of zg_query_learned: learned sizing of every query without an "n"
-        (size_learned), one batch, then further batches for the queries whose empirical CLT
-        half-width is still above eps * estimate (at least 30 hits), each topped up to what its
-        observed variance needs (+10 %) on fresh sample indices, merged exactly.  3-motif queries
-        run their given budgets once.  Returns (counters per query, bound met per query, rounds)."""
-        z = lib().zg_normal_quantile(1.0 - (1.0 - conf) / 2.0)
-        sized = self.size_learned(mlp, qs, eps, conf, pilot_samples)
-        n_q = len(sized)
-        total = [None] * n_q
-        ran = [0] * n_q
-        met = [False] * n_q
-        want = [q["n"] for q in sized]
-        pending = list(range(n_q))
-        rounds = 0
-        while pending and rounds < max_rounds:
-            sub = [dict(sized[i], n=want[i], first_sample=sized[i].get("first_sample", 0) + ran[i]) for i in pending]
-            res = self.run(sub)
-            rounds += 1
-            nxt = []
-            for i, (c, c2) in zip(pending, res):
-                if sized[i]["kind"] == QUERY_THREE_MOTIF:
-                    total[i] = (c, c2)
-                    continue
-                total[i] = c if total[i] is None else merge_counters([total[i], c])
-                ran[i] += want[i]
-                t = total[i]
-                if t.hits >= 30 and t.estimate > 0:
-                    var = max(t.sum_w2 / t.samples - t.estimate ** 2, 0.0)
-                    if z * (var / t.samples) ** 0.5 <= eps * t.estimate:
-                        met[i] = True
-                        continue
-                    need = int(z * z * var / (eps * eps * t.estimate * t.estimate) * 1.1)
-                else:
-                    need = 2 * ran[i]
-                if ran[i] >= max_samples:
-                    continue
-                want[i] = max(min(need, max_samples) - ran[i], ran[i] // 4 + 1)
-                nxt.append(i)
-            pending = nxt
-        return total, met, rounds
+    def bounded(self, mlp, qs, eps, conf, max_rounds=4, max_samples=1 << 40, cuda_stream=None):
+        """zg_batch_bounded, the batch counterpart of zg_query_learned: learned sizing of every
+        query without an "n", one batch, then further batches for the answers whose empirical CLT
+        half-width is still above eps * estimate, topped up on fresh sample indices and merged
+        exactly.  Returns (counters per query (a pair for 3-motif queries), bound met per query,
+        rounds)."""
+        qs = list(qs)
+        arr, nq, keep = self.queries(qs)
+        out = (Counters * max(2, 2 * nq))()
+        met = (C.c_uint32 * max(1, nq))()
+        rounds = C.c_uint32(0)
+        check(lib().zg_batch_bounded(self._h, mlp._h, arr, nq, eps, conf, max_rounds, max_samples, cuda_stream,
+                                     out, met, C.byref(rounds)))
+        total = [(out[2 * i], out[2 * i + 1]) if qs[i]["kind"] == QUERY_THREE_MOTIF else out[2 * i]
+                 for i in range(nq)]
+        return total, [bool(met[i]) for i in range(nq)], int(rounds.value)
 
     def elapsed_ms(self):
         """Device time of the last waited batch (CUDA events around its graph launch)."""
