@@ -291,9 +291,9 @@ int zg_batch_submit(zg_batch* b, const zg_batch_query* queries, uint32_t nq, voi
  * out[2i] the 3-chain, out[2i+1] the triangle). */
 int zg_batch_wait(zg_batch* b, zg_counters* out);
 /* Learned sizing for a batch (no counterpart in the reference): every query with n == 0 gets the
- * learned profile's budget for (error, confidence), from one pilot batch (pilot_samples per query,
- * 0: 2^16, on the pilot stream zg_graph_features uses: first sample 0, stream ZG_ELP_STREAM + 1,
- * the query's seed), the degree statistics of its graph (base or filtered) and one prediction for
+ * learned profile's budget for (error, confidence), from pilot batches (pilot_samples per query, 0:
+ * adaptive as in zg_graph_features, on the pilot stream zg_graph_features uses: first sample 0,
+ * stream ZG_ELP_STREAM + 1, the query's seed), the degree statistics of its graph (base or filtered) and one prediction for
  * all of them; n as zg_elp_learned computes it.  Queries with n > 0 are left as they are; a 3-motif
  * query needs its n.  Runs the batch (so not while one of its batches is pending). */
 int zg_batch_size_learned(zg_batch* b, const zg_mlp* net, zg_batch_query* queries, uint32_t nq,
@@ -413,7 +413,9 @@ int zg_mlp_grad(const zg_mlp* net, const float* X, const float* Y, uint32_t n_ro
 int zg_mlp_predict(const zg_mlp* net, const float* X, uint32_t n_rows, float* Y);
 /* The 16 features of a query: degree statistics of g (one device pass on the first call for g,
  * then kept with the graph), the program's pattern class, and a pilot run of pilot_samples
- * estimators (0: 2^16).  Not to be called for the same graph from two threads at once. */
+ * estimators (0: adaptive, 2^16 and then 2^18, 2^20, 2^22 from the same first sample until the
+ * pilot has 8 hits; the shipped network is trained on adaptive pilots).  Not to be called for the
+ * same graph from two threads at once. */
 int zg_graph_features(const zg_graph* g, const zg_program* p, uint64_t pilot_samples,
                       uint64_t seed, void* cuda_stream, float* features);
 /* Learned sizing (the learned counterpart of ErrorProfile::get_num_estimators,
@@ -423,7 +425,7 @@ int zg_graph_features(const zg_graph* g, const zg_program* p, uint64_t pilot_sam
 int zg_elp_learned(const zg_mlp* net, const zg_graph* g, const zg_program* p, double error,
                    double confidence, uint64_t pilot_samples, uint64_t seed, void* cuda_stream,
                    uint64_t* n_required, float* prediction);
-/* zg_elp_learned (2^16-sample pilot from feature_seed), then zg_query from query_seed.  A budget
+/* zg_elp_learned (adaptive pilot from feature_seed), then zg_query from query_seed.  A budget
  * above 2^30 samples runs in two looks: half of it first, then what the bound check still needs, so an
  * over-predicted budget costs at most half of it in extra samples.  n_required may be NULL. */
 int zg_query_learned(const zg_mlp* net, const zg_graph* g, const zg_program* p, double error,

@@ -594,7 +594,8 @@ extern "C" int zg_batch_size_learned(zg_batch* b, const zg_mlp* net, zg_batch_qu
   if (!(error > 0) || !(confidence > 0 && confidence < 1))
     return zg_set_error(ZG_ERR_INVALID_ARG, "zg_batch_size_learned: error %g / confidence %g", error, confidence),
            ZG_ERR_INVALID_ARG;
-  if (pilot_samples == 0) pilot_samples = 1ull << 16;
+  const bool adaptive = pilot_samples == 0;  // as zg_graph_features: 2^16 .. 2^22 until 8 hits
+  if (adaptive) pilot_samples = 1ull << 16;
   cudaStream_t s = (cudaStream_t)cuda_stream;
   // the queries to size, as pilot queries: the pilot zg_graph_features would run for each
   std::vector<uint32_t> idx;
@@ -617,6 +618,23 @@ extern "C" int zg_batch_size_learned(zg_batch* b, const zg_mlp* net, zg_batch_qu
   int rc = zg_batch_submit(b, pilot.data(), k, cuda_stream);
   if (rc == ZG_OK) rc = zg_batch_wait(b, c.data());
   if (rc) return rc;
+  // adaptive pilots: the queries below 8 hits again with 4x the estimators, up to 2^22
+  for (uint64_t n = pilot_samples << 2; adaptive && n <= (1ull << 22); n <<= 2) {
+    std::vector<uint32_t> again;
+    std::vector<zg_batch_query> more;
+    for (uint32_t j = 0; j < k; ++j)
+      if (c[2 * j].hits < 8) {
+        again.push_back(j);
+        more.push_back(pilot[j]);
+        more.back().n = n;
+      }
+    if (again.empty()) break;
+    std::vector<zg_counters> c2(2 * again.size());
+    if ((rc = zg_batch_submit(b, more.data(), (uint32_t)more.size(), cuda_stream)) ||
+        (rc = zg_batch_wait(b, c2.data())))
+      return rc;
+    for (size_t a = 0; a < again.size(); ++a) c[2 * again[a]] = c2[2 * a];
+  }
   // features: the query graph's degree statistics, the program class, the pilot
   std::vector<float> X((size_t)k * ZG_MLP_FEATURES), Y((size_t)k * ZG_MLP_OUTPUTS);
   std::vector<const zg_graph*> none;

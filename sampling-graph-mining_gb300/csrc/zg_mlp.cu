@@ -525,6 +525,11 @@ float lg2(double x) { return (float)log2(x > 1e-300 ? x : 1e-300); }
 // pattern one-hot (triangle, 4-clique, 3-chain, 4-chain/k-chain, tree pattern, cyclic pattern),
 // and from a pilot run of pilot_samples estimators (stream ZG_ELP_STREAM + 1): log2 hit rate and
 // log2 per-sample relative variance.
+// Adaptive pilots (pilot_samples = 0): from kPilotMin estimators, 4x at a time up to kPilotMax,
+// until kPilotHits hits, so rare patterns get a pilot that has seen some.
+constexpr uint64_t kPilotMin = 1ull << 16, kPilotMax = 1ull << 22;
+constexpr uint64_t kPilotHits = 8;
+
 // The graph part of the features (f[0..7]; the rest zeroed).
 int zg_degree_features(const zg_graph* g, cudaStream_t s, float* f) {
   int rc = deg_stats(g, s);
@@ -568,8 +573,16 @@ extern "C" int zg_graph_features(const zg_graph* g, const zg_program* p, uint64_
   int rc = zg_degree_features(g, (cudaStream_t)cuda_stream, f);
   if (rc) return rc;
   zg_counters c;
-  if (pilot_samples == 0) pilot_samples = 1ull << 16;
-  rc = zg_run(g, p, pilot_samples, 0, seed, ZG_ELP_STREAM + 1, cuda_stream, &c);
+  if (pilot_samples) {
+    rc = zg_run(g, p, pilot_samples, 0, seed, ZG_ELP_STREAM + 1, cuda_stream, &c);
+  } else {
+    // adaptive: 2^16 estimators, then 2^18, 2^20, 2^22 (each from the pilot stream's first sample,
+    // so a larger pilot contains the smaller) until the pilot has seen kPilotHits hits
+    for (uint64_t n = kPilotMin;; n <<= 2) {
+      if ((rc = zg_run(g, p, n, 0, seed, ZG_ELP_STREAM + 1, cuda_stream, &c))) break;
+      if (c.hits >= kPilotHits || n >= kPilotMax) break;
+    }
+  }
   if (rc) return rc;
   zg_query_features(p, c, f);
   return ZG_OK;

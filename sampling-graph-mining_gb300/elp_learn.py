@@ -2,7 +2,7 @@
 network by the library's own CUDA kernels, and budget sizing.
 
 The network (zg_mlp_*) maps 16 query features (zg_graph_features: degree statistics of the
-graph, the pattern class, a 2^16-estimator pilot) to log2 of the per-sample relative variance
+graph, the pattern class, an adaptive pilot of 2^16..2^22 estimators) to log2 of the per-sample relative variance
 Var(1/p) / E(1/p)^2 and log2 of the per-sample latency.  For a target error eps at confidence
 conf the budget is n = z^2 * cv2 / eps^2; zg_query then checks the answer against its empirical
 bound and keeps sampling if needed, so a wrong prediction costs time, never accuracy.
@@ -95,7 +95,7 @@ def make_dataset(specs, patterns=PATTERNS, seed=11, log=None):
         g = build_graph(spec)
         for name, (kind, param, pat) in patterns.items():
             prog = Z.Program(kind, param, pat)
-            f = Z.features(g, prog, 1 << 16, seed + gi)
+            f = Z.features(g, prog, 0, seed + gi)  # adaptive pilot, as zg_elp_learned uses
             mres = measure(g, prog, seed + gi)
             if mres is None or not (mres["cv2"] > 0):
                 continue

@@ -432,7 +432,7 @@ class Batch:
         self.submit(qs, cuda_stream)
         return self.wait()
 
-    def size_learned(self, mlp, qs, eps, conf, pilot_samples=1 << 16, cuda_stream=None):
+    def size_learned(self, mlp, qs, eps, conf, pilot_samples=0, cuda_stream=None):
         """zg_batch_size_learned: the learned budget of every query without an "n" (one pilot
         batch, one prediction); returns the queries with "n" filled in."""
         qs = [dict(q) for q in qs]
@@ -659,7 +659,7 @@ def allgather_counters(c, group=None):
 MLP_FEATURES, MLP_OUTPUTS, MLP_PARAMS = 16, 2, 5378
 
 
-def features(graph, program, pilot_samples=1 << 16, seed=1, cuda_stream=None):
+def features(graph, program, pilot_samples=0, seed=1, cuda_stream=None):
     """zg_graph_features: 16 features of a (graph, program) query."""
     f = np.zeros(MLP_FEATURES, np.float32)
     check(lib().zg_graph_features(graph.handle, program.handle, pilot_samples, seed, cuda_stream, _ptr(f)))
@@ -728,7 +728,7 @@ class Mlp:
             pass
 
 
-def learned_budget(mlp, graph, program, eps, conf, seed=1, pilot_samples=1 << 16):
+def learned_budget(mlp, graph, program, eps, conf, seed=1, pilot_samples=0):
     """zg_elp_learned: predicted per-sample relative variance -> n = z^2 * cv2 / eps^2.
     Returns (n, features, prediction)."""
     f = features(graph, program, pilot_samples, seed)
@@ -740,7 +740,7 @@ def learned_budget(mlp, graph, program, eps, conf, seed=1, pilot_samples=1 << 16
 
 
 def learned_query(mlp, graph, program, eps, conf, seed, query_seed, stream_id=0, max_samples=0, cuda_stream=None):
-    """zg_query_learned: learned sizing (2^16-sample pilot from seed), then the bound check from query_seed;
+    """zg_query_learned: learned sizing (adaptive pilot from seed), then the bound check from query_seed;
     a budget above 2^30 samples runs in two looks (half first).  Returns (QueryResult, budget)."""
     n = C.c_uint64(0)
     out = QueryResult()

@@ -95,6 +95,20 @@ def test_features_match_host():
     assert abs(f[14] - math.log2((c.hits + 0.5) / (1 << 16))) < 1e-5
 
 
+def test_adaptive_pilot():
+    """pilot_samples = 0: the features of the first pilot in 2^16, 2^18, 2^20, 2^22 with 8 hits (the
+    last if none has), each pilot from the pilot stream's first sample."""
+    e = Z.gen_rmat(12, 3, seed=21)
+    g = Z.Graph.from_edges(e, 1 << 12)
+    for kind in (Z.PROG_TRIANGLE, Z.PROG_FOUR_CLIQUE, Z.PROG_FOUR_CLIQUE_UNBIASED):
+        p = Z.Program(kind)
+        f0 = Z.features(g, p, 0, 5)
+        for n in (1 << 16, 1 << 18, 1 << 20, 1 << 22):
+            if p.run(g, n, 5, stream_id=Z.ELP_STREAM + 1).hits >= 8 or n == 1 << 22:
+                break
+        assert np.array_equal(f0, Z.features(g, p, n, 5)), (kind, n)
+
+
 def test_learned_budget_and_query_entry_points():
     """zg_elp_learned is the sizing formula on the network's prediction for the query's features;
     zg_query_learned runs it and checks the answer's bound, half of a long budget first."""
