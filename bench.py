@@ -526,7 +526,7 @@ def run_batch(args):
 
 def learned_batch(Z, b, qs, eps=0.05, conf=0.95):
     """The same queries to eps at conf: learned sizing of the whole batch (zg_batch_size_learned:
-    one pilot batch, one prediction; 3-motif queries keep their budgets), one batch, then top-up
+    pilot batches, one prediction; 3-motif queries keep their budgets), one batch, then top-up
     batches for the answers whose empirical bound does not hold yet (zg_batch_bounded)."""
     model = os.path.join(ROOT, "sampling-graph-mining_gb300", "elp_mlp.npz")
     if not os.path.exists(model):

@@ -152,7 +152,7 @@ def test_pattern_queries_and_first_sample(wgraph):
 
 
 def test_learned_sizing_of_a_batch(wgraph):
-    """zg_batch_size_learned fills the n of every query without one, from one pilot batch and one
+    """zg_batch_size_learned fills the n of every query without one, from pilot batches and one
     prediction, equal (to the last bit of the pilot's variance term) to zg_elp_learned per query."""
     rng = np.random.default_rng(12)
     net = Z.Mlp(3)
