@@ -217,21 +217,18 @@ __host__ __device__ __forceinline__ void zg_u192_set(ZgU192& a, uint64_t v) {
   a.l[1] = 0;
   a.l[2] = 0;
 }
-// a *= f; returns true on overflow beyond 192 bits.
-__host__ __device__ __forceinline__ bool zg_u192_mul(ZgU192& a, uint64_t f) {
-  uint64_t lo0 = a.l[0] * f, hi0 = zg_mulhi64(a.l[0], f);
-  uint64_t lo1 = a.l[1] * f, hi1 = zg_mulhi64(a.l[1], f);
-  uint64_t lo2 = a.l[2] * f, hi2 = zg_mulhi64(a.l[2], f);
-  uint64_t r1 = lo1 + hi0;
-  uint64_t c1 = r1 < lo1;
-  uint64_t r2 = lo2 + hi1;
-  uint64_t c2 = r2 < lo2;
-  uint64_t r2b = r2 + c1;
-  c2 += r2b < r2;
-  a.l[0] = lo0;
-  a.l[1] = r1;
-  a.l[2] = r2b;
-  return (hi2 | c2) != 0;
+// a *= f for a 32-bit factor: per limb two 32 x 32 -> 64-bit multiply-adds, whose sums stay below
+// 2^64 ((2^32 - 1)^2 + 2^32 - 1); returns true on overflow beyond 192 bits.
+__host__ __device__ __forceinline__ bool zg_u192_mul32(ZgU192& a, uint32_t f) {
+  uint64_t c = 0;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const uint64_t lo = (uint64_t)(uint32_t)a.l[i] * f + c;
+    const uint64_t hi = (a.l[i] >> 32) * f + (lo >> 32);
+    a.l[i] = (hi << 32) | (uint32_t)lo;
+    c = hi >> 32;
+  }
+  return c != 0;
 }
 
 const char* zg_set_error(int code, const char* fmt, ...);

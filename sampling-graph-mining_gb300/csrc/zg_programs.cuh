@@ -65,8 +65,11 @@ __device__ __forceinline__ void res_init(Res& r) {
   zg_u192_set(r.num, 1);
   r.w = 0.0;
 }
+// Every factor of a weight is below 2^32: the edge count (at most 2^31 - 1, the build's limit),
+// a suffix sum S over distinct anchors (at most 2m) or a small constant.  A factor that broke this
+// would be reported as an overflow, never truncated silently.
 __device__ __forceinline__ void res_mul(Res& r, uint64_t f) {
-  if (zg_u192_mul(r.num, f)) r.ovf = true;
+  if (zg_u192_mul32(r.num, (uint32_t)f) || (f >> 32)) r.ovf = true;
 }
 
 // First index in adj_e[lo, hi) whose edge id >= key, where every edge id in the range is known
