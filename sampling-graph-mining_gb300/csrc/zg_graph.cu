@@ -150,9 +150,11 @@ __global__ void k_off32(const int64_t* __restrict__ off, uint64_t n, uint32_t* _
 
 // Bucketed two-choice cuckoo insertion of every edge's entry (fingerprint << 32 | edge id).  A
 // thread claims an empty slot of either bucket with atomicCAS; when both are full it swaps its
-// entry into a slot (atomicExch) and carries the evicted entry to that entry's other bucket (its
-// key is rebuilt from rec).  After kMaxKicks swaps it gives up and raises *fail: the host rebuilds
-// with new hash seeds.  Every loop here is bounded.
+// entry into slot 1..3 of one (atomicExch) and carries the evicted entry to that entry's other
+// bucket (its key is rebuilt from rec).  Whenever an entry goes to its second bucket, its first
+// bucket (full then, so slot 0 holds an entry) gets the overflow flag in slot 0, which is only
+// ever written by that first claim and by these flags.  After kMaxKicks swaps it gives up and
+// raises *fail: the host rebuilds with new hash seeds.  Every loop here is bounded.
 constexpr int kMaxKicks = 128;
 
 __device__ __forceinline__ bool cuckoo_try(unsigned long long* ent, uint32_t b, unsigned long long x) {
@@ -174,13 +176,19 @@ __global__ void k_cuckoo_insert(const ZgDevGraph d, uint64_t m, unsigned long lo
     uint32_t from = 0xFFFFFFFFu;  // the bucket the carried entry was evicted from
     bool placed = false;
     for (int kick = 0; kick < kMaxKicks; ++kick) {
-      uint32_t b1 = zg_bucket1(k, seed, bits), b2 = zg_bucket2(k, seed, bits);
-      if (cuckoo_try(ent, b1, x) || (b2 != b1 && cuckoo_try(ent, b2, x))) {
+      const uint32_t b1 = zg_bucket1(k, seed, bits), b2 = zg_bucket2(k, seed, bits);
+      if (cuckoo_try(ent, b1, x)) {
         placed = true;
         break;
       }
-      uint32_t vb = from == b1 ? b2 : from == b2 ? b1 : (((e + kick) & 1) ? b2 : b1);
-      unsigned long long old = atomicExch(&ent[4 * (uint64_t)vb + ((e + (uint64_t)kick) & 3)], x);
+      if (b2 != b1 && cuckoo_try(ent, b2, x)) {
+        atomicOr(&ent[4 * (uint64_t)b1], ZG_HASH_OVERFLOW);
+        placed = true;
+        break;
+      }
+      const uint32_t vb = from == b1 ? b2 : from == b2 ? b1 : (((e + kick) & 1) ? b2 : b1);
+      if (vb != b1) atomicOr(&ent[4 * (uint64_t)b1], ZG_HASH_OVERFLOW);
+      const unsigned long long old = atomicExch(&ent[4 * (uint64_t)vb + 1 + (e + (uint64_t)kick) % 3], x);
       if (old == ZG_HASH_EMPTY) {
         placed = true;
         break;
@@ -194,18 +202,23 @@ __global__ void k_cuckoo_insert(const ZgDevGraph d, uint64_t m, unsigned long lo
   }
 }
 
-// Every edge must be found in one of its two buckets (an insertion that gave up lost one).
+// Every edge must be found in one of its two buckets (an insertion that gave up lost one), and
+// one found only in its second bucket needs the overflow flag on its first.
 __global__ void k_cuckoo_check(const ZgDevGraph d, uint64_t m, const unsigned long long* __restrict__ ent,
                                uint32_t bits, uint64_t seed, unsigned int* __restrict__ fail) {
   for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < m; e += (uint64_t)gridDim.x * blockDim.x) {
     uint4 r = zg_rec_e(d, e);
     unsigned long long k = zg_edge_key(r.x, r.y);
     unsigned long long x = ((unsigned long long)zg_fingerprint(k, seed) << 32) | e;
-    uint32_t bs[2] = {zg_bucket1(k, seed, bits), zg_bucket2(k, seed, bits)};
-    bool found = false;
-    for (int i = 0; i < 2; ++i)
-      for (int j = 0; j < 4; ++j) found |= ent[4 * (uint64_t)bs[i] + j] == x;
-    if (!found) atomicOr(fail, 1u);
+    const uint32_t b1 = zg_bucket1(k, seed, bits), b2 = zg_bucket2(k, seed, bits);
+    bool in1 = false, in2 = false;
+    for (int j = 0; j < 4; ++j) {
+      in1 |= (ent[4 * (uint64_t)b1 + j] & ~ZG_HASH_OVERFLOW) == x;
+      in2 |= (ent[4 * (uint64_t)b2 + j] & ~ZG_HASH_OVERFLOW) == x;
+    }
+    const unsigned long long s0 = ent[4 * (uint64_t)b1];
+    const bool flagged = s0 != ZG_HASH_EMPTY && (s0 & ZG_HASH_OVERFLOW);
+    if (!(in1 || (in2 && flagged))) atomicOr(fail, 1u);
   }
 }
 

@@ -22,9 +22,11 @@
 //   off32[V+1] the offsets as uint32 (2m < 2^32), read by the compact layout's steps.
 //   hent[4B]  the edge set as a two-choice bucketed cuckoo table, B = 2^hbits buckets of 4
 //             entries (one 32-byte sector); entry = (fingerprint << 32) | edge id for the key
-//             (min(u,v) << 32) | max(u,v).  A closure check ("edge (x,y) exists with id >=
-//             min_valid") reads its two buckets together; a fingerprint match is confirmed
-//             against the record of that edge id, so the answer is exact.
+//             (min(u,v) << 32) | max(u,v) (31-bit fingerprint; bit 63 of slot 0 flags a bucket
+//             some of whose keys live in their second bucket).  A closure check ("edge (x,y)
+//             exists with id >= min_valid") reads the first bucket, and the second only behind an
+//             overflow flag; a fingerprint match is confirmed against the record of that edge id,
+//             so the answer is exact.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -56,6 +58,9 @@ struct ZgDevGraph {
 };
 
 #define ZG_HASH_EMPTY 0xFFFFFFFFFFFFFFFFull
+// Set in slot 0 of a bucket (never empty then) when an entry whose first bucket it is lives in its
+// second bucket: only then can a key absent from its first bucket be in its second.
+#define ZG_HASH_OVERFLOW 0x8000000000000000ull
 
 #ifdef __CUDACC__
 // (src, dst, suf_src, suf_dst) of edge e, in either layout.
@@ -79,11 +84,13 @@ __host__ __device__ __forceinline__ uint32_t zg_bucket1(uint64_t key, uint64_t s
 __host__ __device__ __forceinline__ uint32_t zg_bucket2(uint64_t key, uint64_t seed, uint32_t bits) {
   return (uint32_t)(zg_mix64(key ^ (seed * 0x9E3779B97F4A7C15ull + 0x632BE59BD9B4E019ull)) >> (64 - bits));
 }
-// Never 0xFFFFFFFF, the fingerprint field of an empty entry.
+// 31 bits, never 0x7FFFFFFF (the fingerprint field of an empty entry); bit 31 of an entry's tag is
+// its bucket's overflow flag, kept in slot 0 (ZG_HASH_OVERFLOW).
 __host__ __device__ __forceinline__ uint32_t zg_fingerprint(uint64_t key, uint64_t seed) {
-  uint32_t f = (uint32_t)(zg_mix64(key + seed + 0xD6E8FEB86659FD93ull) >> 32);
-  return f == 0xFFFFFFFFu ? 0x7FFFFFFFu : f;
+  uint32_t f = (uint32_t)(zg_mix64(key + seed + 0xD6E8FEB86659FD93ull) >> 33);
+  return f == 0x7FFFFFFFu ? 0x3FFFFFFFu : f;
 }
+__host__ __device__ __forceinline__ uint32_t zg_entry_fp(unsigned long long x) { return (uint32_t)(x >> 32) & 0x7FFFFFFFu; }
 
 struct zg_graph {
   ZgDevGraph d;

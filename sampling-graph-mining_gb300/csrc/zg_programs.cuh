@@ -245,30 +245,33 @@ struct EdgeProbe {
   unsigned long long key, cand;
 };
 
-// The key's first bucket is read first.  An entry sits in its second bucket only if its first
-// bucket was full when it got there (insertion tries the first bucket first, and a slot once
-// filled is never emptied), so a first bucket with an empty slot and no matching fingerprint
-// proves the edge absent after one sector; the second bucket is read only behind a full first one.
+// The key's first bucket is read first, and its second only if the first carries the overflow
+// flag (slot 0, bit 63): the build sets it on a bucket whenever one of the keys whose first bucket
+// it is goes to its second bucket, so an unflagged first bucket without a matching fingerprint
+// proves the edge absent after one sector.
+__device__ __forceinline__ unsigned long long bucket_match(const ulonglong2& a0, const ulonglong2& a1, uint32_t fp) {
+  unsigned long long e = ZG_HASH_EMPTY;  // an empty entry never matches: no fingerprint is 0x7FFFFFFF
+  e = zg_entry_fp(a1.y) == fp ? a1.y : e;
+  e = zg_entry_fp(a1.x) == fp ? a1.x : e;
+  e = zg_entry_fp(a0.y) == fp ? a0.y : e;
+  e = zg_entry_fp(a0.x) == fp ? a0.x : e;
+  return e;
+}
+__device__ __forceinline__ bool bucket_overflow(const ulonglong2& a0) {
+  return a0.x != ZG_HASH_EMPTY && (a0.x & ZG_HASH_OVERFLOW);
+}
+
 __device__ __forceinline__ EdgeProbe edge_candidate(const ZgDevGraph& g, uint32_t x, uint32_t y) {
   EdgeProbe pr;
   pr.key = zg_edge_key(x, y);
   const uint32_t fp = zg_fingerprint(pr.key, g.hseed);
   ulonglong2 a0, a1;
   ld_bucket(g.hent + 4ull * zg_bucket1(pr.key, g.hseed, g.hbits), a0, a1);
-  // an empty entry never matches: no fingerprint is 0xFFFFFFFF
-  unsigned long long e = ZG_HASH_EMPTY;
-  e = (uint32_t)(a1.y >> 32) == fp ? a1.y : e;
-  e = (uint32_t)(a1.x >> 32) == fp ? a1.x : e;
-  e = (uint32_t)(a0.y >> 32) == fp ? a0.y : e;
-  e = (uint32_t)(a0.x >> 32) == fp ? a0.x : e;
-  const bool full = a0.x != ZG_HASH_EMPTY && a0.y != ZG_HASH_EMPTY && a1.x != ZG_HASH_EMPTY && a1.y != ZG_HASH_EMPTY;
-  if (e == ZG_HASH_EMPTY && full) {
+  unsigned long long e = bucket_match(a0, a1, fp);
+  if (e == ZG_HASH_EMPTY && bucket_overflow(a0)) {
     ulonglong2 c0, c1;
     ld_bucket(g.hent + 4ull * zg_bucket2(pr.key, g.hseed, g.hbits), c0, c1);
-    e = (uint32_t)(c1.y >> 32) == fp ? c1.y : e;
-    e = (uint32_t)(c1.x >> 32) == fp ? c1.x : e;
-    e = (uint32_t)(c0.y >> 32) == fp ? c0.y : e;
-    e = (uint32_t)(c0.x >> 32) == fp ? c0.x : e;
+    e = bucket_match(c0, c1, fp);
   }
   pr.cand = e;
   return pr;
@@ -283,16 +286,8 @@ __device__ __forceinline__ EdgeProbe edge_candidate_both(const ZgDevGraph& g, ui
   ulonglong2 a0, a1, c0, c1;
   ld_bucket(g.hent + 4ull * zg_bucket1(pr.key, g.hseed, g.hbits), a0, a1);
   ld_bucket(g.hent + 4ull * zg_bucket2(pr.key, g.hseed, g.hbits), c0, c1);
-  unsigned long long e = ZG_HASH_EMPTY;
-  e = (uint32_t)(c1.y >> 32) == fp ? c1.y : e;
-  e = (uint32_t)(c1.x >> 32) == fp ? c1.x : e;
-  e = (uint32_t)(c0.y >> 32) == fp ? c0.y : e;
-  e = (uint32_t)(c0.x >> 32) == fp ? c0.x : e;
-  e = (uint32_t)(a1.y >> 32) == fp ? a1.y : e;
-  e = (uint32_t)(a1.x >> 32) == fp ? a1.x : e;
-  e = (uint32_t)(a0.y >> 32) == fp ? a0.y : e;
-  e = (uint32_t)(a0.x >> 32) == fp ? a0.x : e;
-  pr.cand = e;
+  const unsigned long long e = bucket_match(a0, a1, fp);
+  pr.cand = e != ZG_HASH_EMPTY ? e : bucket_match(c0, c1, fp);
   return pr;
 }
 
@@ -302,7 +297,7 @@ __device__ __noinline__ int64_t edge_rescan(const ZgDevGraph& g, unsigned long l
   uint32_t fp = zg_fingerprint(key, g.hseed);
   for (int i = 0; i < 8; ++i) {
     unsigned long long x = ZG_LDG(&g.hent[(i < 4 ? b1 : b2) + (i & 3)]);
-    if (x == cand || (uint32_t)(x >> 32) != fp) continue;
+    if (x == cand || zg_entry_fp(x) != fp) continue;
     uint4 q = zg_rec_e(g, (uint32_t)x);
     if (zg_edge_key(q.x, q.y) == key) return (int64_t)(uint32_t)x;
   }
