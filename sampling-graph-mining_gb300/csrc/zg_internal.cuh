@@ -170,6 +170,51 @@ __host__ __device__ __forceinline__ void zg_philox4(uint32_t c0, uint32_t c1, ui
   o2 = c2;
   o3 = c3;
 }
+// Philox4x32-10 round keys of one seed (round r: seed + r * the Weyl constants), computed once per
+// launch and passed as a grid-constant kernel parameter, so each round's key is an operand of the
+// xor instead of two adds per round.
+struct ZgKeys {
+  uint32_t k[10][2];
+};
+__host__ __device__ __forceinline__ ZgKeys zg_round_keys(uint64_t seed) {
+  ZgKeys K;
+  uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+  for (int r = 0; r < 10; ++r) {
+    if (r) {
+      k0 += 0x9E3779B9u;
+      k1 += 0xBB67AE85u;
+    }
+    K.k[r][0] = k0;
+    K.k[r][1] = k1;
+  }
+  return K;
+}
+// zg_philox4 with precomputed round keys (the same outputs).
+__host__ __device__ __forceinline__ void zg_philox4_k(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
+                                                      const ZgKeys& K, uint32_t& o0, uint32_t& o1, uint32_t& o2,
+                                                      uint32_t& o3) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+#ifdef __CUDA_ARCH__
+    uint32_t hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
+    uint32_t hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
+#else
+    uint64_t p0 = (uint64_t)0xD2511F53u * c0, p1 = (uint64_t)0xCD9E8D57u * c2;
+    uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+    uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+#endif
+    uint32_t n0 = hi1 ^ c1 ^ K.k[r][0], n2 = hi0 ^ c3 ^ K.k[r][1];
+    c0 = n0;
+    c1 = lo1;
+    c2 = n2;
+    c3 = lo0;
+  }
+  o0 = c0;
+  o1 = c1;
+  o2 = c2;
+  o3 = c3;
+}
+
 // The first two output words.
 __host__ __device__ __forceinline__ void zg_philox(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
                                                    uint32_t k0, uint32_t k1, uint32_t& o0, uint32_t& o1) {
@@ -201,6 +246,13 @@ __host__ __device__ __forceinline__ uint64_t zg_sample_word(uint64_t seed, uint3
   uint32_t o0, o1, o2, o3;
   zg_philox4((uint32_t)sample, (uint32_t)(sample >> 32), d >> 1, stream, (uint32_t)seed, (uint32_t)(seed >> 32),
              o0, o1, o2, o3);
+  return (d & 1) ? (((uint64_t)o3 << 32) | o2) : (((uint64_t)o1 << 32) | o0);
+}
+// zg_sample_word with the seed's precomputed round keys.
+__host__ __device__ __forceinline__ uint64_t zg_sample_word_k(const ZgKeys& K, uint32_t stream, uint64_t sample,
+                                                              uint32_t d) {
+  uint32_t o0, o1, o2, o3;
+  zg_philox4_k((uint32_t)sample, (uint32_t)(sample >> 32), d >> 1, stream, K, o0, o1, o2, o3);
   return (d & 1) ? (((uint64_t)o3 << 32) | o2) : (((uint64_t)o1 << 32) | o0);
 }
 // A draw's word mapped to [lo, hi] by multiply-high.

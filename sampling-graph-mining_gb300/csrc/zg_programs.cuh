@@ -32,10 +32,13 @@ struct Ctx {
   zg_sample_trace* tr;  // debug only
   uint32_t sectors;     // debug only: access model, 32-byte sectors
   uint32_t closures;    // debug only: access model, closure checks
+  const ZgKeys* rk;     // the seed's round keys (a grid-constant parameter), or null
   __device__ __forceinline__ uint64_t draw(uint64_t lo, uint64_t hi) { return take(word(nd), lo, hi); }
   // The Philox word of draw k, computable before the range it maps to is known (so the integer
   // work overlaps the loads that determine the range); take() maps the next draw's word.
-  __device__ __forceinline__ uint64_t word(uint32_t k) const { return zg_sample_word(seed, stream, sample, k); }
+  __device__ __forceinline__ uint64_t word(uint32_t k) const {
+    return rk ? zg_sample_word_k(*rk, stream, sample, k) : zg_sample_word(seed, stream, sample, k);
+  }
   __device__ __forceinline__ uint64_t take(uint64_t w, uint64_t lo, uint64_t hi) {
     uint64_t v = zg_draw_map(w, lo, hi);
     if (tr && nd < ZG_MAX_DRAWS) {

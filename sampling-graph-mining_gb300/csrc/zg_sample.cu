@@ -38,7 +38,8 @@ __device__ __forceinline__ void run_program(const ZgDevGraph& g, const ZgProgPar
 // in another order.
 template <bool WIDE>
 __device__ __forceinline__ void four_chain_grouped(const ZgDevGraph& g, uint64_t n, uint64_t first, uint64_t seed,
-                                                   uint32_t stream, uint32_t den, Acc& a, AccSlots<kBlock>& sl) {
+                                                   const ZgKeys& keys, uint32_t stream, uint32_t den, Acc& a,
+                                                   AccSlots<kBlock>& sl) {
   __shared__ uint32_t queue[kBlock / 32][3][64];
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint32_t below = (1u << lane) - 1;
@@ -50,7 +51,7 @@ __device__ __forceinline__ void four_chain_grouped(const ZgDevGraph& g, uint64_t
     const uint64_t i = base + (uint64_t)k * stride + lane;
     const bool valid = i < n;
     if (!__ballot_sync(0xffffffffu, valid)) break;
-    const uint32_t sel = valid ? (uint32_t)zg_draw_map(zg_sample_word(seed, stream, first + i, 0), 1, 3) : 0u;
+    const uint32_t sel = valid ? (uint32_t)zg_draw_map(zg_sample_word_k(keys, stream, first + i, 0), 1, 3) : 0u;
     const unsigned m1 = __ballot_sync(0xffffffffu, sel == 1), m2 = __ballot_sync(0xffffffffu, sel == 2),
                    m3 = __ballot_sync(0xffffffffu, sel == 3);
     // every count is <= 31 before this round, so a queue of 64 never overflows
@@ -72,7 +73,7 @@ __device__ __forceinline__ void four_chain_grouped(const ZgDevGraph& g, uint64_t
       c3 -= p == 3 ? 32u : 0u;
       __syncwarp();  // read before the next round refills the queue
       const uint64_t si = base + (uint64_t)(slot >> 5) * stride + (slot & 31);
-      Ctx c{seed, first + si, stream, 0, nullptr, 0};
+      Ctx c{seed, first + si, stream, 0, nullptr, 0, 0, &keys};
       Res r;
       res_init(r);
       prog_four_chain<false>(g, c, r, p);
@@ -87,7 +88,7 @@ __device__ __forceinline__ void four_chain_grouped(const ZgDevGraph& g, uint64_t
     if (lane < cp) {
       const uint32_t slot = q[p - 1][lane];
       const uint64_t si = base + (uint64_t)(slot >> 5) * stride + (slot & 31);
-      Ctx c{seed, first + si, stream, 0, nullptr, 0};
+      Ctx c{seed, first + si, stream, 0, nullptr, 0, 0, &keys};
       Res r;
       res_init(r);
       prog_four_chain<false>(g, c, r, p);
@@ -100,8 +101,9 @@ __device__ __forceinline__ void four_chain_grouped(const ZgDevGraph& g, uint64_t
 // of 256 threads requested from the compiler; zg_tune picks the fastest per program) and per record
 // layout (the layout tests of the record accessors fold away; each layout gets its own registers).
 template <int KIND, int MINB, bool WIDE>
-__global__ void __launch_bounds__(kBlock, MINB) k_sample(ZgDevGraph g, ZgProgParams pp, uint64_t n, uint64_t first,
-                                                   uint64_t seed, uint32_t stream, ZgPartial* __restrict__ partials) {
+__global__ void __launch_bounds__(kBlock, MINB)
+    k_sample(ZgDevGraph g, ZgProgParams pp, uint64_t n, uint64_t first, uint64_t seed, const __grid_constant__ ZgKeys keys,
+             uint32_t stream, ZgPartial* __restrict__ partials) {
   g.wide = WIDE;
   // Sums in shared-memory slots for the programs with long dependent chains (measured: 4-clique
   // and 4-chain faster); the triangle and 3-chain were faster with them in registers.
@@ -111,14 +113,14 @@ __global__ void __launch_bounds__(kBlock, MINB) k_sample(ZgDevGraph g, ZgProgPar
   acc_init(a);
   if (kSlots) acc_slots_init(sl);
   if (KIND == ZG_PROG_FOUR_CHAIN) {
-    four_chain_grouped<WIDE>(g, n, first, seed, stream, pp.den_log2, a, sl);
+    four_chain_grouped<WIDE>(g, n, first, seed, keys, stream, pp.den_log2, a, sl);
     acc_from_slots(a, sl);
     block_reduce_store<kBlock>(a, &partials[blockIdx.x]);
     return;
   }
   uint64_t stride = (uint64_t)gridDim.x * kBlock;
   for (uint64_t i = blockIdx.x * (uint64_t)kBlock + threadIdx.x; i < n; i += stride) {
-    Ctx c{seed, first + i, stream, 0, nullptr, 0};
+    Ctx c{seed, first + i, stream, 0, nullptr, 0, 0, &keys};
     Res r;
     res_init(r);
     if (KIND == ZG_PROG_TRIANGLE) prog_triangle<false>(g, c, r);
@@ -445,7 +447,8 @@ int grid_of(K kernel) {
 // Launch-shape variants: __launch_bounds__ min-blocks (register caps 255/128/80/64/48/40/32).
 constexpr int kVariants = 7;
 constexpr int kMinBlocks[kVariants] = {1, 2, 3, 4, 5, 6, 8};
-typedef void (*SampleKernel)(ZgDevGraph, ZgProgParams, uint64_t, uint64_t, uint64_t, uint32_t, ZgPartial*);
+typedef void (*SampleKernel)(ZgDevGraph, ZgProgParams, uint64_t, uint64_t, uint64_t, const ZgKeys, uint32_t,
+                             ZgPartial*);
 
 template <int KIND, bool WIDE>
 SampleKernel kernel_variant(int v) {
@@ -523,7 +526,7 @@ int launch_variant(const zg_graph* g, const zg_program* p, int v, uint64_t n, ui
                    uint32_t stream_id, cudaStream_t s, ZgPartial* parts, int grid) {
   ZgProgParams pp = params_for(p);
   SampleKernel k = kernel_for(p->kind, v, g->wide != 0);
-  k<<<grid, kBlock, 0, s>>>(g->d, pp, n, first, seed, stream_id, parts);
+  k<<<grid, kBlock, 0, s>>>(g->d, pp, n, first, seed, zg_round_keys(seed), stream_id, parts);
   return ZG_OK;
 }
 
