@@ -173,11 +173,11 @@ __device__ __forceinline__ uint32_t lb_eid_win(const uint2* __restrict__ adj, ui
 // Does edge (x,y) exist with edge id >= min_valid?  conditional_close's question
 // (src/ZGraphInstance.cpp:372-407): the pattern edges still to close join two sampled vertices,
 // so "found in some sampled vertex's list with id >= min_valid" is "edge (x,y) exists with such
-// an id".  Answered by the cuckoo table: both candidate buckets (one 32-byte sector each) are
-// read together; a fingerprint match is confirmed against rec, so the answer is exact.
-// Two phases, so a caller with several look-ups can stop before any dependent load:
-// edge_candidate() reads the two buckets and returns the first entry whose fingerprint matches
-// (or the empty marker: then the edge does not exist); edge_confirm() checks the candidate
+// an id".  Answered by the cuckoo table (one 32-byte sector per bucket): a fingerprint match is
+// confirmed against rec, so the answer is exact.  Two phases, so a caller with several look-ups
+// can stop before any dependent load: edge_candidate() reads the key's first bucket, and its
+// second behind an overflow flag (edge_candidate_both: both at once), and returns the first entry
+// whose fingerprint matches (or the empty marker: then the edge does not exist); edge_confirm() checks the candidate
 // against rec and, in the rare case of a second fingerprint match, rescans.  The result is the
 // edge id, or -1 when the edge does not exist.
 // One bucket = one 32-byte sector, read with a single 256-bit load (sm_100 family).
@@ -294,7 +294,7 @@ __device__ __forceinline__ EdgeProbe edge_candidate_both(const ZgDevGraph& g, ui
   return pr;
 }
 
-// another entry of the two buckets with the same fingerprint (probability ~ 8 / 2^32 a look-up)
+// another entry of the two buckets with the same fingerprint (probability ~ 8 / 2^31 a look-up)
 __device__ __noinline__ int64_t edge_rescan(const ZgDevGraph& g, unsigned long long key, unsigned long long cand) {
   uint64_t b1 = 4ull * zg_bucket1(key, g.hseed, g.hbits), b2 = 4ull * zg_bucket2(key, g.hseed, g.hbits);
   uint32_t fp = zg_fingerprint(key, g.hseed);
