@@ -177,9 +177,9 @@ __device__ __forceinline__ uint32_t lb_eid_win(const uint2* __restrict__ adj, ui
 // confirmed against rec, so the answer is exact.  Two phases, so a caller with several look-ups
 // can stop before any dependent load: edge_candidate() reads the key's first bucket, and its
 // second behind an overflow flag (edge_candidate_both: both at once), and returns the first entry
-// whose fingerprint matches (or the empty marker: then the edge does not exist); edge_confirm() checks the candidate
-// against rec and, in the rare case of a second fingerprint match, rescans.  The result is the
-// edge id, or -1 when the edge does not exist.
+// whose fingerprint matches (or the empty marker: then the edge does not exist); edge_confirm()
+// checks the candidate against rec and, in the rare case of a second fingerprint match, rescans.
+// The result is the edge id, or -1 when the edge does not exist.
 // One bucket = one 32-byte sector, read with a single 256-bit load (sm_100 family).
 __device__ __forceinline__ void ld_bucket(const unsigned long long* p, ulonglong2& lo, ulonglong2& hi) {
   asm("ld.global.nc.v4.u64 {%0, %1, %2, %3}, [%4];" : "=l"(lo.x), "=l"(lo.y), "=l"(hi.x), "=l"(hi.y) : "l"(p));
