@@ -88,8 +88,8 @@ typedef struct zg_graph_meta {
   uint64_t num_edges;
   uint64_t max_degree;
   uint64_t device_bytes;
-  uint32_t record_bytes;   /* bytes per edge record: 16 (compact) or 32 (wide layout)     */
-  uint32_t reserved;
+  uint32_t record_bytes;   /* bytes per edge record: 16 (compact, packed) or 32 (wide)    */
+  uint32_t record_layout;  /* ZG_RECORDS_COMPACT, ZG_RECORDS_WIDE or ZG_RECORDS_PACKED       */
 } zg_graph_meta;
 
 /* Result of one calculate()-style run.  The exact estimate is
@@ -154,14 +154,18 @@ int zg_graph_permuted(const uint32_t* edges, uint64_t m, uint32_t num_vertices,
 int zg_graph_free(zg_graph* g);
 /* Layout of the per-edge records of graphs built after this call (every graph constructor,
  * filters and subsamples included); process-wide, not to be changed while another thread builds.
- * AUTO (the default): compact while the graph's sampling working set is within twice the GPU's
- * L2, wide beyond.  COMPACT: (src, dst, suffix sizes), 16 bytes; the steps also read vertex
- * offsets.  WIDE: adds each edge's slot and predecessor count in both endpoint lists, 32 bytes
- * (one sector); a step then needs no offset read.  Every estimate is identical under either
- * layout.  No counterpart in the reference (its layout is fixed: src/Graph.cpp:215-377). */
+ * AUTO (the default): packed (else compact) while the graph's sampling working set is within
+ * twice the GPU's L2, wide beyond.  COMPACT: (src, dst, suffix sizes), 16 bytes; the steps also
+ * read vertex offsets.  WIDE: adds each edge's slot and predecessor count in both endpoint lists,
+ * 32 bytes (one sector); a step then needs no offset read.  PACKED: src, dst, both suffix sizes
+ * and both slots as bit fields of 16 bytes, where they fit (2 x vertex bits + suffix bits <= 64
+ * and suffix bits + 2 x slot bits <= 64; else compact); a step needs no offset read.  Every
+ * estimate is identical under each layout.  No counterpart in the reference (its layout is fixed:
+ * src/Graph.cpp:215-377). */
 #define ZG_RECORDS_AUTO 0
 #define ZG_RECORDS_COMPACT 1
 #define ZG_RECORDS_WIDE 2
+#define ZG_RECORDS_PACKED 3
 int zg_set_record_layout(int layout);
 int zg_graph_get_meta(const zg_graph* g, zg_graph_meta* out);
 int zg_graph_set_meta(zg_graph* g, uint64_t num_edges, uint64_t max_degree);

@@ -148,6 +148,22 @@ __global__ void k_off32(const int64_t* __restrict__ off, uint64_t n, uint32_t* _
     off32[i] = (uint32_t)off[i];
 }
 
+// Wide records (as built) into 16-byte ones: packed bit fields (the slots included) or compact
+// (src, dst, suf_src, suf_dst).
+__global__ void k_narrow(const ZgRec* __restrict__ wide, uint64_t m, uint4* __restrict__ out, uint32_t packed,
+                         uint32_t vb, uint32_t sb, uint32_t pb) {
+  for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < m; e += (uint64_t)gridDim.x * blockDim.x) {
+    const ZgRec r = wide[e];
+    if (packed) {
+      const uint64_t w0 = (uint64_t)r.e.x | ((uint64_t)r.e.y << vb) | ((uint64_t)r.e.z << (2 * vb));
+      const uint64_t w1 = (uint64_t)r.e.w | ((uint64_t)r.p.x << sb) | ((uint64_t)r.p.y << (sb + pb));
+      out[e] = make_uint4((uint32_t)w0, (uint32_t)(w0 >> 32), (uint32_t)w1, (uint32_t)(w1 >> 32));
+    } else {
+      out[e] = r.e;
+    }
+  }
+}
+
 // Bucketed two-choice cuckoo insertion of every edge's entry (fingerprint << 32 | edge id).  A
 // thread claims an empty slot of either bucket with atomicCAS; when both are full it swaps its
 // entry into slot 1..3 of one (atomicExch) and carries the evicted entry to that entry's other
@@ -279,7 +295,7 @@ int g_record_layout = ZG_RECORDS_AUTO;
 // Near the L2 size the compact layout keeps more of the graph resident.
 bool wide_records(uint64_t m, uint32_t nv) {
   if (g_record_layout == ZG_RECORDS_WIDE) return true;
-  if (g_record_layout == ZG_RECORDS_COMPACT) return false;
+  if (g_record_layout == ZG_RECORDS_COMPACT || g_record_layout == ZG_RECORDS_PACKED) return false;
   int dev = 0, l2 = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev) != cudaSuccess) {
     cudaGetLastError();
@@ -307,7 +323,10 @@ int build_graph(const uint2* d_coo, const uint32_t* d_w_in, uint64_t m, uint32_t
     return code;
   };
   uint64_t n2 = 2 * m;
-  g->wide = wide_records(m, nv);
+  // packed records are made from wide ones once the degrees are known (else compact ones)
+  const bool try_packed =
+      !wide_records(m, nv) && m && (g_record_layout == ZG_RECORDS_AUTO || g_record_layout == ZG_RECORDS_PACKED);
+  g->wide = try_packed || wide_records(m, nv);
   const size_t rec_bytes = (g->wide ? sizeof(ZgRec) : sizeof(uint4)) * m;
   // adj_e, 8 entries of slack (lb_eid_win's windows may read up to 7 entries past the last one),
   // and off32 share one allocation
@@ -412,10 +431,31 @@ int build_graph(const uint2* d_coo, const uint32_t* d_w_in, uint64_t m, uint32_t
     }
     g->max_degree = hmax;
   }
+  if (try_packed) {
+    const uint32_t vb = (uint32_t)bits_for(nv - 1), sb = (uint32_t)bits_for(g->max_degree);
+    const uint32_t pb = (uint32_t)bits_for(n2 - 1);
+    const bool fits = 2 * vb + sb <= 64 && sb + 2 * pb <= 64;
+    uint4* r16 = nullptr;
+    if ((rc = dev_alloc(&r16, m))) return fail(rc);
+    k_narrow<<<grid_for(m, B), B, 0, s>>>((const ZgRec*)g->rec, m, r16, fits, vb, sb, pb);
+    if ((ce = cudaStreamSynchronize(s)) != cudaSuccess) {
+      cudaFree(r16);
+      return fail(zg_check_cuda(ce, "record narrowing"));
+    }
+    cudaFree(g->rec);
+    g->rec = r16;
+    g->wide = 0;
+    g->packed = fits;
+    g->bytes -= (sizeof(ZgRec) - sizeof(uint4)) * m;
+    g->d.pk_v = vb;
+    g->d.pk_s = sb;
+    g->d.pk_p = pb;
+  }
   k_off32<<<grid_for((uint64_t)nv + 1, B), B, 0, s>>>(g->off, (uint64_t)nv + 1, g->off32);
   g->d.m = m;
   g->d.rec = g->rec;
   g->d.wide = g->wide;
+  g->d.packed = g->packed;
   g->d.off32 = g->off32;
   if ((rc = build_hash(g, s))) return fail(rc);
   ce = cudaGetLastError();
@@ -675,7 +715,7 @@ extern "C" int zg_graph_permuted(const uint32_t* edges, uint64_t m, uint32_t num
 }
 
 extern "C" int zg_set_record_layout(int layout) {
-  if (layout < ZG_RECORDS_AUTO || layout > ZG_RECORDS_WIDE)
+  if (layout < ZG_RECORDS_AUTO || layout > ZG_RECORDS_PACKED)
     return zg_set_error(ZG_ERR_INVALID_ARG, "unknown record layout %d", layout), ZG_ERR_INVALID_ARG;
   g_record_layout = layout;
   return ZG_OK;
@@ -702,7 +742,7 @@ extern "C" int zg_graph_get_meta(const zg_graph* g, zg_graph_meta* out) {
   out->max_degree = g->max_degree;
   out->device_bytes = g->bytes;
   out->record_bytes = g->wide ? (uint32_t)sizeof(ZgRec) : (uint32_t)sizeof(uint4);
-  out->reserved = 0;
+  out->record_layout = g->wide ? ZG_RECORDS_WIDE : g->packed ? ZG_RECORDS_PACKED : ZG_RECORDS_COMPACT;
   return ZG_OK;
 }
 
@@ -724,7 +764,13 @@ extern "C" int zg_graph_download(const zg_graph* g, uint32_t* edges, uint32_t* w
     ce = cudaMemcpy(rec.data(), g->rec, 4 * words * m, cudaMemcpyDeviceToHost);
     if (ce != cudaSuccess) return zg_check_cuda(ce, "download rec");
     for (uint64_t e = 0; e < m; ++e) {
-      const uint32_t* r = &rec[words * e];
+      uint32_t r[4], pos[2];
+      const uint32_t* x = &rec[words * e];
+      if (g->packed)
+        zg_unpack(g->d.pk_v, g->d.pk_s, g->d.pk_p, x[0] | ((uint64_t)x[1] << 32), x[2] | ((uint64_t)x[3] << 32), r[0],
+                  r[1], r[2], r[3], pos[0], pos[1]);
+      else
+        memcpy(r, x, sizeof(r));
       if (edges) {
         edges[2 * e] = r[0];
         edges[2 * e + 1] = r[1];

@@ -2,17 +2,22 @@
 //
 // Device graph layout (all arrays in HBM, built by zg_graph.cu):
 //   rec[m]    one record per edge in edge-id order (edge id = position, src/Graph.cpp:295-306), in
-//             one of two layouts chosen when the graph is built (results are identical):
+//             one of three layouts chosen when the graph is built (results are identical):
 //             compact, uint4 (src, dst, suf_src, suf_dst): the COO plus, per endpoint, how many
 //               entries follow this edge in that endpoint's edge-id-ordered list;
 //             wide, ZgRec (32 bytes, one sector): e = the compact record, p = (pos_src, pos_dst,
 //               pre_src, pre_dst), the index of the edge's own entry in adj_e within each
-//               endpoint's list and how many entries precede it there.
+//               endpoint's list and how many entries precede it there;
+//             packed (16 bytes): src, dst, suf_src, suf_dst, pos_src, pos_dst as bit fields of
+//               two words, w0 = src | dst << V | suf_src << 2V and w1 = suf_dst | pos_src << S |
+//               pos_dst << (S + P) (V, S, P: the graph's vertex, suffix and slot bits), where
+//               they fit.
 //             A conditional step from an edge's endpoints needs S = suf_src + suf_dst and the
-//             entries' addresses pos + 1 .. pos + suf: the wide record gives both in one read, the
-//             compact one needs the endpoints' offsets (off32) as a second, dependent read.  The
-//             compact layout keeps graphs whose working set is near the L2 size resident; the wide
-//             one saves a dependent read and two sectors per step on graphs far larger than L2.
+//             entries' addresses pos + 1 .. pos + suf: the wide and packed records give both in
+//             one read, the compact one needs the endpoints' offsets (off32) as a second,
+//             dependent read.  The 16-byte layouts keep graphs whose working set is near the L2
+//             size resident; the wide one saves a dependent read and two sectors per step on graphs
+//             far larger than L2 (where the packed fields would not fit either).
 //   off[V+1]  int64 offsets shared by both adjacency arrays (outgoing_adj_index).
 //   adj_e[2m] uint2 (nbr, edge_id) sorted by edge id per vertex (outgoing_adj_list order,
 //             asserted at src/Graph.cpp:324-334): the sampling order.  Followed by 8 entries of
@@ -46,8 +51,10 @@ struct ZgDevGraph {
   uint32_t nv;
   uint32_t hbits;  // log2 of the cuckoo table's bucket count
   uint64_t m;
-  const void* rec;  // ZgRec[m] when wide, else uint4[m]
+  const void* rec;  // ZgRec[m] when wide, else uint4[m] (compact) or ulonglong2[m] (packed)
   uint32_t wide;
+  uint32_t packed;
+  uint32_t pk_v, pk_s, pk_p;  // packed: vertex, suffix and slot field bits
   const int64_t* off;
   const uint2* adj_e;
   const uint2* adj_n;
@@ -62,9 +69,33 @@ struct ZgDevGraph {
 // second bucket: only then can a key absent from its first bucket be in its second.
 #define ZG_HASH_OVERFLOW 0x8000000000000000ull
 
+// A packed record's fields: q = (src, dst, suf_src, suf_dst), pos = (pos_src, pos_dst).
+__host__ __device__ __forceinline__ void zg_unpack(uint32_t vb, uint32_t sb, uint32_t pb, uint64_t w0, uint64_t w1,
+                                                   uint32_t& src, uint32_t& dst, uint32_t& suf_src, uint32_t& suf_dst,
+                                                   uint32_t& pos_src, uint32_t& pos_dst) {
+  const uint32_t vm = (uint32_t)((1ull << vb) - 1), sm = (uint32_t)((1ull << sb) - 1), pm = (uint32_t)((1ull << pb) - 1);
+  src = (uint32_t)w0 & vm;
+  dst = (uint32_t)(w0 >> vb) & vm;
+  suf_src = (uint32_t)(w0 >> (2 * vb)) & sm;
+  suf_dst = (uint32_t)w1 & sm;
+  pos_src = (uint32_t)(w1 >> sb) & pm;
+  pos_dst = (uint32_t)(w1 >> (sb + pb)) & pm;
+}
+
 #ifdef __CUDACC__
-// (src, dst, suf_src, suf_dst) of edge e, in either layout.
+// A packed record of edge e: q = (src, dst, suf_src, suf_dst), pos = (pos_src, pos_dst).
+__device__ __forceinline__ void zg_rec_packed(const ZgDevGraph& g, uint64_t e, uint4& q, uint2& pos) {
+  const ulonglong2 w = __ldg(&((const ulonglong2*)g.rec)[e]);
+  zg_unpack(g.pk_v, g.pk_s, g.pk_p, w.x, w.y, q.x, q.y, q.z, q.w, pos.x, pos.y);
+}
+// (src, dst, suf_src, suf_dst) of edge e, in any layout.
 __device__ __forceinline__ uint4 zg_rec_e(const ZgDevGraph& g, uint64_t e) {
+  if (g.packed) {
+    uint4 q;
+    uint2 pos;
+    zg_rec_packed(g, e, q, pos);
+    return q;
+  }
   return g.wide ? __ldg(&((const ZgRec*)g.rec)[e].e) : __ldg(&((const uint4*)g.rec)[e]);
 }
 #endif
@@ -96,6 +127,7 @@ struct zg_graph {
   ZgDevGraph d;
   void* rec;
   uint32_t wide;
+  uint32_t packed;
   int64_t* off;
   uint2* adj_e;
   uint2* adj_n;

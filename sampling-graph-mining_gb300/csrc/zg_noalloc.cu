@@ -18,7 +18,7 @@
 
 #include "zg_internal.cuh"
 
-int zg_sample_grid(int kind, bool wide);
+int zg_sample_grid(int kind, int layout);
 int zg_launch_sample_with_scratch(const zg_graph* g, const zg_program* p, uint64_t n, uint64_t first, uint64_t seed,
                                   uint32_t stream_id, cudaStream_t s, ZgPartial* scratch, int grid, void* d_result);
 
@@ -52,7 +52,7 @@ int scratch_for_current_device(ZgPartial** out) {
 extern "C" int zg_run_noalloc(const zg_graph* g, const zg_program* p, uint64_t n, uint64_t first_sample,
                               uint64_t seed, uint32_t stream_id, void* cuda_stream, void* d_result) {
   if (!g || !p || !d_result) return zg_set_error(ZG_ERR_INVALID_ARG, "null graph, program or result"), ZG_ERR_INVALID_ARG;
-  int grid = zg_sample_grid(p->kind, g->wide != 0);
+  int grid = zg_sample_grid(p->kind, g->wide ? 1 : g->packed ? 2 : 0);
   uint64_t need = (n + 255) / 256;
   if ((uint64_t)grid > need) grid = (int)(need ? need : 1);
   if (grid > ZG_NOALLOC_MAX_BLOCKS)

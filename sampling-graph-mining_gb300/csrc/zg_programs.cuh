@@ -201,6 +201,15 @@ __device__ __forceinline__ void edge_rec(const ZgDevGraph& g, uint64_t e, uint4&
     ld_rec(&((const ZgRec*)g.rec)[e], q, p);
     return;
   }
+  if (g.packed) {  // the slots from the record, the predecessor counts from the offsets (if used)
+    uint2 pos;
+    zg_rec_packed(g, e, q, pos);
+    p.x = pos.x;
+    p.y = pos.y;
+    p.z = p.x - ZG_LDG(&g.off32[q.x]);
+    p.w = p.y - ZG_LDG(&g.off32[q.y]);
+    return;
+  }
   q = ZG_LDG(&((const uint4*)g.rec)[e]);
   p.x = ZG_LDG(&g.off32[q.x + 1]) - q.z - 1;
   p.y = ZG_LDG(&g.off32[q.y + 1]) - q.w - 1;
@@ -211,7 +220,7 @@ __device__ __forceinline__ void edge_rec(const ZgDevGraph& g, uint64_t e, uint4&
 // The first entry after edge (q, p) in its src's (dst = false) or dst's list.  Compact layout:
 // one offset read, of the chosen endpoint only.
 __device__ __forceinline__ uint32_t after_edge(const ZgDevGraph& g, const uint4& q, const uint4& p, bool dst) {
-  if (g.wide) return (dst ? p.y : p.x) + 1;
+  if (g.wide || g.packed) return (dst ? p.y : p.x) + 1;
   return ZG_LDG(&g.off32[(dst ? q.y : q.x) + 1]) - (dst ? q.w : q.z);
 }
 
@@ -229,6 +238,16 @@ __device__ __forceinline__ EdgeAt edge_at(const ZgDevGraph& g, uint64_t e, uint3
     r.suf = s ? q.z : q.w;
     r.pos = s ? p.x : p.y;
     r.pre = s ? p.z : p.w;
+    return r;
+  }
+  if (g.packed) {
+    uint4 q;
+    uint2 pos;
+    zg_rec_packed(g, e, q, pos);
+    const bool s = q.x == v;
+    r.suf = s ? q.z : q.w;
+    r.pos = s ? pos.x : pos.y;
+    r.pre = 0;
     return r;
   }
   const uint4 q = ZG_LDG(&((const uint4*)g.rec)[e]);

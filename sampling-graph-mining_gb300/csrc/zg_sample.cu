@@ -36,7 +36,7 @@ __device__ __forceinline__ void run_program(const ZgDevGraph& g, const ZgProgPar
 // holds 32 samples, so most warps run one program on all lanes; leftovers run at the end.
 // Exact sums are unchanged (the same samples, integer sums); the variance term is summed per lane
 // in another order.
-template <bool WIDE>
+template <int LAYOUT>
 __device__ __forceinline__ void four_chain_grouped(const ZgDevGraph& g, uint64_t n, uint64_t first, uint64_t seed,
                                                    const ZgKeys& keys, uint32_t stream, uint32_t den, Acc& a,
                                                    AccSlots<kBlock>& sl) {
@@ -99,12 +99,14 @@ __device__ __forceinline__ void four_chain_grouped(const ZgDevGraph& g, uint64_t
 
 // Production kernels: one specialisation per program, per register budget (MINB resident blocks
 // of 256 threads requested from the compiler; zg_tune picks the fastest per program) and per record
-// layout (the layout tests of the record accessors fold away; each layout gets its own registers).
-template <int KIND, int MINB, bool WIDE>
+// layout (0 compact, 1 wide, 2 packed: the layout tests of the record accessors fold away; each
+// layout gets its own registers).
+template <int KIND, int MINB, int LAYOUT>
 __global__ void __launch_bounds__(kBlock, MINB)
     k_sample(ZgDevGraph g, ZgProgParams pp, uint64_t n, uint64_t first, uint64_t seed, const __grid_constant__ ZgKeys keys,
              uint32_t stream, ZgPartial* __restrict__ partials) {
-  g.wide = WIDE;
+  g.wide = LAYOUT == 1;
+  g.packed = LAYOUT == 2;
   // Sums in shared-memory slots for the programs with long dependent chains (measured: 4-clique
   // and 4-chain faster); the triangle and 3-chain were faster with them in registers.
   constexpr bool kSlots = KIND != ZG_PROG_THREE_CHAIN && KIND != ZG_PROG_TRIANGLE;
@@ -113,7 +115,7 @@ __global__ void __launch_bounds__(kBlock, MINB)
   acc_init(a);
   if (kSlots) acc_slots_init(sl);
   if (KIND == ZG_PROG_FOUR_CHAIN) {
-    four_chain_grouped<WIDE>(g, n, first, seed, keys, stream, pp.den_log2, a, sl);
+    four_chain_grouped<LAYOUT>(g, n, first, seed, keys, stream, pp.den_log2, a, sl);
     acc_from_slots(a, sl);
     block_reduce_store<kBlock>(a, &partials[blockIdx.x]);
     return;
@@ -450,41 +452,45 @@ constexpr int kMinBlocks[kVariants] = {1, 2, 3, 4, 5, 6, 8};
 typedef void (*SampleKernel)(ZgDevGraph, ZgProgParams, uint64_t, uint64_t, uint64_t, const ZgKeys, uint32_t,
                              ZgPartial*);
 
-template <int KIND, bool WIDE>
+template <int KIND, int LAYOUT>
 SampleKernel kernel_variant(int v) {
   switch (v) {
-    case 0: return k_sample<KIND, 1, WIDE>;
-    case 1: return k_sample<KIND, 2, WIDE>;
-    case 2: return k_sample<KIND, 3, WIDE>;
-    case 3: return k_sample<KIND, 4, WIDE>;
-    case 4: return k_sample<KIND, 5, WIDE>;
-    case 5: return k_sample<KIND, 6, WIDE>;
-    default: return k_sample<KIND, 8, WIDE>;
+    case 0: return k_sample<KIND, 1, LAYOUT>;
+    case 1: return k_sample<KIND, 2, LAYOUT>;
+    case 2: return k_sample<KIND, 3, LAYOUT>;
+    case 3: return k_sample<KIND, 4, LAYOUT>;
+    case 4: return k_sample<KIND, 5, LAYOUT>;
+    case 5: return k_sample<KIND, 6, LAYOUT>;
+    default: return k_sample<KIND, 8, LAYOUT>;
   }
 }
 
-template <bool WIDE>
+template <int LAYOUT>
 SampleKernel kernel_for_layout(int kind, int v) {
   switch (kind) {
-    case ZG_PROG_TRIANGLE: return kernel_variant<ZG_PROG_TRIANGLE, WIDE>(v);
-    case ZG_PROG_FOUR_CLIQUE: return kernel_variant<ZG_PROG_FOUR_CLIQUE, WIDE>(v);
-    case ZG_PROG_FOUR_CLIQUE_UNBIASED: return kernel_variant<ZG_PROG_FOUR_CLIQUE_UNBIASED, WIDE>(v);
-    case ZG_PROG_THREE_CHAIN: return kernel_variant<ZG_PROG_THREE_CHAIN, WIDE>(v);
-    case ZG_PROG_FOUR_CHAIN: return kernel_variant<ZG_PROG_FOUR_CHAIN, WIDE>(v);
-    case ZG_PROG_CHAIN: return kernel_variant<ZG_PROG_CHAIN, WIDE>(v);
-    default: return kernel_variant<ZG_PROG_PATTERN, WIDE>(v);
+    case ZG_PROG_TRIANGLE: return kernel_variant<ZG_PROG_TRIANGLE, LAYOUT>(v);
+    case ZG_PROG_FOUR_CLIQUE: return kernel_variant<ZG_PROG_FOUR_CLIQUE, LAYOUT>(v);
+    case ZG_PROG_FOUR_CLIQUE_UNBIASED: return kernel_variant<ZG_PROG_FOUR_CLIQUE_UNBIASED, LAYOUT>(v);
+    case ZG_PROG_THREE_CHAIN: return kernel_variant<ZG_PROG_THREE_CHAIN, LAYOUT>(v);
+    case ZG_PROG_FOUR_CHAIN: return kernel_variant<ZG_PROG_FOUR_CHAIN, LAYOUT>(v);
+    case ZG_PROG_CHAIN: return kernel_variant<ZG_PROG_CHAIN, LAYOUT>(v);
+    default: return kernel_variant<ZG_PROG_PATTERN, LAYOUT>(v);
   }
 }
 
-SampleKernel kernel_for(int kind, int v, bool wide) {
-  return wide ? kernel_for_layout<true>(kind, v) : kernel_for_layout<false>(kind, v);
+SampleKernel kernel_for(int kind, int v, int layout) {
+  return layout == 1 ? kernel_for_layout<1>(kind, v) : layout == 2 ? kernel_for_layout<2>(kind, v)
+                                                                  : kernel_for_layout<0>(kind, v);
 }
+
+// The record layout a graph's sampling kernels are compiled for: 0 compact, 1 wide, 2 packed.
+int rec_layout(const zg_graph* g) { return g->wide ? 1 : g->packed ? 2 : 0; }
 
 // Per device: the variant each program kind uses and its occupancy grid.
 constexpr int kMaxDev = 64;
 std::mutex g_tune_mu;
 int g_variant[kMaxDev][8];
-int g_grid[kMaxDev][8][kVariants][2];
+int g_grid[kMaxDev][8][kVariants][3];
 bool g_tune_init[kMaxDev];
 // Defaults before tuning (register footprints measured with -Xptxas -v).
 constexpr int kDefaultVariant[8] = {3, 3, 2, 3, 2, 3, 3, 3};
@@ -507,15 +513,15 @@ int variant_for(int kind) {
   return g_variant[d][kind_slot(kind)];
 }
 
-int grid_for_variant(int kind, int v, bool wide) {
+int grid_for_variant(int kind, int v, int layout) {
   int d = current_device();
   std::lock_guard<std::mutex> lk(g_tune_mu);
-  int& g = g_grid[d][kind_slot(kind)][v][wide ? 1 : 0];
-  if (!g) g = grid_of(kernel_for(kind, v, wide));
+  int& g = g_grid[d][kind_slot(kind)][v][layout];
+  if (!g) g = grid_of(kernel_for(kind, v, layout));
   return g;
 }
 
-int grid_for_kind(int kind, bool wide) { return grid_for_variant(kind, variant_for(kind), wide); }
+int grid_for_kind(int kind, int layout) { return grid_for_variant(kind, variant_for(kind), layout); }
 
 int validate_run(const zg_graph* g, const zg_program* p) {
   if (!g || !p) return zg_set_error(ZG_ERR_INVALID_ARG, "null graph or program"), ZG_ERR_INVALID_ARG;
@@ -525,7 +531,7 @@ int validate_run(const zg_graph* g, const zg_program* p) {
 int launch_variant(const zg_graph* g, const zg_program* p, int v, uint64_t n, uint64_t first, uint64_t seed,
                    uint32_t stream_id, cudaStream_t s, ZgPartial* parts, int grid) {
   ZgProgParams pp = params_for(p);
-  SampleKernel k = kernel_for(p->kind, v, g->wide != 0);
+  SampleKernel k = kernel_for(p->kind, v, rec_layout(g));
   k<<<grid, kBlock, 0, s>>>(g->d, pp, n, first, seed, zg_round_keys(seed), stream_id, parts);
   return ZG_OK;
 }
@@ -546,7 +552,7 @@ void zg_partial_to_counters(const void* partial, uint32_t den, zg_counters* out)
 double zg_exact_mean_host(const uint64_t s[5], uint32_t den, uint64_t n) { return exact_mean(s, den, n); }
 
 // Shared by the allocation-free entry points of other translation units.
-int zg_sample_grid(int kind, bool wide) { return grid_for_kind(kind, wide); }
+int zg_sample_grid(int kind, int layout) { return grid_for_kind(kind, layout); }
 
 // Per-group estimates (device array out[n_groups]) on stream s.
 int zg_launch_groups(const zg_graph* g, const zg_program* p, uint64_t n_groups, uint32_t group, uint64_t first,
@@ -578,7 +584,7 @@ extern "C" int zg_run(const zg_graph* g, const zg_program* p, uint64_t n, uint64
   if (!out) return zg_set_error(ZG_ERR_INVALID_ARG, "null output"), ZG_ERR_INVALID_ARG;
   cudaStream_t s = (cudaStream_t)cuda_stream;
   uint64_t maxg = (n + kBlock - 1) / kBlock;
-  int grid = grid_for_kind(p->kind, g->wide != 0);
+  int grid = grid_for_kind(p->kind, rec_layout(g));
   if ((uint64_t)grid > maxg) grid = (int)(maxg ? maxg : 1);
   ZgPartial* parts = nullptr;
   ZG_CUDA(zg_malloc_async((void**)&parts, sizeof(ZgPartial) * (grid + 1), s));
@@ -603,7 +609,7 @@ extern "C" int zg_run_async(const zg_graph* g, const zg_program* p, uint64_t n, 
   if (!d_result) return zg_set_error(ZG_ERR_INVALID_ARG, "null device result"), ZG_ERR_INVALID_ARG;
   cudaStream_t s = (cudaStream_t)cuda_stream;
   uint64_t maxg = (n + kBlock - 1) / kBlock;
-  int grid = grid_for_kind(p->kind, g->wide != 0);
+  int grid = grid_for_kind(p->kind, rec_layout(g));
   if ((uint64_t)grid > maxg) grid = (int)(maxg ? maxg : 1);
   ZgPartial* parts = nullptr;
   ZG_CUDA(zg_malloc_async((void**)&parts, sizeof(ZgPartial) * grid, s));
@@ -646,7 +652,7 @@ extern "C" int zg_tune(const zg_graph* g, const zg_program* p, uint64_t probe_sa
   if (probe_samples == 0) probe_samples = 1ull << 22;
   cudaStream_t s = (cudaStream_t)cuda_stream;
   int grid_max = 0;
-  for (int v = 0; v < kVariants; ++v) grid_max = std::max(grid_max, grid_for_variant(p->kind, v, g->wide != 0));
+  for (int v = 0; v < kVariants; ++v) grid_max = std::max(grid_max, grid_for_variant(p->kind, v, rec_layout(g)));
   ZgPartial* parts = nullptr;
   ZG_CUDA(zg_malloc_async((void**)&parts, sizeof(ZgPartial) * (grid_max + 1), s));
   cudaEvent_t e0, e1;
@@ -657,7 +663,7 @@ extern "C" int zg_tune(const zg_graph* g, const zg_program* p, uint64_t probe_sa
   const int reps = 3;
   cudaError_t ce = cudaSuccess;
   for (int v = 0; v < kVariants && ce == cudaSuccess; ++v) {
-    int grid = grid_for_variant(p->kind, v, g->wide != 0);
+    int grid = grid_for_variant(p->kind, v, rec_layout(g));
     uint64_t maxg = (probe_samples + kBlock - 1) / kBlock;
     if ((uint64_t)grid > maxg) grid = (int)maxg;
     float vbest = 1e30f;

@@ -34,7 +34,7 @@ EXACT_TRIANGLE, EXACT_WEDGE, EXACT_THREE_PATH, EXACT_FIVE_STAR, EXACT_FOUR_CLIQU
 PRED_GE, PRED_LT, PRED_GT, PRED_LE, PRED_EQ, PRED_NE, PRED_RANGE = 1, 2, 3, 4, 5, 6, 7
 QUERY_THREE_MOTIF = 16
 GRAPH_SAMPLING_ONLY = 1
-RECORDS_AUTO, RECORDS_COMPACT, RECORDS_WIDE = 0, 1, 2
+RECORDS_AUTO, RECORDS_COMPACT, RECORDS_WIDE, RECORDS_PACKED = 0, 1, 2, 3
 BATCH_MAX_QUERIES, BATCH_MAX_CHUNKS = 65536, 65536
 NO_SHUFFLE = 0xFFFFFFFFFFFFFFFF
 MAX_DRAWS = 16
@@ -50,7 +50,7 @@ class ZgError(RuntimeError):
 class GraphMeta(C.Structure):
     _fields_ = [("num_vertices", C.c_uint32), ("weighted", C.c_uint32), ("num_local_edges", C.c_uint64),
                 ("num_edges", C.c_uint64), ("max_degree", C.c_uint64), ("device_bytes", C.c_uint64),
-                ("record_bytes", C.c_uint32), ("reserved", C.c_uint32)]
+                ("record_bytes", C.c_uint32), ("record_layout", C.c_uint32)]
 
 
 class Counters(C.Structure):
@@ -366,7 +366,8 @@ class Graph:
 
 def set_record_layout(layout):
     """zg_set_record_layout: per-edge record layout of the graphs built from now on
-    (RECORDS_AUTO, RECORDS_COMPACT or RECORDS_WIDE); estimates are identical under each."""
+    (RECORDS_AUTO, RECORDS_COMPACT, RECORDS_WIDE or RECORDS_PACKED); estimates are identical under
+    each."""
     check(lib().zg_set_record_layout(layout))
 
 

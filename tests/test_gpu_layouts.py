@@ -1,8 +1,9 @@
-"""The two per-edge record layouts (zg_set_record_layout): compact (16 bytes, steps read vertex
-offsets) and wide (32 bytes: each edge's slot and predecessor count in both endpoint lists).
-Every program, the fused 3-motif, batches, derived graphs and exports give identical results
-under both, sample for sample; the parity tests against the oracle run on the layout the
-automatic choice picks for their (small) graphs, so equality here carries them to the other."""
+"""The three per-edge record layouts (zg_set_record_layout): compact (16 bytes, steps read vertex
+offsets), wide (32 bytes: each edge's slot and predecessor count in both endpoint lists) and
+packed (16 bytes of bit fields: the vertices, suffix sizes and slots).  Every program, the fused
+3-motif, batches, derived graphs and exports give identical results under each, sample for
+sample; the parity tests against the oracle run on the layout the automatic choice picks for
+their (small) graphs, packed, so equality here carries them to the others."""
 import numpy as np
 import pytest
 
@@ -36,16 +37,21 @@ def pair():
     e = Z.gen_rmat(12, 10, seed=17)
     w = Z.gen_weights(len(e), 100, seed=4)
     mk = lambda: Z.Graph.from_edges(e, 1 << 12, weights=w, shuffle_seed=5)  # noqa: E731
-    return _build(Z.RECORDS_COMPACT, mk), _build(Z.RECORDS_WIDE, mk)
+    return _build(Z.RECORDS_COMPACT, mk), _build(Z.RECORDS_WIDE, mk), _build(Z.RECORDS_PACKED, mk)
 
 
 def test_meta_and_exports(pair):
-    c, wd = pair
-    assert c.meta().record_bytes == 16 and wd.meta().record_bytes == 32
+    c, wd, pk = pair
+    assert (c.meta().record_bytes, wd.meta().record_bytes, pk.meta().record_bytes) == (16, 32, 16)
+    assert (c.meta().record_layout, wd.meta().record_layout, pk.meta().record_layout) == (
+        Z.RECORDS_COMPACT, Z.RECORDS_WIDE, Z.RECORDS_PACKED)
     assert wd.meta().device_bytes - c.meta().device_bytes == 16 * c.num_local_edges
-    dc, dw = c.download(), wd.download()
-    for k in ("edges", "weights", "offsets", "adj_e", "adj_n", "suffix"):
-        assert np.array_equal(dc[k], dw[k]), k
+    assert pk.meta().device_bytes == c.meta().device_bytes
+    dc = c.download()
+    for other in (wd, pk):
+        do = other.download()
+        for k in ("edges", "weights", "offsets", "adj_e", "adj_n", "suffix"):
+            assert np.array_equal(dc[k], do[k]), k
 
 
 PROGRAMS = [("triangle", Z.PROG_TRIANGLE, 0, None), ("four_clique", Z.PROG_FOUR_CLIQUE, 0, None),
@@ -58,41 +64,51 @@ PROGRAMS = [("triangle", Z.PROG_TRIANGLE, 0, None), ("four_clique", Z.PROG_FOUR_
 
 @pytest.mark.parametrize("name,kind,param,pat", PROGRAMS, ids=[p[0] for p in PROGRAMS])
 def test_programs_identical(pair, name, kind, param, pat):
-    c, wd = pair
+    c, wd, pk = pair
     p = Z.Program(kind, param, pat)
-    for n, seed, first in ((1 << 20, 3, 0), (77777, 9, 1 << 33)):
-        _same(p.run(c, n, seed, stream_id=4, first_sample=first), p.run(wd, n, seed, stream_id=4, first_sample=first),
-              (name, n))
-    tc, tw = p.run_debug(c, 4096, 11), p.run_debug(wd, 4096, 11)
-    for k in ("ndraws", "hit", "fail", "shift", "sectors", "closures", "w", "num", "lo", "hi", "val"):
-        assert np.array_equal(tc[k], tw[k]), (name, k)
+    for other in (wd, pk):
+        for n, seed, first in ((1 << 20, 3, 0), (77777, 9, 1 << 33)):
+            _same(p.run(c, n, seed, stream_id=4, first_sample=first),
+                  p.run(other, n, seed, stream_id=4, first_sample=first), (name, n))
+        tc, tw = p.run_debug(c, 4096, 11), p.run_debug(other, 4096, 11)
+        for k in ("ndraws", "hit", "fail", "shift", "sectors", "closures", "w", "num", "lo", "hi", "val"):
+            assert np.array_equal(tc[k], tw[k]), (name, k)
 
 
 def test_three_motif_and_batch_identical(pair):
-    c, wd = pair
-    for a, b in zip(Z.run_three_motif(c, 1 << 20, 1 << 19, 7, 1, 2), Z.run_three_motif(wd, 1 << 20, 1 << 19, 7, 1, 2)):
-        _same(a, b, "three_motif")
+    c, wd, pk = pair
+    for other in (wd, pk):
+        for a, b in zip(Z.run_three_motif(c, 1 << 20, 1 << 19, 7, 1, 2),
+                        Z.run_three_motif(other, 1 << 20, 1 << 19, 7, 1, 2)):
+            _same(a, b, "three_motif")
     qs = [{"kind": Z.PROG_TRIANGLE, "n": 300000, "seed": 1, "pred_op": Z.PRED_GE, "t0": 40},
           {"kind": Z.QUERY_THREE_MOTIF, "n": 200000, "seed": 2},
           {"kind": Z.PROG_FOUR_CHAIN, "n": 250000, "seed": 3, "first_sample": 99},
           {"kind": Z.PROG_PATTERN, "program": Z.Program(Z.PROG_PATTERN, pattern=STAR), "n": 100000, "seed": 4}]
     rc = _build(Z.RECORDS_COMPACT, lambda: Z.Batch(c, max_queries=8).run(qs))
     rw = _build(Z.RECORDS_WIDE, lambda: Z.Batch(wd, max_queries=8).run(qs))
-    for q, (a, a2), (b, b2) in zip(qs, rc, rw):
+    rp = _build(Z.RECORDS_PACKED, lambda: Z.Batch(pk, max_queries=8).run(qs))
+    for q, (a, a2), (b, b2), (d, d2) in zip(qs, rc, rw, rp):
         _same(a, b, q)
         _same(a2, b2, q)
+        _same(a, d, q)
+        _same(a2, d2, q)
 
 
 def test_derived_graphs_and_exact_counts(pair):
-    c, wd = pair
+    c, wd, pk = pair
     fc = _build(Z.RECORDS_COMPACT, lambda: c.filter(Z.PRED_LT, 50, shuffle_seed=8))
     fw = _build(Z.RECORDS_WIDE, lambda: wd.filter(Z.PRED_LT, 50, shuffle_seed=8))
+    fp = _build(Z.RECORDS_PACKED, lambda: pk.filter(Z.PRED_LT, 50, shuffle_seed=8))
     assert fc.meta().record_bytes == 16 and fw.meta().record_bytes == 32
+    assert fp.meta().record_layout == Z.RECORDS_PACKED
     assert np.array_equal(fc.download()["edges"], fw.download()["edges"])
+    assert np.array_equal(fc.download()["edges"], fp.download()["edges"])
     p = Z.Program(Z.PROG_FOUR_CLIQUE)
     _same(p.run(fc, 1 << 19, 5), p.run(fw, 1 << 19, 5), "filtered")
+    _same(p.run(fc, 1 << 19, 5), p.run(fp, 1 << 19, 5), "filtered")
     for kind in (Z.EXACT_TRIANGLE, Z.EXACT_WEDGE, Z.EXACT_FOUR_CLIQUE):
-        assert c.exact_count(kind) == wd.exact_count(kind), kind
+        assert c.exact_count(kind) == wd.exact_count(kind) == pk.exact_count(kind), kind
     e_c = _build(Z.RECORDS_COMPACT, lambda: Z.elp_plain(c, Z.Program(Z.PROG_TRIANGLE), 0.05, 0.95, 3))
     e_w = _build(Z.RECORDS_WIDE, lambda: Z.elp_plain(wd, Z.Program(Z.PROG_TRIANGLE), 0.05, 0.95, 3))
     assert e_c.n_required == e_w.n_required
@@ -102,10 +118,13 @@ def test_device_generator_layouts():
     Z.init(0)
     gc = _build(Z.RECORDS_COMPACT, lambda: Z.Graph.gen_chung_lu(30000, 2.4, 10.0, seed=3, sampling_only=True))
     gw = _build(Z.RECORDS_WIDE, lambda: Z.Graph.gen_chung_lu(30000, 2.4, 10.0, seed=3, sampling_only=True))
+    gp = _build(Z.RECORDS_PACKED, lambda: Z.Graph.gen_chung_lu(30000, 2.4, 10.0, seed=3, sampling_only=True))
+    assert gp.meta().record_layout == Z.RECORDS_PACKED
     p = Z.Program(Z.PROG_FOUR_CHAIN)
     _same(p.run(gc, 1 << 20, 2), p.run(gw, 1 << 20, 2), "chung-lu")
+    _same(p.run(gc, 1 << 20, 2), p.run(gp, 1 << 20, 2), "chung-lu")
     with pytest.raises(Z.ZgError):
-        Z.set_record_layout(3)
+        Z.set_record_layout(4)
 
 
 def test_tiny_graphs_and_sample_counts():
@@ -118,7 +137,10 @@ def test_tiny_graphs_and_sample_counts():
     for e, nv in cases:
         gc = _build(Z.RECORDS_COMPACT, lambda: Z.Graph.from_edges(e, nv))
         gw = _build(Z.RECORDS_WIDE, lambda: Z.Graph.from_edges(e, nv))
+        gp = _build(Z.RECORDS_PACKED, lambda: Z.Graph.from_edges(e, nv))
         for name, kind, param, pat in PROGRAMS:
             p = Z.Program(kind, param, pat)
             for n in (1, 31, 33, 1000):
-                _same(p.run(gc, n, 3, first_sample=n), p.run(gw, n, 3, first_sample=n), (len(e), name, n))
+                a = p.run(gc, n, 3, first_sample=n)
+                _same(a, p.run(gw, n, 3, first_sample=n), (len(e), name, n))
+                _same(a, p.run(gp, n, 3, first_sample=n), (len(e), name, n))
