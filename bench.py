@@ -1,24 +1,34 @@
 #!/usr/bin/env python
 """Benchmark of the neighbour-sampling estimator hot path on GB300.
 
-Workload (default "rmat20"): undirected R-MAT scale 20, edge factor 3, a/b/c/d = .57/.19/.19/.05,
-self-loops and duplicates removed (~3.1M edges, seeded synthetic input); one step = the
-triangle, 4-clique, 3-chain and 4-chain estimators with 2^26 samples each (2^28 estimators).
+Default workload "rmat26" (the largest single-GPU configuration): undirected R-MAT scale 26, edge
+factor 24, a/b/c/d = .57/.19/.19/.05, seed 26, self-loops and duplicates removed (1.57 G edges,
+seeded synthetic input generated and built on the device).  One step = the 4-clique, 5-star and
+5-house estimators with 2^30 samples each, submitted as one batch (persistent work-queue kernels
+replayed through a CUDA graph).
 
-  value : samples/s over the timed steps, device time from CUDA events on the launching stream
-          (graph resident in HBM; L2 flushed between steps by writing a 512 MiB buffer).
-  e2e   : samples/s through the public API (ZGraphInstance.calculate -> zg_run): host wall time
-          per query including the device->host read of each result.
-  roofline: dominant kernel, algorithmic bytes = access-model sectors x 32 B per sample (measured
-          per program by the debug kernel on 2^16 samples) x samples / kernel time.
-  cpu_baseline: the CPU restatement of the reference path (oracle, all host threads) on a
-          bounded sample of the same workload.
+  value : samples/s over the timed steps, device time from CUDA events around the batch's graph
+          launch on the launching stream (graph resident in HBM; L2 flushed between steps).
+  e2e   : samples/s through the public batch API (zg_batch_submit + zg_batch_wait) with the host
+          buffers: every step copies the query descriptors and work list host->device and the
+          results device->host (byte counts from zg_batch_copy_bytes); the graph stays resident.
+  roofline: bytes the production sampling kernels move per sample (zg_touch_sectors: the same
+          kernel with every load's 32-byte sectors counted) x samples / the step's device time,
+          against the measured HBM copy peak (the graph is ~300x the L2).
+  cpu_baseline: the oracle (CPU restatement of the reference path, all host threads) on the same
+          graph, a bounded sample of each program.
+  time_to_bound: triangle and unbiased 4-clique queries to 1 % at 95 %, plain ErrorProfile sizing
+          vs learned sizing, the same empirical bound check; coverage over 40 seeds on R-MAT scale 20.
 
---impl reference runs that CPU restatement as the measured arm (the reference is CPU code and
-does not build on this host without its MPI/NUMA stack).  Under torchrun each rank runs its
-own shard of sample indices (weak scaling); rank 0 prints one JSON line.
+--impl reference times the oracle (the reference's CPU path restated in C, all host threads) on
+the same workload and graph, generated on the host by oracle/zgo_gen.c without the GPU library.
+Other workloads: rmat20 (R-MAT scale 20, ef 3; four programs x 2^26), rmat13 (scale 13, ef 12;
+triangle x 2^20), chunglu_batch (Chung-Lu 4.8 M vertices, 512 mixed predicate queries).
+Under torchrun each rank runs its own shard of sample indices (weak scaling, rmat20/rmat13); rank 0
+prints one JSON line.
 """
 import argparse
+import hashlib
 import json
 import os
 import statistics
@@ -31,24 +41,24 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "sampling-graph-mining_gb300"))
 
 METRIC = "time-to-1%-error@95% and samples/s, learned vs plain ELP, 1 GB300"
+RMAT = {"a": 0.57, "b": 0.19, "c": 0.19}
 WORKLOADS = {
-    "rmat20": {"scale": 20, "edge_factor": 3, "a": 0.57, "b": 0.19, "c": 0.19, "seed": 1, "samples": 1 << 26,
+    "rmat20": {"scale": 20, "edge_factor": 3, "seed": 1, "samples": 1 << 26,
                "programs": ["triangle", "four_clique", "three_chain", "four_chain"]},
-    "rmat13": {"scale": 13, "edge_factor": 12, "a": 0.57, "b": 0.19, "c": 0.19, "seed": 1, "samples": 1 << 20,
-               "programs": ["triangle"]},
+    "rmat13": {"scale": 13, "edge_factor": 12, "seed": 1, "samples": 1 << 20, "programs": ["triangle"]},
 }
-# Batched workloads (one submit of many queries per step; graphs generated on the device):
-#   chunglu_batch: Chung-Lu 4.8 M vertices, exponent 2.3, ~43 M edges, edge data in [0, 100);
-#                  512 queries over {triangle, 3-motif, all-predicate w >= T, at-least-one w >= T},
-#                  T uniform in [10, 90], budgets 2^U(12, 24).
-#   rmat26:        R-MAT scale 26, edge factor 24 (~1.4 G edges); 4-clique, 5-star, 5-house at 2^30.
 BATCH_WORKLOADS = {
+    "rmat26": {"gen": "rmat", "scale": 26, "edge_factor": 24, "seed": 26, "samples": 1 << 30,
+               "programs": ["four_clique", "five_star", "five_house"]},
     "chunglu_batch": {"gen": "chung_lu", "n": 4800000, "exponent": 2.3, "avg_degree": 18.0, "seed": 2024,
                       "max_weight": 100, "queries": 512},
-    "rmat26": {"gen": "rmat", "scale": 26, "edge_factor": 24, "seed": 26, "samples": 1 << 30},
 }
-PROG_IDS = {"triangle": 1, "four_clique": 2, "three_chain": 3, "four_chain": 4}
-EXACT_IDS = {"triangle": 1, "three_chain": 2, "four_chain": 3, "four_clique": 5}
+PROG_IDS = {"triangle": 1, "four_clique": 2, "three_chain": 3, "four_chain": 4, "four_clique_unbiased": 7}
+PATTERNS = {"five_star": (5, [(0, 1), (0, 2), (0, 3), (0, 4)]),
+            "five_house": (5, [(0, 1), (0, 2), (1, 2), (1, 3), (2, 4), (3, 4)])}
+EXACT_IDS = {"triangle": 1, "three_chain": 2, "four_chain": 3, "four_clique": 5, "four_clique_unbiased": 5}
+KERNEL_SOURCES = ("zg_internal.cuh", "zg_programs.cuh", "zg_sample_kernel.cuh", "zg_sample.cu", "zg_batch.cu",
+                  "zg_graph.cu")
 
 
 def parse():
@@ -57,9 +67,10 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="rmat20", choices=sorted(WORKLOADS) + sorted(BATCH_WORKLOADS))
+    ap.add_argument("--workload", default="rmat26", choices=sorted(WORKLOADS) + sorted(BATCH_WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-time-to-bound", action="store_true")
+    ap.add_argument("--no-coverage", action="store_true")
     ap.add_argument("--variants", default=None,
                     help="fixed launch shapes instead of tuning, e.g. triangle=4,four_clique=3 "
                          "(profiling runs: no tuner probe launches)")
@@ -113,69 +124,175 @@ def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
             p = json.load(f)
-        return float(p["hbm_gbs"]), "measured"
+        return float(p["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs)"
     except (OSError, KeyError, ValueError):
         return 6800.0, "fallback"
 
 
-def profile_traffic(samples):
-    """DRAM bytes (read + write) per launch of each sampling kernel from the committed ncu summary
-    (profiles/k_sample_traffic_rmat20.txt), scaled to `samples` per launch; {} if absent."""
-    out = {}
+def kernel_source_hash():
+    """Hash of the sampling kernels' sources: ties a committed ncu traffic figure to the code it
+    was measured on (the GPU host has no git history to compare against)."""
+    h = hashlib.sha256()
+    for name in KERNEL_SOURCES:
+        with open(os.path.join(ROOT, "sampling-graph-mining_gb300", "csrc", name), "rb") as f:
+            h.update(f.read())
+    return h.hexdigest()[:16]
+
+
+def profile_traffic(kernel, workload, layout):
+    """DRAM bytes per sample of `kernel` on `workload` from profiles/dram_traffic.txt (ncu
+    dram__bytes_read.sum + dram__bytes_write.sum per launch / samples per launch), used only when the
+    record layout and the kernel-source hash it was captured at match this build; else None with
+    the reason."""
+    path = os.path.join(ROOT, "profiles", "dram_traffic.txt")
     try:
-        with open(os.path.join(ROOT, "profiles", "k_sample_traffic_rmat20.txt")) as f:
-            for line in f:
-                if line.startswith("#") or not line.strip():
-                    continue
-                name, b, n = line.split()
-                out[name] = float(b) * samples / float(n)
-    except (OSError, ValueError):
-        return {}
+        lines = [l.split() for l in open(path) if l.strip() and not l.startswith("#")]
+    except OSError:
+        return None, "no capture committed"
+    cur = kernel_source_hash()
+    for f in lines:
+        if len(f) >= 6 and f[0] == kernel and f[1] == workload:
+            if f[2] != layout:
+                return None, "capture taken with %s records, this graph has %s" % (f[2], layout)
+            if f[3] != cur:
+                return None, "stale: captured at kernel-source hash %s, this build is %s" % (f[3], cur)
+            return float(f[4]) / float(f[5]), "ncu capture (%s)" % " ".join(f[6:]) if len(f) > 6 else "ncu capture"
+    return None, "no capture of %s on %s" % (kernel, workload)
+
+
+def workload_config(name, m):
+    """The workload as both arms print it (same dict, so the two lines compare like for like)."""
+    if name in BATCH_WORKLOADS and BATCH_WORKLOADS[name]["gen"] == "rmat":
+        wl = BATCH_WORKLOADS[name]
+        desc = ("%s: R-MAT scale %d, edge factor %d, a/b/c/d=.57/.19/.19/.05, seed %d, simplified (%d undirected "
+                "edges); one step = %s estimators x 2^%d samples each"
+                % (name, wl["scale"], wl["edge_factor"], wl["seed"], m, " + ".join(wl["programs"]),
+                   wl["samples"].bit_length() - 1))
+    else:
+        wl = WORKLOADS[name]
+        desc = ("%s: R-MAT scale %d, edge factor %d, a/b/c/d=.57/.19/.19/.05, seed %d, simplified (%d undirected "
+                "edges); one step = %s estimators x 2^%d samples each"
+                % (name, wl["scale"], wl["edge_factor"], wl["seed"], m, " + ".join(wl["programs"]),
+                   wl["samples"].bit_length() - 1))
+    return {"workload": desc, "inputs": "graph built before the timed steps and kept resident (GPU arm: device memory, L2 flushed "
+                                           "between steps)"}
+
+
+# ---- CPU side (oracle): cpu_baseline and the reference arm -------------------------------------
+def oracle_programs(O, names):
+    out = []
+    for name in names:
+        if name in PATTERNS:
+            nv, pe = PATTERNS[name]
+            out.append((name, O.OracleProgram(6, pattern=(nv, pe)), 6))
+        else:
+            out.append((name, O.OracleProgram(PROG_IDS[name]), PROG_IDS[name]))
     return out
 
 
-def l2_read_gbs(Z, mib=48, reps=100):
-    """Read bandwidth of a 48 MiB buffer resident in the 129 MB L2 (zg_read_bandwidth: one
-    persistent grid, CUDA events): the L2 view of the roofline for graphs that nearly fit in L2."""
-    return Z.read_bandwidth(mib << 20, reps)
-
-
-def make_graph(Z, wl):
-    e = Z.gen_rmat(wl["scale"], wl["edge_factor"], wl["a"], wl["b"], wl["c"], wl["seed"])
-    return e, 1 << wl["scale"]
-
-
-def cpu_baseline(wl, edges, nv, threads, target_s=12.0):
-    """The oracle (CPU restatement of the reference path) on a bounded sample of the workload."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle as O
-    og = O.OracleGraph(edges, nv)
-    rates, total_samples, total_s = {}, 0, 0.0
-    budget = target_s / len(wl["programs"])
-    for name in wl["programs"]:
-        prog = O.OracleProgram(PROG_IDS[name])
-        n = 1 << 14
+def oracle_rates(O, og, names, threads, target_s):
+    """Samples/s of each program on the oracle graph: n doubles until one run takes target_s / 4."""
+    rates, total_n, total_s = {}, 0, 0.0
+    budget = target_s / len(names)
+    for name, prog, kind in oracle_programs(O, names):
+        n = 1 << 10
         while True:
             t0 = time.perf_counter()
-            O.run(og, prog, n, 0, 17, PROG_IDS[name], threads)
+            O.run(og, prog, n, 0, 17, kind, threads)
             dt = time.perf_counter() - t0
-            if dt > budget / 4 or n >= (1 << 26):
+            if dt > budget / 4 or n >= (1 << 28):
                 break
             n *= 4
         rates[name] = n / dt
-        total_samples += n
+        total_n += n
         total_s += dt
-    return {"value": total_samples / total_s, "unit": "samples/s", "cores": threads, "kind": "port",
-            "sample": "%s: %d samples per pattern class (bounded), oracle/zg_oracle.c with %d threads; per pattern %s"
-                      % (",".join(wl["programs"]), total_samples // len(wl["programs"]), threads,
-                         {k: round(v) for k, v in rates.items()})}
+    return rates, total_n, total_s
 
 
-def time_to_bound(Z, g, names, acc, eps=0.01, conf=0.95, cap=1 << 37, coverage_queries=40):
+def cpu_baseline(edges, nv, names, threads, target_s=16.0):
+    """The oracle (CPU restatement of the reference path) on a bounded sample of the workload."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    t0 = time.perf_counter()
+    og = O.OracleGraph(edges, nv)
+    build_s = time.perf_counter() - t0
+    rates, total_n, total_s = oracle_rates(O, og, names, threads, target_s)
+    return {"value": total_n / total_s, "unit": "samples/s", "cores": threads, "kind": "port",
+            "sample": "%s: %d samples in total (the last, longest run per program), oracle/zg_oracle.c with %d threads "
+                      "on the same graph (oracle graph build %.1f s); per program %s"
+                      % (",".join(names), total_n, threads, build_s, {k: round(v) for k, v in rates.items()})}
+
+
+def run_reference(args):
+    """The reference arm: the oracle (the reference's CPU path restated in C) with all host threads
+    on the same graph, generated on the host (oracle/zgo_gen.c, edge for edge the device generator's
+    graph) without the GPU library; each step a bounded sample of every program."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    if args.workload in BATCH_WORKLOADS and BATCH_WORKLOADS[args.workload]["gen"] != "rmat":
+        print(json.dumps({"impl": "reference", "unavailable": "the Chung-Lu batch has no CPU arm: the reference runs "
+                          "one query at a time; see the rmat26 and rmat20 workloads' reference arms"}), flush=True)
+        return
+    wl = BATCH_WORKLOADS.get(args.workload) or WORKLOADS[args.workload]
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    edges = O.gen_rmat(wl["scale"], wl["edge_factor"], RMAT["a"], RMAT["b"], RMAT["c"], wl["seed"])
+    gen_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    og = O.OracleGraph(edges, 1 << wl["scale"])
+    build_s = time.perf_counter() - t0
+    progs = oracle_programs(O, wl["programs"])
+    # a bounded per-step sample: about one second of CPU per step
+    n = 1 << 8
+    while True:
+        t0 = time.perf_counter()
+        for _, p, kind in progs:
+            O.run(og, p, n, 0, 5, kind, threads)
+        dt = time.perf_counter() - t0
+        if dt > 0.5 or n >= wl["samples"]:
+            break
+        n *= 2
+    for i in range(args.warmup):
+        for j, (_, p, kind) in enumerate(progs):
+            O.run(og, p, n, i * n, 5 + j, kind, threads)
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        for j, (_, p, kind) in enumerate(progs):
+            O.run(og, p, n, (args.warmup + i) * n, 5 + j, kind, threads)
+    dt = time.perf_counter() - t0
+    value = len(progs) * n * args.steps / dt
+    sample = ("%d samples of each of %d programs per step (bounded sample of the 2^%d per program), "
+              "oracle/zg_oracle.c on %d host threads; graph generated on the host in %.1f s, oracle graph built in %.1f s"
+              % (n, len(progs), wl["samples"].bit_length() - 1, threads, gen_s, build_s))
+    line = {"metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dt * 1000 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int64/f64", "data": "synthetic (seeded R-MAT)",
+            "impl": "reference", "config": workload_config(args.workload, len(edges)),
+            "cpu_baseline": {"value": value, "unit": "samples/s", "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---- GPU side ---------------------------------------------------------------------------------
+def make_program(Z, name):
+    if name in PATTERNS:
+        return Z.Program(Z.PROG_PATTERN, pattern=PATTERNS[name])
+    return Z.Program(PROG_IDS[name])
+
+
+def touch_bytes(Z, g, progs, names, seed, n=1 << 20):
+    """Bytes per sample each production sampling kernel moves (zg_touch_sectors on n samples)."""
+    return {name: p.touch_bytes_per_sample(g, n, seed) for name, p in zip(names, progs)}
+
+
+def time_to_bound(Z, g, names, exact, eps=0.01, conf=0.95, cap=1 << 37, seed=31):
     """Time from query submission (graph resident) to an answer whose empirical 95 % half-width is
-    <= 1 % of the estimate: plain ErrorProfile sizing vs the learned network, same bound check (zg_query).
-    For 4-cliques the unbiased canonical-path program runs: the reference's estimator is biased (it
-    finds ~60 % of the cliques), so a tight interval around it is not an accuracy claim."""
+    <= 1 % of the estimate: plain ErrorProfile sizing vs the learned network, the same bound check.
+    4-cliques run the unbiased canonical-path program: the reference's estimator finds ~60 % of the
+    cliques, so a tight interval around it is not an accuracy claim."""
     import elp_learn as EL
     model = os.path.join(ROOT, "sampling-graph-mining_gb300", "elp_mlp.npz")
     if not os.path.exists(model):
@@ -184,67 +301,36 @@ def time_to_bound(Z, g, names, acc, eps=0.01, conf=0.95, cap=1 << 37, coverage_q
     out = {"eps": eps, "confidence": conf, "max_samples": cap, "model": "sampling-graph-mining_gb300/elp_mlp.npz",
            "patterns": {}}
     for name in names:
-        prog_name = "four_clique_unbiased" if name == "four_clique" else name
-        r = EL.compare(net, g, prog_name, eps=eps, conf=conf, seed=31, max_samples=cap)
-        ex = acc[name]["exact"]
+        r = EL.compare(net, g, name, eps=eps, conf=conf, seed=seed, max_samples=cap)
+        ex = exact.get(name)
         for k in ("plain", "learned"):
-            r[k]["rel_err_vs_exact"] = abs(r[k]["estimate"] - ex) / ex
+            r[k]["rel_err_vs_exact"] = abs(r[k]["estimate"] - ex) / ex if ex else None
+        r["exact"] = ex
         r["speedup_learned_over_plain"] = r["plain"]["seconds"] / r["learned"]["seconds"]
-        out["patterns"][prog_name] = r
-    # delivered accuracy: triangle queries over independent seeds, learned sizing + bound check
-    prog = Z.Program(1)
-    ex = acc["triangle"]["exact"] if "triangle" in acc else g.exact_count(1)
-    inside, met = 0, 0
-    for s in range(coverage_queries):
-        q = Z.learned_query(net, g, prog, eps, conf, 1000 + s, 5000 + s, stream_id=0x60 + s, max_samples=cap)[0]
-        met += q.bound_met
-        inside += abs(q.estimate - ex) <= eps * ex
-    out["coverage"] = {"pattern": "triangle", "queries": coverage_queries, "bound_met": met,
-                       "within_1pct_of_exact": inside}
+        out["patterns"][name] = r
     return out
 
 
-def run_reference(args):
-    rank, world, _ = dist_env()
-    if rank != 0:
-        return
-    wl = WORKLOADS[args.workload]
-    import zgraph as Z
-    edges, nv = make_graph(Z, wl)
-    threads = os.cpu_count() or 1
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle as O
-    og = O.OracleGraph(edges, nv)
-    progs = [(PROG_IDS[p], O.OracleProgram(PROG_IDS[p])) for p in wl["programs"]]
-    # calibrate a bounded per-step sample (about 1-2 s of CPU per step)
-    n = 1 << 12
-    while True:
-        t0 = time.perf_counter()
-        for pid, p in progs:
-            O.run(og, p, n, 0, 5, pid, threads)
-        dt = time.perf_counter() - t0
-        if dt > 0.5 or n >= wl["samples"]:
-            break
-        n *= 2
-    for i in range(args.warmup):
-        for pid, p in progs:
-            O.run(og, p, n, i * n, 5, pid, threads)
-    t0 = time.perf_counter()
-    for i in range(args.steps):
-        for pid, p in progs:
-            O.run(og, p, n, (args.warmup + i) * n, 5, pid, threads)
-    dt = time.perf_counter() - t0
-    value = len(progs) * n * args.steps / dt
-    line = {"metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": dt * 1000 / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "int64/f64", "data": "synthetic",
-            "impl": "reference",
-            "config": {"workload": "%s: R-MAT scale %d ef %d (%d edges), %s; bounded sample %d per pattern per step"
-                       % (args.workload, wl["scale"], wl["edge_factor"], len(edges), "+".join(wl["programs"]), n)},
-            "cpu_baseline": {"value": value, "unit": "samples/s", "cores": threads, "kind": "port",
-                             "sample": "%d samples x %d patterns per step, oracle/zg_oracle.c" % (n, len(progs))},
-            "e2e": {"value": value, "unit": "samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    print(json.dumps(line), flush=True)
+def coverage(Z, g, exact, names=("triangle", "four_clique_unbiased"), queries=40, eps=0.01, conf=0.95, cap=1 << 37):
+    """Delivered accuracy: independent queries (learned sizing + bound check), how many met their
+    bound and how many landed within eps of the exact count."""
+    model = os.path.join(ROOT, "sampling-graph-mining_gb300", "elp_mlp.npz")
+    if not os.path.exists(model):
+        return {"skipped": "no trained network at %s" % model}
+    net = Z.Mlp.load(model)
+    out = {}
+    for name in names:
+        prog = Z.Program(PROG_IDS[name])
+        ex = exact[name]
+        inside, met, samples, t0 = 0, 0, 0, time.perf_counter()
+        for s in range(queries):
+            q = Z.learned_query(net, g, prog, eps, conf, 1000 + s, 5000 + s, stream_id=0x60 + s, max_samples=cap)[0]
+            met += q.bound_met
+            inside += abs(q.estimate - ex) <= eps * ex
+            samples += q.samples
+        out[name] = {"queries": queries, "bound_met": met, "within_1pct_of_exact": inside, "exact": ex,
+                     "mean_samples": samples / queries, "seconds": time.perf_counter() - t0}
+    return out
 
 
 def run_gb300(args):
@@ -258,16 +344,15 @@ def run_gb300(args):
     Z.init(local)
     wl = WORKLOADS[args.workload]
     n = wl["samples"]
-    edges, nv = make_graph(Z, wl)
+    nv = 1 << wl["scale"]
     t0 = time.perf_counter()
-    g = Z.Graph.from_edges(edges, nv)
+    g = Z.Graph.gen_rmat(wl["scale"], wl["edge_factor"], RMAT["a"], RMAT["b"], RMAT["c"], wl["seed"])
     torch.cuda.synchronize()
     build_s = time.perf_counter() - t0
     names = wl["programs"]
-    progs = [Z.Program(PROG_IDS[p]) for p in names]
+    progs = [make_program(Z, p) for p in names]
     stream = torch.cuda.current_stream()
     sp = stream.cuda_stream
-    # autotuner: pick each program's launch shape on this graph (setup, untimed)
     tuning = {}
     fixed = dict(kv.split("=") for kv in args.variants.split(",")) if args.variants else None
     for name, p in zip(names, progs):
@@ -279,8 +364,7 @@ def run_gb300(args):
         best, ms = p.tune(g, 1 << 23, cuda_stream=sp)
         tuning[name] = {"variant": best, "min_blocks": p.variant()["min_blocks"], "grid": p.variant()["grid"],
                         "ms_per_variant_2^23": [round(x, 3) for x in ms]}
-    d_res = torch.zeros((len(progs), Z.ZG_RESULT_BYTES if hasattr(Z, "ZG_RESULT_BYTES") else 112),
-                        dtype=torch.uint8, device="cuda")
+    d_res = torch.zeros((len(progs), Z.RESULT_BYTES), dtype=torch.uint8, device="cuda")
     flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
     seed = 20250101
 
@@ -323,8 +407,7 @@ def run_gb300(args):
     if world > 1:  # exact merge of the ranks' shards (integer limbs, no floating reduction)
         res = [Z.allgather_counters(r) for r in res]
 
-    # end to end through the public API: calculate() per program, results read back each query
-    # (each rank its own Philox streams, so the ranks draw different samples)
+    # end to end through the public API: calculate() per program, each result read back
     insts = [getattr(Z, c)(g, seed=seed + 7, stream_id=16 * rank + j + 11) for j, c in
              enumerate({"triangle": "TriangleCountingInstance", "four_clique": "FourCliqueCountingInstance",
                         "three_chain": "ThreeChainCountingInstance",
@@ -343,65 +426,66 @@ def run_gb300(args):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         e2e_s = float(t.item())
     e2e = {"value": world * len(insts) * n * e2e_steps / e2e_s, "unit": "samples/s", "h2d_bytes_per_step": 0,
-           "d2h_bytes_per_step": len(insts) * 112}
+           "d2h_bytes_per_step": len(insts) * Z.RESULT_BYTES,
+           "note": "calculate() per program; the graph is resident and a query's inputs are scalars (no host "
+                   "buffer to copy in); each result (112 bytes) is read back"}
 
     if rank != 0:
         if world > 1:
             torch.distributed.destroy_process_group()
         return
-    # algorithmic bytes per sample: access model from the debug kernel (2^16 samples)
-    model, closures = {}, {}
-    for j, p in enumerate(progs):
-        tr = p.run_debug(g, 1 << 16, seed, stream_id=j + 1)
-        model[names[j]] = float(tr["sectors"].mean()) * 32.0
-        closures[names[j]] = float(tr["closures"].mean())  # conditional_close look-ups per sample
-    peak, peak_kind = peaks()
+    touched = touch_bytes(Z, g, progs, names, seed)
+    closures = {name: float(p.run_debug(g, 1 << 16, seed, stream_id=j + 1)["closures"].mean())
+                for j, (name, p) in enumerate(zip(names, progs))}
+    hbm, hbm_src = peaks()
+    l2_gbs = Z.read_bandwidth(48 << 20, 100)
+    layout = {1: "compact", 2: "wide", 3: "packed"}[g.meta().record_layout]
     kern = []
     for j, name in enumerate(names):
         t = per_prog[j] / args.steps / 1000.0
-        ach = model[name] * n / t / 1e9
-        kern.append({"kernel": "k_sample<%s>" % name, "ms": per_prog[j] / args.steps, "bytes_per_sample": model[name],
-                     "achieved_gbs": ach, "samples_per_s": n / t,
+        dram_ps, dram_src = profile_traffic("k_sample<%s>" % name, args.workload, layout)
+        kern.append({"kernel": "k_sample<%s>" % name, "ms": per_prog[j] / args.steps, "samples_per_s": n / t,
+                     "touched_bytes_per_sample": touched[name], "touched_gbs": touched[name] * n / t / 1e9,
+                     "dram_bytes_per_sample": dram_ps, "dram_source": dram_src,
+                     "dram_gbs": dram_ps * n / t / 1e9 if dram_ps else None,
                      "closure_checks_per_sample": closures[name], "closure_checks_per_s": closures[name] * n / t,
                      "hits": int(res[j].hits), "estimate": res[j].estimate})
     dom = max(kern, key=lambda k: k["ms"])
-    traffic = profile_traffic(n).get(dom["kernel"]) if args.workload == "rmat20" else None
-    l2_gbs = l2_read_gbs(Z)
-    # the DRAM bytes the kernel really moved (ncu, per launch) over its CUDA-event time: how close to
-    # the HBM roof it runs, next to the access-model view above
-    dram = {"gbs": traffic / (dom["ms"] / 1000.0) / 1e9, "frac": traffic / (dom["ms"] / 1000.0) / 1e9 / peak,
-            "source": "traffic (ncu dram__bytes_read + write per launch) / measured kernel time"} if traffic else None
-    roofline = {"bound": "hbm", "achieved": dom["achieved_gbs"], "peak": peak, "unit": "GB/s",
-                "frac": dom["achieved_gbs"] / peak, "traffic": traffic, "dram": dram, "kernel": dom["kernel"],
-                "l2": {"peak": l2_gbs, "frac": dom["achieved_gbs"] / l2_gbs if l2_gbs else None,
-                       "peak_source": "measured live: reads of a 48 MiB buffer resident in L2 (zg_read_bandwidth)"},
-                "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
+    # The graph's sampling working set is about the L2 size, so the bound is the L2 read bandwidth
+    # (measured live); the DRAM figure says how much of it came from HBM.
+    roofline = {"bound": "l2", "achieved": dom["touched_gbs"], "peak": l2_gbs, "unit": "GB/s",
+                "frac": dom["touched_gbs"] / l2_gbs, "kernel": dom["kernel"],
+                "traffic": dom["dram_bytes_per_sample"] * n if dom["dram_bytes_per_sample"] else None,
+                "traffic_source": dom["dram_source"],
+                "algorithmic_bytes": "zg_touch_sectors: 32-byte sectors the kernel's loads touch, per sample x samples",
+                "peak_source": "measured live: reads of a 48 MiB buffer resident in L2 (zg_read_bandwidth)",
+                "hbm": {"peak": hbm, "peak_source": hbm_src,
+                        "dram_frac": dom["dram_gbs"] / hbm if dom["dram_gbs"] else None},
                 "per_kernel": kern}
-    # accuracy against the GPU exact counts
+    exact = {}
     acc = {}
     for j, name in enumerate(names):
         ex = g.exact_count(EXACT_IDS[name])
-        acc[name] = {"exact": ex, "estimate": res[j].estimate,
-                     "rel_err": abs(res[j].estimate - ex) / ex if ex else None}
-        if name == "four_clique":  # the reference's estimator is biased; the canonical-path one is not
-            u = Z.Program(Z.PROG_FOUR_CLIQUE_UNBIASED).run(g, n, seed, stream_id=j + 1)
-            acc["four_clique_unbiased"] = {"exact": ex, "estimate": u.estimate,
-                                           "rel_err": abs(u.estimate - ex) / ex if ex else None}
-    ttb = time_to_bound(Z, g, names, acc) if not args.no_time_to_bound else None
+        exact[name] = ex
+        acc[name] = {"exact": ex, "estimate": res[j].estimate, "rel_err": abs(res[j].estimate - ex) / ex if ex else None}
+    if "four_clique" in names:
+        exact["four_clique_unbiased"] = exact["four_clique"]
+    ttb = None
+    if not args.no_time_to_bound:
+        ttb = time_to_bound(Z, g, [x for x in ("triangle", "four_clique_unbiased") if x in exact], exact)
+        if not args.no_coverage:
+            ttb["coverage"] = coverage(Z, g, exact, names=[x for x in ("triangle", "four_clique_unbiased") if x in exact])
     line = {"metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int64/u192 exact (f64 reference 1/p)",
-            "data": "synthetic (seeded R-MAT, zg_gen_rmat)",
-            "config": {"workload": "%s: R-MAT scale %d, edge factor %d, a/b/c=.57/.19/.19, %d undirected edges; "
-                                   "%s x 2^%d samples per step" % (args.workload, wl["scale"], wl["edge_factor"],
-                                                                   len(edges), "+".join(names),
-                                                                   n.bit_length() - 1),
-                       "l2": "flushed between steps (512 MiB write)", "graph_build_s": round(build_s, 3),
-                       "graph_device_bytes": int(g.meta().device_bytes), "launch_tuning": tuning},
+            "data": "synthetic (seeded R-MAT, generated on the device)",
+            "config": workload_config(args.workload, g.num_local_edges),
+            "setup": {"graph_gen_and_build_s": round(build_s, 3), "graph_device_bytes": int(g.meta().device_bytes),
+                      "record_layout": layout, "launch_tuning": tuning},
             "e2e": e2e, "gpu_launches": 2 * len(progs) * args.steps, "clocks": clk, "roofline": roofline,
             "accuracy": acc, "time_to_bound": ttb}
     if not args.no_cpu_baseline and world == 1:
-        line["cpu_baseline"] = cpu_baseline(wl, edges, nv, os.cpu_count() or 1)
+        line["cpu_baseline"] = cpu_baseline(g.download_edges(), nv, names, os.cpu_count() or 1)
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -430,7 +514,7 @@ def batch_queries(Z, rng, nq):
 
 
 def run_batch(args):
-    """One step = one submit of the workload's queries (zg_batch: persistent kernel replayed through
+    """One step = one submit of the workload's queries (zg_batch: persistent kernels replayed through
     a CUDA graph).  value: samples/s from CUDA events around the graph launch; e2e: submit + wait
     wall time (descriptors in, counters out)."""
     import numpy as np
@@ -440,28 +524,37 @@ def run_batch(args):
     Z.init(0)
     torch.cuda.set_device(0)
     t0 = time.perf_counter()
-    if wl["gen"] == "chung_lu":
+    rmat = wl["gen"] == "rmat"
+    if not rmat:
         g = Z.Graph.gen_chung_lu(wl["n"], wl["exponent"], wl["avg_degree"], seed=wl["seed"],
                                  max_weight=wl["max_weight"], weight_seed=7)
         qs = batch_queries(Z, np.random.default_rng(3), wl["queries"])
-        desc = ("Chung-Lu %d vertices, exponent %.1f, %d edges, edge data in [0, 100); %d queries (%d batch "
-                "queries) over triangle / 3-motif / all-predicate / at-least-one-predicate, budgets 2^U(12,24)"
-                % (wl["n"], wl["exponent"], g.num_local_edges, wl["queries"], len(qs)))
+        nv = wl["n"]
+        config = {"workload": "%s: Chung-Lu %d vertices, exponent %.1f, %d edges, edge data in [0, 100); %d queries (%d "
+                              "batch queries) over triangle / 3-motif / all-predicate / at-least-one-predicate, budgets "
+                              "2^U(12,24)" % (args.workload, wl["n"], wl["exponent"], g.num_local_edges, wl["queries"],
+                                              len(qs)),
+                  "inputs": "graph built before the timed steps and kept resident (GPU arm: device memory, L2 flushed "
+                                           "between steps)"}
+        names = []
     else:
-        g = Z.Graph.gen_rmat(wl["scale"], wl["edge_factor"], seed=wl["seed"], sampling_only=True)
-        star = Z.Program(Z.PROG_PATTERN, pattern=(5, [(0, 1), (0, 2), (0, 3), (0, 4)]))
-        house = Z.Program(Z.PROG_PATTERN, pattern=(5, [(0, 1), (0, 2), (1, 2), (1, 3), (2, 4), (3, 4)]))
-        n = wl["samples"]
-        qs = [{"kind": Z.PROG_FOUR_CLIQUE, "n": n, "seed": 1},
-              {"kind": Z.PROG_PATTERN, "program": star, "n": n, "seed": 2},
-              {"kind": Z.PROG_PATTERN, "program": house, "n": n, "seed": 3}]
-        desc = ("R-MAT scale %d, edge factor %d, %d edges (built on the device); 4-clique, 5-star, 5-house x 2^%d"
-                % (wl["scale"], wl["edge_factor"], g.num_local_edges, n.bit_length() - 1))
+        g = Z.Graph.gen_rmat(wl["scale"], wl["edge_factor"], RMAT["a"], RMAT["b"], RMAT["c"], seed=wl["seed"],
+                             sampling_only=True)
+        nv = 1 << wl["scale"]
+        names = wl["programs"]
+        progs = {name: make_program(Z, name) for name in names}
+        qs = []
+        for j, name in enumerate(names):
+            q = {"kind": progs[name].kind, "n": wl["samples"], "seed": j + 1}
+            if name in PATTERNS:
+                q["program"] = progs[name]
+            qs.append(q)
+        config = workload_config(args.workload, g.num_local_edges)
     torch.cuda.synchronize()
     gen_s = time.perf_counter() - t0
     b = Z.Batch(g, max_queries=max(8, len(qs)), cache_bytes=200 << 30)
     t0 = time.perf_counter()
-    first = b.run(qs)  # builds the filtered graphs the predicates need
+    b.run(qs)  # builds the filtered graphs the predicates need
     first_s = time.perf_counter() - t0
     best, ms_variants = b.tune(qs)
     samples = sum(q["n"] for q in qs) + sum(q["n"] for q in qs if q["kind"] == Z.QUERY_THREE_MOTIF)
@@ -469,9 +562,11 @@ def run_batch(args):
         b.run(qs)
     st = torch.cuda.current_stream()
     flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    h2d, d2h = b.copy_bytes()
     clocks = ClockSampler(0)
     clocks.start()
     dev_ms, wall = [], []
+    res = None
     for _ in range(args.steps):
         flush.zero_()
         torch.cuda.synchronize()
@@ -483,45 +578,94 @@ def run_batch(args):
     clk = clocks.stop()
     total_ms = sum(dev_ms)
     value = samples * args.steps / (total_ms / 1000.0)
-    # algorithmic bytes: access-model sectors per sample of every (program, graph) pair, 2^14 samples
-    model_bytes, seen = 0.0, {}
-    for q in qs:
-        key = (q["kind"], q.get("pred_op", 0), q.get("t0", 0), id(q.get("program")))
-        if key not in seen:
-            gg = b.filtered_graph(q["pred_op"], q["t0"]) if q.get("pred_op") else g
-            if q["kind"] == Z.QUERY_THREE_MOTIF:
-                tc, tt = Z.run_three_motif_debug(gg, 1 << 14, 1 << 14, 5)[:2]
-                seen[key] = 32.0 * (float(tc["sectors"].mean()) + float(tt["sectors"].mean()))
-            else:
-                p = q.get("program") or Z.Program(q["kind"])
-                seen[key] = 32.0 * float(p.run_debug(gg, 1 << 14, 5)["sectors"].mean())
-        model_bytes += seen[key] * q["n"]
-    peak, peak_kind = peaks()
-    ach = model_bytes / (total_ms / args.steps / 1000.0) / 1e9
-    h2d = len(qs) * 72 + 8 * (Z.BATCH_MAX_CHUNKS + max(8, len(qs))) + 16
+    hbm, hbm_src = peaks()
+    layout = {1: "compact", 2: "wide", 3: "packed"}[g.meta().record_layout]
     line = {"metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int64/u192 exact", "data": "synthetic (device generator)",
-            "config": {"workload": "%s: %s" % (args.workload, desc), "queries_per_step": len(qs),
-                       "samples_per_step": samples, "graph_gen_and_build_s": round(gen_s, 3),
-                       "first_batch_s (builds filtered graphs)": round(first_s, 3),
-                       "batch_variant": best, "ms_per_variant": [round(x, 3) for x in ms_variants],
-                       "l2": "flushed between steps (512 MiB write)"},
+            "config": config,
+            "setup": {"graph_gen_and_build_s": round(gen_s, 3), "graph_device_bytes": int(g.meta().device_bytes),
+                      "record_layout": layout, "queries_per_step": len(qs), "samples_per_step": samples,
+                      "first_batch_s": round(first_s, 3), "batch_variant": best,
+                      "ms_per_variant": [round(x, 3) for x in ms_variants]},
             "e2e": {"value": samples * args.steps / sum(wall), "unit": "samples/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": 2 * 112 * max(8, len(qs)),
-                    "queries_per_s": len(qs) * args.steps / sum(wall)},
-            "gpu_launches": 3 * args.steps, "clocks": clk,
-            "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                         "traffic": None, "kernel": "k_batch (all queries of the step)",
-                         "peak_source": peak_kind}}
-    if wl["gen"] == "rmat":
-        line["results"] = {name: {"hits": int(c.hits), "estimate": c.estimate}
-                           for name, (c, _) in zip(["four_clique", "five_star", "five_house"], res)}
+                    "d2h_bytes_per_step": d2h, "queries_per_s": len(qs) * args.steps / sum(wall),
+                    "note": "zg_batch_submit + zg_batch_wait from host buffers: query descriptors and work list in, "
+                            "results out; the graph stays resident"},
+            "gpu_launches": 3 * args.steps, "clocks": clk}
+    if rmat:
+        # bytes the production kernels move per sample, and each program alone (CUDA events, k_sample)
+        touched = touch_bytes(Z, g, [progs[x] for x in names], names, 1)
+        step_bytes = sum(touched[x] * wl["samples"] for x in names)
+        achieved = step_bytes / (total_ms / args.steps / 1000.0) / 1e9
+        stream = torch.cuda.current_stream()
+        d_res = torch.zeros(Z.RESULT_BYTES, dtype=torch.uint8, device="cuda")
+        kern = []
+        for j, name in enumerate(names):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            flush.zero_()
+            e0.record(stream)
+            progs[name].run_async(g, wl["samples"], j + 1, d_res.data_ptr(), cuda_stream=stream.cuda_stream)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+            dram_ps, dram_src = profile_traffic("k_sample<%s>" % name, args.workload, layout)
+            kern.append({"kernel": "k_sample<%s> (the program alone)" % name, "ms": ms,
+                         "samples_per_s": wl["samples"] / (ms / 1000.0), "touched_bytes_per_sample": touched[name],
+                         "touched_gbs": touched[name] * wl["samples"] / (ms / 1000.0) / 1e9,
+                         "frac_of_hbm_peak": touched[name] * wl["samples"] / (ms / 1000.0) / 1e9 / hbm,
+                         "dram_bytes_per_sample": dram_ps, "dram_source": dram_src})
+        dram_ps, dram_src = profile_traffic("k_batch", args.workload, layout)
+        line["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                            "kernel": "k_batch + k_batch_pattern (the step's sampling kernels, one CUDA graph)",
+                            "traffic": dram_ps * samples if dram_ps else None, "traffic_source": dram_src,
+                            "algorithmic_bytes": "zg_touch_sectors: 32-byte sectors the production kernels' loads "
+                                                 "touch per sample (%s) x 2^30 samples per program"
+                                                 % {k: round(v, 1) for k, v in touched.items()},
+                            "peak_source": hbm_src, "per_kernel": kern}
+        line["results"] = {name: {"hits": int(c.hits), "estimate": c.estimate} for name, (c, _) in zip(names, res)}
         if not args.no_time_to_bound:
-            line["time_to_bound"] = large_time_to_bound(Z, g)
-    elif not args.no_time_to_bound:
-        line["learned_batch"] = learned_batch(Z, b, qs)
+            exact = {"triangle": None, "four_clique_unbiased": None}
+            line["time_to_bound"] = time_to_bound(Z, g, ["triangle", "four_clique_unbiased"], exact)
+            if not args.no_coverage:
+                line["time_to_bound"]["coverage"] = coverage_rmat20(Z)
+        if not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline(g.download_edges(), nv, names, os.cpu_count() or 1)
+    else:
+        # algorithmic bytes: the sectors every (program, graph) pair's production kernel touches
+        bytes_step, seen = 0.0, {}
+        for q in qs:
+            key = (q["kind"], q.get("pred_op", 0), q.get("t0", 0))
+            if key not in seen:
+                gg = b.filtered_graph(q["pred_op"], q["t0"]) if q.get("pred_op") else g
+                if q["kind"] == Z.QUERY_THREE_MOTIF:
+                    seen[key] = sum(Z.Program(k).touch_bytes_per_sample(gg, 1 << 16, 5) for k in (3, 1))
+                else:
+                    seen[key] = Z.Program(q["kind"]).touch_bytes_per_sample(gg, 1 << 16, 5)
+            bytes_step += seen[key] * q["n"]
+        ach = bytes_step / (total_ms / args.steps / 1000.0) / 1e9
+        dram_ps, dram_src = profile_traffic("k_batch", args.workload, layout)
+        line["roofline"] = {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+                            "kernel": "k_batch (all queries of the step)",
+                            "traffic": dram_ps * samples if dram_ps else None, "traffic_source": dram_src,
+                            "algorithmic_bytes": "zg_touch_sectors of each (program, graph) pair x its samples",
+                            "peak_source": hbm_src}
+        if not args.no_time_to_bound:
+            line["learned_batch"] = learned_batch(Z, b, qs)
     print(json.dumps(line), flush=True)
+
+
+def coverage_rmat20(Z):
+    """Coverage of the 1 %/95 % answers on R-MAT scale 20 (whose exact counts are cheap): triangle and
+    unbiased 4-clique, 40 seeds each, learned sizing + bound check."""
+    wl = WORKLOADS["rmat20"]
+    g = Z.Graph.gen_rmat(wl["scale"], wl["edge_factor"], RMAT["a"], RMAT["b"], RMAT["c"], wl["seed"],
+                         sampling_only=False)
+    exact = {"triangle": g.exact_count(EXACT_IDS["triangle"]),
+             "four_clique_unbiased": g.exact_count(EXACT_IDS["four_clique"])}
+    out = coverage(Z, g, exact)
+    out["graph"] = "rmat20: R-MAT scale 20, edge factor 3, seed 1 (%d edges)" % g.num_local_edges
+    return out
 
 
 def learned_batch(Z, b, qs, eps=0.05, conf=0.95):
@@ -546,43 +690,12 @@ def learned_batch(Z, b, qs, eps=0.05, conf=0.95):
             "bound_met": sum(1 for i in sized_q if met[i])}
 
 
-def large_time_to_bound(Z, g, eps=0.01, conf=0.95, cap=1 << 37):
-    """Triangle and (unbiased) 4-clique queries to 1 % at 95 % on the largest graph: learned-ELP
-    budget, then the empirical-CLT bound check keeps sampling until the bound holds (or the cap)."""
-    import elp_learn as EL
-    model = os.path.join(ROOT, "sampling-graph-mining_gb300", "elp_mlp.npz")
-    if not os.path.exists(model):
-        return {"skipped": "no trained network at %s" % model}
-    net = Z.Mlp.load(model)
-    out = {"eps": eps, "confidence": conf, "max_samples": cap, "patterns": {}}
-    for name, kind, exact_kind in (("triangle", Z.PROG_TRIANGLE, Z.EXACT_TRIANGLE),
-                                   ("four_clique_unbiased", Z.PROG_FOUR_CLIQUE_UNBIASED, Z.EXACT_FOUR_CLIQUE)):
-        prog = Z.Program(kind)
-        t0 = time.perf_counter()
-        q, n = Z.learned_query(net, g, prog, eps, conf, 77, 4242, stream_id=0x71, max_samples=cap)
-        dt = time.perf_counter() - t0
-        r = {"n_sized": int(n), "samples": int(q.samples), "bound_met": int(q.bound_met),
-             "rel_half_width": q.rel_half_width, "estimate": q.estimate, "seconds": dt}
-        if name == "triangle":  # an exact count of the 1.57 G-edge graph's triangles is affordable
-            t1 = time.perf_counter()
-            ex = g.exact_count(exact_kind)
-            r["exact"] = ex
-            r["exact_count_seconds"] = time.perf_counter() - t1
-            r["rel_err_vs_exact"] = abs(q.estimate - ex) / ex
-        out["patterns"][name] = r
-    return out
-
-
 def main():
     args = parse()
-    if args.workload in BATCH_WORKLOADS:
-        if args.impl == "reference":
-            print(json.dumps({"impl": "reference", "unavailable": "the batched workloads have no CPU arm here: the "
-                              "reference runs one query at a time; see the rmat20 workload's reference arm"}))
-        else:
-            run_batch(args)
-    elif args.impl == "reference":
+    if args.impl == "reference":
         run_reference(args)
+    elif args.workload in BATCH_WORKLOADS:
+        run_batch(args)
     else:
         run_gb300(args)
 

@@ -58,6 +58,11 @@ extern "C" {
 #define ZG_EXACT_THREE_PATH   3  /* FourChain.cpp   (3-edge paths)  */
 #define ZG_EXACT_FIVE_STAR    4  /* FiveStar.cpp    (sum C(d,4))    */
 #define ZG_EXACT_FOUR_CLIQUE  5  /* FourClique.cpp                  */
+#define ZG_EXACT_FIVE_HOUSE   6  /* FiveHouse.cpp   (house subgraphs: a triangle on one side of a 4-cycle) */
+#define ZG_EXACT_FIVE_CHAIN   7  /* FiveChain.cpp   (4-edge paths)  */
+/* Predicate-weighted triangles, zg_exact_count_weighted (threshold T; the naive programs use 50): */
+#define ZG_EXACT_WEIGHTED_TRIANGLE      8  /* WeightedTriangleCounting.cpp: every edge's data >= T */
+#define ZG_EXACT_AT_LEAST_ONE_TRIANGLE  9  /* AtLeastOneWeightedTriangleCounting.cpp: some edge >= T */
 
 /* ---- edge predicates for GraphFilter (std::function<bool(VertexId)>) ------ */
 #define ZG_PRED_GE            1  /* w >= t0       (AllPredicateWeightedTriangle.cpp:101-103) */
@@ -304,8 +309,9 @@ int zg_batch_size_learned(zg_batch* b, const zg_mlp* net, zg_batch_query* querie
                           double error, double confidence, uint64_t pilot_samples, void* cuda_stream);
 /* The batch counterpart of zg_query_learned (no counterpart in the reference): learned sizing of
  * the queries without a sample count (zg_batch_size_learned), one batch, then further batches for
- * the answers whose empirical CLT half-width is still above error * estimate (at least 30 hits),
- * each topped up to what its observed variance needs (+10 %) on fresh sample indices and merged
+ * the answers whose half-width (as zg_query checks it: empirical CLT or Bernstein, with the base
+ * graph's weight range) is still above error * estimate, each topped up to what its observed
+ * variance needs (headroom 1 + 0.5 / sqrt(hits)) on fresh sample indices and merged
  * exactly (an answer equals one run over all its samples), for at most max_rounds batches (0: 4)
  * and max_samples per query (0: 2^40).  3-motif queries run their given budgets once.  out: two
  * zg_counters per query as zg_batch_wait; bound_met: one flag per query; *rounds_run may be NULL. */
@@ -314,6 +320,9 @@ int zg_batch_bounded(zg_batch* b, const zg_mlp* net, const zg_batch_query* queri
                      void* cuda_stream, zg_counters* out, uint32_t* bound_met, uint32_t* rounds_run);
 /* Device time of the last waited batch (CUDA events around its graph launch), in ms. */
 int zg_batch_elapsed_ms(const zg_batch* b, float* ms);
+/* Bytes one submit copies host -> device (header, query descriptors, work list) and one wait
+ * copies device -> host (the per-query results), for end-to-end accounting. */
+int zg_batch_copy_bytes(const zg_batch* b, uint64_t* h2d, uint64_t* d2h);
 /* The cached filtered graph of a predicate (built if missing): what a filtered query samples. */
 int zg_batch_filtered_graph(zg_batch* b, int pred_op, int64_t t0, int64_t t1, void* cuda_stream,
                             const zg_graph** out);
@@ -373,22 +382,41 @@ int zg_elp_plain(const zg_graph* g, const zg_program* p, int pred_op, int64_t t0
 int zg_time_profile(const zg_graph* g, const zg_program* p, uint32_t time_limit_ms, uint64_t seed,
                     uint32_t stream_id, void* cuda_stream, double* estimate, uint64_t* samples_used);
 
+#define ZG_BOUND_CLT        1  /* empirical CLT: z * sqrt(var / n), from 30 hits on          */
+#define ZG_BOUND_BERNSTEIN  2  /* empirical Bernstein: sqrt(2 var x / n) + 3 R x / n         */
 typedef struct zg_query_result {
   double   estimate;          /* exact mean over all samples taken */
-  double   half_width;        /* z * sqrt(var / n) at the requested confidence */
+  double   half_width;        /* the half-width of the bound below at the requested confidence */
   double   rel_half_width;
   uint64_t samples, hits;
   uint32_t bound_met, rounds;
   uint64_t n_sized;           /* the initial budget */
   double   ms_total;
+  uint32_t bound_method;      /* ZG_BOUND_CLT or ZG_BOUND_BERNSTEIN: the bound half_width is from */
+  uint32_t reserved;
+  double   weight_range;      /* R: the largest value one estimator can return on the graph */
 } zg_query_result;
-/* A bounded query (no counterpart in the reference, whose ErrorProfile::run trusts its bound):
- * run n_initial estimators, check the answer's empirical CLT half-width, and keep sampling
- * fresh estimators until half_width <= error * estimate with at least 30 hits, or max_samples
- * (0: 2^40) is reached (then bound_met = 0). */
+/* A bounded query (no counterpart in the reference, whose ErrorProfile::run trusts its bound; the
+ * stop rule of its sampling/IEStop.cpp is a CLT interval): run n_initial estimators and keep
+ * sampling fresh estimators until the running estimate's half-width at the requested confidence is
+ * <= error * estimate, or max_samples (0: 2^40) is reached (then bound_met = 0).  The half-width is
+ * the empirical CLT one, z * sqrt(var / n) (from 30 hits on), or the empirical Bernstein one
+ * (Audibert, Munos, Szepesvari 2009: for values in [0, R], with probability >= 1 - delta,
+ * |mean - mu| <= sqrt(2 var ln(3/delta) / n) + 3 R ln(3/delta) / n, var the empirical variance),
+ * whichever is smaller; below 30 hits only the Bernstein one.  R bounds one estimator's weight:
+ * m * prod over the conditional steps i = 1.. of min((i + 1) * max_degree, 2m) (x 3 for the
+ * 4-chain).  Each further round runs what the observed variance needs, with headroom
+ * 1 + 0.5 / sqrt(hits). */
 int zg_query(const zg_graph* g, const zg_program* p, double error, double confidence,
              uint64_t n_initial, uint64_t max_samples, uint64_t seed, uint32_t stream_id,
              void* cuda_stream, zg_query_result* out);
+/* The check zg_query applies to a running estimate (host arithmetic only, no device): mean and
+ * empirical (1/n) variance of n estimators with `hits` non-zero ones, each in [0, weight_range].
+ * *half_width gets the half-width at `confidence` (CLT from 30 hits on, or Bernstein, whichever is
+ * smaller; Bernstein alone below 30 hits), *method the bound it came from, *met whether
+ * half_width <= error * mean. */
+int zg_bound_half_width(double mean, double var, uint64_t n, uint64_t hits, double error, double confidence,
+                        double weight_range, double* half_width, uint32_t* method, uint32_t* met);
 
 /* ---- learned error-latency profile (no counterpart in the reference) ------------------- */
 /* A 16 -> 64 -> 64 (GELU) -> 2 MLP predicting, for a (graph, program) query, log2 of the
@@ -441,10 +469,24 @@ int zg_query_learned(const zg_mlp* net, const zg_graph* g, const zg_program* p, 
  * timed with CUDA events: below the 129 MB L2 it measures L2, well above it HBM.  The L2 view of
  * the roofline for graphs that nearly fit in L2 (no counterpart in the reference). */
 int zg_read_bandwidth(uint64_t bytes, uint32_t reps, void* cuda_stream, double* gbs);
+/* The bytes zg_run's sampling kernel moves (no counterpart in the reference): the same kernel,
+ * compiled a second time with every global load also counting the 32-byte sectors it spans (a
+ * sector equal to the thread's previous load's last sector is counted once), run on n estimators
+ * (sample indices [first_sample, first_sample + n), 1 <= n <= 2^32); *sectors gets the total over
+ * all threads.  sectors * 32 / n is the kernel's bytes per sample: the numerator of its roofline.
+ * Synchronous; allocates its per-block scratch. */
+int zg_touch_sectors(const zg_graph* g, const zg_program* p, uint64_t n, uint64_t first_sample, uint64_t seed,
+                     uint32_t stream_id, void* cuda_stream, uint64_t* sectors);
 
 /* ---- exact counts ---------------------------------------------------------- */
 /* out[0..1]: 128-bit little-endian count.  kind: ZG_EXACT_*. */
 int zg_exact_count(const zg_graph* g, int kind, void* cuda_stream, uint64_t out[2]);
+/* The predicate-weighted triangle counts of a graph with edge data (out as zg_exact_count):
+ * ZG_EXACT_WEIGHTED_TRIANGLE counts the triangles whose three edges all have data >= threshold
+ * (naive_implementation/WeightedTriangleCounting.cpp:46-75, threshold 50 there),
+ * ZG_EXACT_AT_LEAST_ONE_TRIANGLE those with at least one such edge
+ * (naive_implementation/AtLeastOneWeightedTriangleCounting.cpp). */
+int zg_exact_count_weighted(const zg_graph* g, int kind, uint32_t threshold, void* cuda_stream, uint64_t out[2]);
 
 /* ---- synthetic inputs (host) ------------------------------------------------ */
 /* The reference reads SNAP files prepared by datasets/toolkits/edgelist_to_biedgelist.cpp;

@@ -75,6 +75,7 @@ def lib():
             "zgo_calculate_bound": ([D, D, D, D, D, U64, U64], D),
             "zgo_regression_k": ([P, P, U32], D),
             "zgo_ext_inv_product": ([P, I32], D),
+            "zgo_gen_rmat": ([U32, U32, D, D, D, U64, U64, P, C.POINTER(C.c_uint64)], I32),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -190,6 +191,18 @@ def three_motif(graph, n_chain, n_tri, seed, stream_chain=0, stream_tri=1):
                                    C.byref(b), _p(tc), _p(tt))
     assert rc == 0
     return tc[:n_chain], tt[:n_tri], a, b
+
+
+def gen_rmat(scale, edge_factor, a=0.57, b=0.19, c=0.19, seed=1):
+    """Seeded R-MAT edge list built on the host (oracle/zgo_gen.c): the library's zg_gen_rmat
+    graph, edge for edge, without loading the GPU library.  Returns an (m, 2) uint32 array."""
+    cap = edge_factor << scale  # every draw kept: an upper bound on the edge count
+    out = np.empty((cap, 2), dtype=np.uint32)
+    m = C.c_uint64(0)
+    rc = lib().zgo_gen_rmat(scale, edge_factor, a, b, c, seed, cap, _p(out), C.byref(m))
+    if rc != 0:
+        raise ValueError("zgo_gen_rmat failed (%d)" % rc)
+    return out[:m.value]
 
 
 def draw(seed, stream, sample, d, lo, hi):

@@ -72,7 +72,9 @@ uint64_t zgo_sample_draw(uint64_t seed, uint32_t stream, uint64_t sample, uint32
 /* ------------------------------------------------------------------------- */
 /* Graph: CSRConstructor::construct_bitmap_assisted_csr without its shuffle
  * (src/Graph.cpp:255-311): two half-edges per edge, appended in edge-id order, so every
- * adjacency list is sorted by edge id (the asserts at :324-334). */
+ * adjacency list is sorted by edge id (the asserts at :324-334).
+ * Large graphs are built by several threads with the same result: thread t owns a range of
+ * vertices, scans every edge in id order and appends only the half-edges of its own vertices. */
 int zgo_graph_build(zgo_graph* g, uint32_t nv, uint64_t m, const uint32_t* edges,
                     const uint32_t* weights) {
   memset(g, 0, sizeof(*g));
@@ -88,33 +90,84 @@ int zgo_graph_build(zgo_graph* g, uint32_t nv, uint64_t m, const uint32_t* edges
     g->w = (uint32_t*)malloc(sizeof(uint32_t) * (m ? m : 1));
     g->adj_w = (uint32_t*)malloc(sizeof(uint32_t) * (m ? 2 * m : 1));
   }
+  if (!g->src || !g->dst || !g->off || !g->adj_nbr || !g->adj_eid || (weights && (!g->w || !g->adj_w)))
+    return ZG_ERR_OOM;
+  int nt = 1;
+#ifdef _OPENMP
+  if (m >= (1u << 20)) nt = omp_get_max_threads();
+#endif
+  int bad = 0;
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(nt) schedule(static) reduction(| : bad)
+#endif
   for (uint64_t e = 0; e < m; ++e) {
     uint32_t s = edges[2 * e], d = edges[2 * e + 1];
-    if (s >= nv || d >= nv || s == d) return ZG_ERR_INVALID_GRAPH; /* src/Graph.cpp:454 */
+    if (s >= nv || d >= nv || s == d) bad = 1; /* src/Graph.cpp:454 */
     g->src[e] = s;
     g->dst[e] = d;
     if (weights) g->w[e] = weights[e];
-    g->off[s + 1]++;
-    g->off[d + 1]++;
+  }
+  if (bad) return ZG_ERR_INVALID_GRAPH;
+  /* degrees: thread t counts the endpoints in its equal share of the vertex ids */
+#ifdef _OPENMP
+#pragma omp parallel num_threads(nt)
+#endif
+  {
+    int t = 0;
+#ifdef _OPENMP
+    t = omp_get_thread_num();
+#endif
+    uint32_t vlo = (uint32_t)((uint64_t)nv * t / nt), vhi = (uint32_t)((uint64_t)nv * (t + 1) / nt);
+    for (uint64_t e = 0; e < m; ++e) {
+      uint32_t s = g->src[e], d = g->dst[e];
+      if (s >= vlo && s < vhi) g->off[s + 1]++;
+      if (d >= vlo && d < vhi) g->off[d + 1]++;
+    }
   }
   for (uint32_t v = 1; v <= nv; ++v) g->off[v] += g->off[v - 1];
   uint64_t* cur = (uint64_t*)malloc(sizeof(uint64_t) * ((size_t)nv + 1));
+  uint32_t* cut = (uint32_t*)malloc(sizeof(uint32_t) * ((size_t)nt + 1));
+  if (!cur || !cut) { free(cur); free(cut); return ZG_ERR_OOM; }
   memcpy(cur, g->off, sizeof(uint64_t) * ((size_t)nv + 1));
-  uint64_t maxd = 0;
-  for (uint64_t e = 0; e < m; ++e) {
-    uint32_t s = g->src[e], d = g->dst[e];
-    uint64_t pos = cur[s]++;
-    g->adj_nbr[pos] = d; g->adj_eid[pos] = e;
-    if (weights) g->adj_w[pos] = weights[e];
-    pos = cur[d]++;
-    g->adj_nbr[pos] = s; g->adj_eid[pos] = e;
-    if (weights) g->adj_w[pos] = weights[e];
+  /* scatter: vertex ranges of about equal half-edge counts */
+  cut[0] = 0;
+  for (int t = 1; t < nt; ++t) {
+    uint64_t target = 2 * m / (uint64_t)nt * (uint64_t)t;
+    uint32_t lo = cut[t - 1], hi = nv;
+    while (lo < hi) { uint32_t mid = lo + (hi - lo) / 2; if (g->off[mid] < target) lo = mid + 1; else hi = mid; }
+    cut[t] = lo;
   }
+  cut[nt] = nv;
+#ifdef _OPENMP
+#pragma omp parallel num_threads(nt)
+#endif
+  {
+    int t = 0;
+#ifdef _OPENMP
+    t = omp_get_thread_num();
+#endif
+    uint32_t vlo = cut[t], vhi = cut[t + 1];
+    for (uint64_t e = 0; e < m; ++e) {
+      uint32_t s = g->src[e], d = g->dst[e];
+      if (s >= vlo && s < vhi) {
+        uint64_t pos = cur[s]++;
+        g->adj_nbr[pos] = d; g->adj_eid[pos] = e;
+        if (weights) g->adj_w[pos] = weights[e];
+      }
+      if (d >= vlo && d < vhi) {
+        uint64_t pos = cur[d]++;
+        g->adj_nbr[pos] = s; g->adj_eid[pos] = e;
+        if (weights) g->adj_w[pos] = weights[e];
+      }
+    }
+  }
+  uint64_t maxd = 0;
   for (uint32_t v = 0; v < nv; ++v) {
     uint64_t dv = g->off[v + 1] - g->off[v];
     if (dv > maxd) maxd = dv;
   }
   free(cur);
+  free(cut);
   g->max_degree = maxd; /* src/Graph.cpp:467-474 */
   return ZG_OK;
 }
@@ -1004,6 +1057,54 @@ int zgo_exact_naive(const zgo_graph* g, int kind, uint64_t out[2]) {
           }
         }
       break;
+    case ZG_EXACT_FIVE_HOUSE:
+      /* naive_implementation/FiveHouse.cpp:25-49,110-130: every triangle i < j < k, and for each of
+       * its edges (left, right) with the third vertex `other`, the pairs (x, y), x a neighbour of
+       * left and y one of right, both outside the triangle, x != y, joined by an edge */
+      for (uint32_t i = 0; i < V; ++i)
+        for (uint64_t a = off[i]; a < off[i + 1]; ++a) {
+          uint32_t j = nb[a];
+          if (j <= i) continue;
+          for (uint64_t b = off[j]; b < off[j + 1]; ++b) {
+            uint32_t k = nb[b];
+            if (k <= j || !has_edge(g, k, i)) continue;
+            const uint32_t tri[3][3] = {{i, j, k}, {i, k, j}, {j, k, i}};
+            for (int r = 0; r < 3; ++r) {
+              uint32_t l = tri[r][0], rt = tri[r][1], o = tri[r][2];
+              for (uint64_t x = off[l]; x < off[l + 1]; ++x) {
+                uint32_t vl = nb[x];
+                if (vl == l || vl == rt || vl == o) continue;
+                for (uint64_t y = off[rt]; y < off[rt + 1]; ++y) {
+                  uint32_t vr = nb[y];
+                  if (vr == l || vr == rt || vr == o || vr == vl) continue;
+                  if (has_edge(g, vr, vl)) cnt++;
+                }
+              }
+            }
+          }
+        }
+      break;
+    case ZG_EXACT_FIVE_CHAIN:
+      /* naive_implementation/FiveChain.cpp:44-72: walks v0-v1-v2-v3-v4 with v2 != v0,
+       * v3 not in {v0, v1}, v4 not in {v0, v1, v2}; each path is walked from both ends */
+      for (uint32_t v0 = 0; v0 < V; ++v0)
+        for (uint64_t a = off[v0]; a < off[v0 + 1]; ++a) {
+          uint32_t v1 = nb[a];
+          for (uint64_t b = off[v1]; b < off[v1 + 1]; ++b) {
+            uint32_t v2 = nb[b];
+            if (v2 == v0) continue;
+            for (uint64_t c = off[v2]; c < off[v2 + 1]; ++c) {
+              uint32_t v3 = nb[c];
+              if (v3 == v0 || v3 == v1) continue;
+              for (uint64_t d = off[v3]; d < off[v3 + 1]; ++d) {
+                uint32_t v4 = nb[d];
+                if (v4 != v0 && v4 != v1 && v4 != v2) cnt++;
+              }
+            }
+          }
+        }
+      cnt /= 2;
+      break;
     default:
       return ZG_ERR_INVALID_ARG;
   }
@@ -1016,55 +1117,161 @@ static int cmp_u32(const void* a, const void* b) {
   return x < y ? -1 : (x > y);
 }
 
-/* Faster restatements: sorted neighbour lists, merge intersections. */
+/* Faster restatements: sorted neighbour lists, merge intersections; vertices split over the
+ * OpenMP threads, per-thread 128-bit partial sums added in thread order. */
+static uint64_t merge_count(const uint32_t* s, uint64_t i, uint64_t ie, uint64_t j, uint64_t je) {
+  uint64_t c = 0;
+  while (i < ie && j < je) {
+    if (s[i] < s[j]) ++i;
+    else if (s[i] > s[j]) ++j;
+    else { ++c; ++i; ++j; }
+  }
+  return c;
+}
+
+/* Houses and 4-edge paths from per-edge counts (the identities the GPU counter uses, checked here
+ * against the naive walks above): with t(e) the triangles and c4(e) the 4-cycles through edge
+ * e = (a, b), c4(a, b) = sum over x in N(a) \ {b} of (|N(x) ∩ N(b)| - 1),
+ *   houses      = sum_e t(e) c4(e) - 2 sum_e t(e)^2 + 6 T
+ *   4-edge paths = (sum_v (S1(v)^2 - S2(v)) + 2 sum_e t(e) (3 - d_a - d_b) - 2 sum_e c4(e)) / 2
+ * with S1(v) = sum over w in N(v) of (d_w - 1) and S2(v) the sum of the squares. */
+static int exact_house_chain(const zgo_graph* g, int kind, const uint32_t* s, uint64_t out[2]) {
+  typedef __int128 i128;
+  const uint64_t* off = g->off;
+  uint32_t V = g->nv;
+  int nt = 1;
+#ifdef _OPENMP
+  nt = omp_get_max_threads();
+#endif
+  i128* part = (i128*)calloc((size_t)nt, sizeof(i128));
+  if (!part) return ZG_ERR_OOM;
+#ifdef _OPENMP
+#pragma omp parallel num_threads(nt)
+#endif
+  {
+    int t = 0;
+#ifdef _OPENMP
+    t = omp_get_thread_num();
+#endif
+    i128 acc = 0;
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 64)
+#endif
+    for (uint32_t a = 0; a < V; ++a) {
+      uint64_t da = off[a + 1] - off[a];
+      if (kind == ZG_EXACT_FIVE_CHAIN) {
+        i128 s1 = 0, s2 = 0;
+        for (uint64_t p = off[a]; p < off[a + 1]; ++p) {
+          i128 dw = (i128)(off[s[p] + 1] - off[s[p]]) - 1;
+          s1 += dw;
+          s2 += dw * dw;
+        }
+        acc += s1 * s1 - s2;
+      }
+      for (uint64_t p = off[a]; p < off[a + 1]; ++p) {
+        uint32_t b = s[p];
+        if (b <= a) continue; /* each undirected edge once */
+        uint64_t db = off[b + 1] - off[b];
+        i128 te = (i128)merge_count(s, off[a], off[a + 1], off[b], off[b + 1]);
+        if (kind == ZG_EXACT_FIVE_HOUSE && te == 0) continue;
+        i128 c4 = 0;
+        for (uint64_t q = off[a]; q < off[a + 1]; ++q) {
+          uint32_t x = s[q];
+          if (x == b) continue;
+          c4 += (i128)merge_count(s, off[x], off[x + 1], off[b], off[b + 1]) - 1;
+        }
+        if (kind == ZG_EXACT_FIVE_HOUSE)
+          acc += te * c4 - 2 * te * te + 2 * te; /* 6 T = 2 sum_e t(e) */
+        else
+          acc += 2 * te * (3 - (i128)da - (i128)db) - 2 * c4;
+      }
+    }
+    part[t] = acc;
+  }
+  i128 tot = 0;
+  for (int t = 0; t < nt; ++t) tot += part[t];
+  free(part);
+  if (kind == ZG_EXACT_FIVE_CHAIN) tot /= 2;
+  put128(out, (u128)tot);
+  return ZG_OK;
+}
+
 int zgo_exact_fast(const zgo_graph* g, int kind, uint64_t out[2]) {
   uint32_t V = g->nv;
   const uint64_t* off = g->off;
+  if (kind == ZG_EXACT_WEDGE || kind == ZG_EXACT_FIVE_STAR) return zgo_exact_naive(g, kind, out);
   uint32_t* s = (uint32_t*)malloc(sizeof(uint32_t) * (g->m ? 2 * g->m : 1));
+  if (!s) return ZG_ERR_OOM;
   memcpy(s, g->adj_nbr, sizeof(uint32_t) * 2 * g->m);
+  int nt = 1;
+#ifdef _OPENMP
+  nt = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 256) num_threads(nt)
+#endif
   for (uint32_t v = 0; v < V; ++v) qsort(s + off[v], off[v + 1] - off[v], sizeof(uint32_t), cmp_u32);
-  u128 cnt = 0;
-  if (kind == ZG_EXACT_WEDGE || kind == ZG_EXACT_FIVE_STAR) {
+  if (kind == ZG_EXACT_FIVE_HOUSE || kind == ZG_EXACT_FIVE_CHAIN) {
+    int rc = exact_house_chain(g, kind, s, out);
     free(s);
-    return zgo_exact_naive(g, kind, out);
+    return rc;
   }
-  /* triangles per edge (u<v): |N(u) ∩ N(v)| */
-  u128 tri3 = 0, paths = 0;
-  for (uint32_t u = 0; u < V; ++u)
-    for (uint64_t a = off[u]; a < off[u + 1]; ++a) {
-      uint32_t v = s[a];
-      if (v <= u) continue;
-      uint64_t du = off[u + 1] - off[u], dv = off[v + 1] - off[v];
-      paths += (u128)(du - 1) * (dv - 1);
-      if (kind == ZG_EXACT_THREE_PATH || kind == ZG_EXACT_TRIANGLE) {
-        uint64_t i = off[u], j = off[v];
-        while (i < off[u + 1] && j < off[v + 1]) {
-          if (s[i] < s[j]) ++i;
-          else if (s[i] > s[j]) ++j;
-          else { if (kind == ZG_EXACT_TRIANGLE) { if (s[i] > v) tri3++; } else tri3++; ++i; ++j; }
-        }
-      } else if (kind == ZG_EXACT_FOUR_CLIQUE) {
-        /* common neighbours w > v, then pairs (w,x) with w<x both common and adjacent */
-        uint32_t* com = (uint32_t*)malloc(sizeof(uint32_t) * (du < dv ? du : dv) + 4);
-        uint64_t nc = 0, i = off[u], j = off[v];
-        while (i < off[u + 1] && j < off[v + 1]) {
-          if (s[i] < s[j]) ++i;
-          else if (s[i] > s[j]) ++j;
-          else { if (s[i] > v) com[nc++] = s[i]; ++i; ++j; }
-        }
-        for (uint64_t x = 0; x < nc; ++x) {
-          uint32_t w = com[x];
-          /* count com[y] (y > x) adjacent to w: merge N(w) with com[x+1..] */
-          uint64_t p = off[w], q = x + 1;
-          while (p < off[w + 1] && q < nc) {
-            if (s[p] < com[q]) ++p;
-            else if (s[p] > com[q]) ++q;
-            else { cnt++; ++p; ++q; }
+  u128* part = (u128*)calloc((size_t)nt * 3, sizeof(u128)); /* tri3, paths, cliques per thread */
+  if (!part) { free(s); return ZG_ERR_OOM; }
+#ifdef _OPENMP
+#pragma omp parallel num_threads(nt)
+#endif
+  {
+    int t = 0;
+#ifdef _OPENMP
+    t = omp_get_thread_num();
+#endif
+    u128 tri3 = 0, paths = 0, cnt = 0;
+    uint32_t* com = NULL;
+    uint64_t com_cap = 0;
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 64)
+#endif
+    for (uint32_t u = 0; u < V; ++u)
+      for (uint64_t a = off[u]; a < off[u + 1]; ++a) {
+        uint32_t v = s[a];
+        if (v <= u) continue;
+        uint64_t du = off[u + 1] - off[u], dv = off[v + 1] - off[v];
+        paths += (u128)(du - 1) * (dv - 1);
+        if (kind == ZG_EXACT_THREE_PATH || kind == ZG_EXACT_TRIANGLE) {
+          /* triangles per edge (u<v): |N(u) ∩ N(v)| */
+          uint64_t i = off[u], j = off[v];
+          while (i < off[u + 1] && j < off[v + 1]) {
+            if (s[i] < s[j]) ++i;
+            else if (s[i] > s[j]) ++j;
+            else { if (kind == ZG_EXACT_TRIANGLE) { if (s[i] > v) tri3++; } else tri3++; ++i; ++j; }
+          }
+        } else if (kind == ZG_EXACT_FOUR_CLIQUE) {
+          /* common neighbours w > v, then pairs (w,x) with w<x both common and adjacent */
+          uint64_t need = (du < dv ? du : dv) + 4;
+          if (need > com_cap) { free(com); com_cap = need; com = (uint32_t*)malloc(sizeof(uint32_t) * com_cap); }
+          uint64_t nc = 0, i = off[u], j = off[v];
+          while (i < off[u + 1] && j < off[v + 1]) {
+            if (s[i] < s[j]) ++i;
+            else if (s[i] > s[j]) ++j;
+            else { if (s[i] > v) com[nc++] = s[i]; ++i; ++j; }
+          }
+          for (uint64_t x = 0; x < nc; ++x) {
+            uint32_t w = com[x];
+            /* count com[y] (y > x) adjacent to w: merge N(w) with com[x+1..] */
+            uint64_t p = off[w], q = x + 1;
+            while (p < off[w + 1] && q < nc) {
+              if (s[p] < com[q]) ++p;
+              else if (s[p] > com[q]) ++q;
+              else { cnt++; ++p; ++q; }
+            }
           }
         }
-        free(com);
       }
-    }
+    free(com);
+    part[3 * t] = tri3; part[3 * t + 1] = paths; part[3 * t + 2] = cnt;
+  }
+  u128 tri3 = 0, paths = 0, cnt = 0;
+  for (int t = 0; t < nt; ++t) { tri3 += part[3 * t]; paths += part[3 * t + 1]; cnt += part[3 * t + 2]; }
+  free(part);
   if (kind == ZG_EXACT_TRIANGLE) cnt = tri3;
   else if (kind == ZG_EXACT_THREE_PATH) cnt = paths - tri3; /* tri3 here = 3 * triangles */
   free(s);

@@ -104,6 +104,11 @@ double zgo_calculate_bound(double epsilon, double delta, double nse, double ncse
 /* UnbiasedLinearRegression::solve (src/Regression.cpp:17-28), long double as the reference. */
 double zgo_regression_k(const double* x, const double* y, uint32_t len);
 
+/* Seeded R-MAT edge list on the host (oracle/zgo_gen.c), edge for edge the library's
+ * zg_gen_rmat output: the CPU arm's input.  edges == NULL only reports *m_out. */
+int zgo_gen_rmat(uint32_t scale, uint32_t edge_factor, double a, double b, double c, uint64_t seed,
+                 uint64_t capacity, uint32_t* edges, uint64_t* m_out);
+
 /* x87 80-bit extended arithmetic restated in integers (used by ChainMining's long double p). */
 double zgo_ext_inv_product(const double* factors, int n);
 

@@ -66,7 +66,7 @@ cudaError_t zg_malloc_async(void** p, size_t bytes, cudaStream_t s) {
   return cudaMallocFromPoolAsync(p, bytes, pool, s);
 }
 
-extern "C" int zg_version(void) { return 2; }
+extern "C" int zg_version(void) { return 3; }
 
 extern "C" const char* zg_last_error(void) { return g_err; }
 

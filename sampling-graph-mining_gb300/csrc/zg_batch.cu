@@ -687,7 +687,7 @@ extern "C" int zg_batch_bounded(zg_batch* b, const zg_mlp* net, const zg_batch_q
   std::vector<zg_batch_query> sized(q, q + nq);
   int rc = zg_batch_size_learned(b, net, sized.data(), nq, error, confidence, 0, cuda_stream);
   if (rc) return rc;
-  const double z = zg_normal_quantile(1.0 - (1.0 - confidence) / 2.0);
+  const cudaStream_t s = (cudaStream_t)cuda_stream;
   std::vector<uint64_t> ran(nq, 0), want(nq);
   std::vector<uint32_t> pending;
   for (uint32_t i = 0; i < nq; ++i) {
@@ -724,19 +724,20 @@ extern "C" int zg_batch_bounded(zg_batch* b, const zg_mlp* net, const zg_batch_q
       else merge_into(out[2 * i], res[2 * j]);
       ran[i] += want[i];
       const zg_counters& t = out[2 * i];
-      double need;
-      if (t.hits >= 30 && t.estimate > 0) {
-        const double n = (double)t.samples;
-        double var = t.sum_w2 / n - t.estimate * t.estimate;
-        if (var < 0) var = 0;
-        if (z * sqrt(var / n) <= error * t.estimate) {
-          bound_met[i] = 1;
-          continue;
-        }
-        need = z * z * var / (error * error * t.estimate * t.estimate) * 1.1;
-      } else {
-        need = 2.0 * (double)ran[i];
+      const double n = (double)t.samples;
+      double var = n > 0 ? t.sum_w2 / n - t.estimate * t.estimate : 0.0;
+      if (var < 0) var = 0;
+      // a filtered graph's estimators are bounded by the base graph's range (fewer edges, lower degrees)
+      double range = 0, half = 0;
+      uint32_t method = 0;
+      if ((rc = zg_weight_range(b->base, sized[i].kind, sized[i].param,
+                                sized[i].program ? sized[i].program->pe : 0, s, &range)))
+        return rc;
+      if (zg_bound_check(t.estimate, var, t.samples, t.hits, error, confidence, range, &half, &method)) {
+        bound_met[i] = 1;
+        continue;
       }
+      const double need = zg_samples_needed(t.estimate, var, t.samples, t.hits, error, confidence);
       if (ran[i] >= max_samples) continue;
       const double cap = (double)max_samples;
       const uint64_t target = (uint64_t)(need < cap ? need : cap);
@@ -790,5 +791,12 @@ extern "C" int zg_batch_tune(zg_batch* b, const zg_batch_query* q, uint32_t nq, 
 extern "C" int zg_batch_elapsed_ms(const zg_batch* b, float* ms) {
   if (!b || !ms) return zg_set_error(ZG_ERR_INVALID_ARG, "zg_batch_elapsed_ms: null argument"), ZG_ERR_INVALID_ARG;
   *ms = b->last_ms;
+  return ZG_OK;
+}
+
+extern "C" int zg_batch_copy_bytes(const zg_batch* b, uint64_t* h2d, uint64_t* d2h) {
+  if (!b || !h2d || !d2h) return zg_set_error(ZG_ERR_INVALID_ARG, "zg_batch_copy_bytes: null argument"), ZG_ERR_INVALID_ARG;
+  *h2d = sizeof(BatchHeader) + sizeof(BatchQuery) * (uint64_t)b->max_queries + sizeof(BatchWork) * (uint64_t)b->max_work;
+  *d2h = sizeof(ZgPartial) * 2 * (uint64_t)b->max_queries;
   return ZG_OK;
 }

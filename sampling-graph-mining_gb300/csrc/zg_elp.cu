@@ -234,6 +234,60 @@ extern "C" int zg_time_profile(const zg_graph* g, const zg_program* p, uint32_t 
 // Bounded query: sample n_initial estimators (the sizing step's budget), then check the answer by
 // its CLT half-width z * sqrt(var / n) at `conf`; while it exceeds eps * estimate, extend with more
 // estimators (never reusing sample indices) sized from the current variance, up to max_samples.
+int zg_weight_range(const zg_graph* g, int kind, uint32_t param, uint32_t pattern_edges, cudaStream_t s,
+                    double* range) {
+  uint64_t dmax = 0;
+  int rc = zg_graph_max_degree(g, s, &dmax);
+  if (rc) return rc;
+  uint32_t steps;  // conditional_sample_edge calls after the first sample_edge
+  switch (kind) {
+    case ZG_PROG_TRIANGLE:
+    case ZG_PROG_THREE_CHAIN: steps = 1; break;
+    case ZG_PROG_FOUR_CLIQUE:
+    case ZG_PROG_FOUR_CLIQUE_UNBIASED:
+    case ZG_PROG_FOUR_CHAIN: steps = 2; break;
+    case ZG_PROG_CHAIN: steps = param >= 2 ? param - 2 : 0; break;
+    default: steps = pattern_edges ? pattern_edges - 1 : 0; break;
+  }
+  const double m = (double)g->d.m;
+  double r = (kind == ZG_PROG_FOUR_CHAIN ? 3.0 : 1.0) * m;
+  for (uint32_t i = 1; i <= steps; ++i) r *= std::min((double)(i + 1) * (double)dmax, 2.0 * m);
+  *range = r;
+  return ZG_OK;
+}
+
+bool zg_bound_check(double mean, double var, uint64_t n, uint64_t hits, double eps, double conf, double range,
+                    double* half, uint32_t* method) {
+  const double z = normal_quantile(1.0 - (1.0 - conf) / 2.0);
+  const double x = log(3.0 / (1.0 - conf));
+  const double dn = (double)n;
+  const double bern = n ? sqrt(2.0 * var * x / dn) + 3.0 * range * x / dn : INFINITY;
+  const double clt = n ? z * sqrt(var / dn) : INFINITY;
+  if (hits >= 30 && clt <= bern) {
+    *half = clt;
+    *method = ZG_BOUND_CLT;
+  } else {
+    *half = bern;
+    *method = ZG_BOUND_BERNSTEIN;
+  }
+  return mean > 0 && *half <= eps * mean;
+}
+
+extern "C" int zg_bound_half_width(double mean, double var, uint64_t n, uint64_t hits, double error, double confidence,
+                                   double weight_range, double* half_width, uint32_t* method, uint32_t* met) {
+  if (!half_width || !method || !met || !(confidence > 0 && confidence < 1) || !(error > 0) || var < 0 ||
+      weight_range < 0)
+    return zg_set_error(ZG_ERR_INVALID_ARG, "zg_bound_half_width: invalid argument"), ZG_ERR_INVALID_ARG;
+  *met = zg_bound_check(mean, var, n, hits, error, confidence, weight_range, half_width, method) ? 1 : 0;
+  return ZG_OK;
+}
+
+double zg_samples_needed(double mean, double var, uint64_t n, uint64_t hits, double eps, double conf) {
+  if (hits < 30 || !(mean > 0)) return 2.0 * (double)n;
+  const double z = normal_quantile(1.0 - (1.0 - conf) / 2.0);
+  return z * z * var / (eps * eps * mean * mean) * (1.0 + 0.5 / sqrt((double)hits));
+}
+
 extern "C" int zg_query(const zg_graph* g, const zg_program* p, double eps, double conf, uint64_t n_initial,
                         uint64_t max_samples, uint64_t seed, uint32_t stream_id, void* cuda_stream,
                         zg_query_result* out) {
@@ -241,8 +295,11 @@ extern "C" int zg_query(const zg_graph* g, const zg_program* p, double eps, doub
   if (!(eps > 0) || !(conf > 0 && conf < 1))
     return zg_set_error(ZG_ERR_INVALID_ARG, "zg_query: error %g / confidence %g", eps, conf), ZG_ERR_INVALID_ARG;
   double tstart = now_ms();
-  const double z = normal_quantile(1.0 - (1.0 - conf) / 2.0);
   memset(out, 0, sizeof(*out));
+  double range = 0;
+  int rc = zg_weight_range(g, p->kind, p->param, p->pe, (cudaStream_t)cuda_stream, &range);
+  if (rc) return rc;
+  out->weight_range = range;
   uint64_t n_total = 0, hits = 0;
   uint64_t sum[5] = {0, 0, 0, 0, 0};
   uint32_t den = 0;
@@ -253,7 +310,7 @@ extern "C" int zg_query(const zg_graph* g, const zg_program* p, double eps, doub
     next = std::min(next, max_samples - n_total);
     if (next == 0) break;
     zg_counters c;
-    int rc = zg_run(g, p, next, n_total, seed, stream_id, cuda_stream, &c);
+    rc = zg_run(g, p, next, n_total, seed, stream_id, cuda_stream, &c);
     if (rc) return rc;
     den = c.den_log2;
     unsigned __int128 carry = 0;
@@ -270,18 +327,20 @@ extern "C" int zg_query(const zg_graph* g, const zg_program* p, double eps, doub
     double mean = zg_exact_mean_host(sum, den, n_total);
     double var = sw2 / (double)n_total - mean * mean;
     if (var < 0) var = 0;
-    double half = z * sqrt(var / (double)n_total);
+    double half = INFINITY;
+    uint32_t method = 0;
+    const bool met = zg_bound_check(mean, var, n_total, hits, eps, conf, range, &half, &method);
     out->estimate = mean;
     out->half_width = half;
     out->rel_half_width = mean > 0 ? half / mean : INFINITY;
+    out->bound_method = method;
     out->samples = n_total;
     out->hits = hits;
-    if (hits >= 30 && mean > 0 && half <= eps * mean) {
+    if (met) {
       out->bound_met = 1;
       break;
     }
-    // samples needed at the current variance, with 10 % headroom; at least double when unknown
-    double need = (hits >= 30 && mean > 0) ? (z * z * var / (eps * eps * mean * mean)) * 1.1 : 2.0 * n_total;
+    double need = zg_samples_needed(mean, var, n_total, hits, eps, conf);
     uint64_t want = need > 1e15 ? (uint64_t)1e15 : (uint64_t)need;
     next = want > n_total ? want - n_total : n_total / 4 + 1;
   }

@@ -753,33 +753,40 @@ extern "C" int zg_graph_set_meta(zg_graph* g, uint64_t num_edges, uint64_t max_d
   return ZG_OK;
 }
 
+namespace {
+// Edge e0 + i's (src, dst) and suffix sizes out of its record, in any layout.
+__global__ void k_export_rec(ZgDevGraph g, uint64_t e0, uint64_t cnt, uint32_t* __restrict__ edges,
+                             uint32_t* __restrict__ suffix) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < cnt; i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint4 q = zg_rec_e(g, e0 + i);
+    if (edges) reinterpret_cast<uint2*>(edges)[i] = make_uint2(q.x, q.y);
+    if (suffix) reinterpret_cast<uint2*>(suffix)[i] = make_uint2(q.z, q.w);
+  }
+}
+}  // namespace
+
 extern "C" int zg_graph_download(const zg_graph* g, uint32_t* edges, uint32_t* weights, int64_t* offsets,
                                  uint32_t* adj_e, uint32_t* adj_n, uint32_t* suffix) {
   if (!g) return zg_set_error(ZG_ERR_INVALID_ARG, "null graph"), ZG_ERR_INVALID_ARG;
   uint64_t m = g->d.m;
   cudaError_t ce = cudaSuccess;
   if ((edges || suffix) && m) {
-    const uint64_t words = g->wide ? 8 : 4;  // 32-bit words per record
-    std::vector<uint32_t> rec(words * m);
-    ce = cudaMemcpy(rec.data(), g->rec, 4 * words * m, cudaMemcpyDeviceToHost);
-    if (ce != cudaSuccess) return zg_check_cuda(ce, "download rec");
-    for (uint64_t e = 0; e < m; ++e) {
-      uint32_t r[4], pos[2];
-      const uint32_t* x = &rec[words * e];
-      if (g->packed)
-        zg_unpack(g->d.pk_v, g->d.pk_s, g->d.pk_p, x[0] | ((uint64_t)x[1] << 32), x[2] | ((uint64_t)x[3] << 32), r[0],
-                  r[1], r[2], r[3], pos[0], pos[1]);
-      else
-        memcpy(r, x, sizeof(r));
-      if (edges) {
-        edges[2 * e] = r[0];
-        edges[2 * e + 1] = r[1];
-      }
-      if (suffix) {
-        suffix[2 * e] = r[2];
-        suffix[2 * e + 1] = r[3];
-      }
+    // unpacked on the device in chunks of at most 2^27 edges (1 GiB per array), then copied out
+    const uint64_t chunk = m < (1ull << 27) ? m : (1ull << 27);
+    uint32_t *d_e = nullptr, *d_s = nullptr;
+    if (edges) ce = cudaMalloc((void**)&d_e, 8 * chunk);
+    if (ce == cudaSuccess && suffix) ce = cudaMalloc((void**)&d_s, 8 * chunk);
+    for (uint64_t e0 = 0; ce == cudaSuccess && e0 < m; e0 += chunk) {
+      const uint64_t cnt = m - e0 < chunk ? m - e0 : chunk;
+      const int grid = (int)std::min<uint64_t>((cnt + 255) / 256, (uint64_t)zg_num_sms() * 16);
+      k_export_rec<<<grid, 256>>>(g->d, e0, cnt, d_e, d_s);
+      ce = cudaGetLastError();
+      if (ce == cudaSuccess && edges) ce = cudaMemcpy(edges + 2 * e0, d_e, 8 * cnt, cudaMemcpyDeviceToHost);
+      if (ce == cudaSuccess && suffix) ce = cudaMemcpy(suffix + 2 * e0, d_s, 8 * cnt, cudaMemcpyDeviceToHost);
     }
+    if (d_e) cudaFree(d_e);
+    if (d_s) cudaFree(d_s);
+    if (ce != cudaSuccess) return zg_check_cuda(ce, "download records");
   }
   if (weights && g->w && m) ce = cudaMemcpy(weights, g->w, 4 * m, cudaMemcpyDeviceToHost);
   if (ce == cudaSuccess && offsets)

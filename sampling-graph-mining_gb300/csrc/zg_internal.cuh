@@ -83,9 +83,49 @@ __host__ __device__ __forceinline__ void zg_unpack(uint32_t vb, uint32_t sb, uin
 }
 
 #ifdef __CUDACC__
+// Loads of the sampling programs go through ZG_LDG (read-only path) and, where a load is written
+// in inline PTX, name their address in ZG_NOTE_LOAD.  A translation unit that defines ZG_TOUCH
+// before including this header gets a copy of the programs that also counts, per thread, the
+// 32-byte sectors its loads touch (a sector equal to the thread's previous one is not counted
+// again): the bytes the kernel itself moves, the numerator of its roofline (zg_touch.cu).  Every
+// other translation unit compiles both as the plain load.
+#ifdef ZG_TOUCH
+struct ZgTouch {
+  unsigned long long last;  // the previous load's last sector
+  unsigned long long sectors;
+};
+// One slot per thread of a block of at most 256 threads (the touch kernels' block size).
+__device__ __forceinline__ ZgTouch& zg_touch_state() {
+  __shared__ ZgTouch slots[256];
+  return slots[threadIdx.x];
+}
+__device__ __forceinline__ void zg_touch_note(const void* p, uint32_t bytes) {
+  ZgTouch& t = zg_touch_state();
+  const unsigned long long a = (unsigned long long)p >> 5, b = ((unsigned long long)p + bytes - 1) >> 5;
+  t.sectors += b - a + 1 - (a == t.last ? 1 : 0);
+  t.last = b;
+}
+template <typename T>
+__device__ __forceinline__ T zg_touch_ldg(const T* p) {
+  zg_touch_note(p, sizeof(T));
+  return __ldg(p);
+}
+// The sectors of every thread of a launch, summed.
+__device__ unsigned long long zg_touch_total;
+#define ZG_LDG(p) zg_touch_ldg(p)
+#define ZG_NOTE_LOAD(p, bytes) zg_touch_note((p), (bytes))
+#define ZG_TOUCH_BEGIN() (zg_touch_state().last = ~0ull, zg_touch_state().sectors = 0)
+#define ZG_TOUCH_END() atomicAdd(&zg_touch_total, zg_touch_state().sectors)
+#else
+#define ZG_LDG(p) __ldg(p)
+#define ZG_NOTE_LOAD(p, bytes) ((void)0)
+#define ZG_TOUCH_BEGIN() ((void)0)
+#define ZG_TOUCH_END() ((void)0)
+#endif
+
 // A packed record of edge e: q = (src, dst, suf_src, suf_dst), pos = (pos_src, pos_dst).
 __device__ __forceinline__ void zg_rec_packed(const ZgDevGraph& g, uint64_t e, uint4& q, uint2& pos) {
-  const ulonglong2 w = __ldg(&((const ulonglong2*)g.rec)[e]);
+  const ulonglong2 w = ZG_LDG(&((const ulonglong2*)g.rec)[e]);
   zg_unpack(g.pk_v, g.pk_s, g.pk_p, w.x, w.y, q.x, q.y, q.z, q.w, pos.x, pos.y);
 }
 // (src, dst, suf_src, suf_dst) of edge e, in any layout.
@@ -96,7 +136,7 @@ __device__ __forceinline__ uint4 zg_rec_e(const ZgDevGraph& g, uint64_t e) {
     zg_rec_packed(g, e, q, pos);
     return q;
   }
-  return g.wide ? __ldg(&((const ZgRec*)g.rec)[e].e) : __ldg(&((const uint4*)g.rec)[e]);
+  return g.wide ? ZG_LDG(&((const ZgRec*)g.rec)[e].e) : ZG_LDG(&((const uint4*)g.rec)[e]);
 }
 #endif
 
@@ -344,3 +384,20 @@ cudaError_t zg_malloc_async(void** p, size_t bytes, cudaStream_t s);
 int zg_degree_features(const zg_graph* g, cudaStream_t s, float* f);
 void zg_query_features(const zg_program* p, const zg_counters& c, float* f);
 uint64_t zg_learned_n(float pred_log2_cv2, double error, double confidence);
+// The graph's largest degree (from its degree statistics, computed once per graph).
+int zg_graph_max_degree(const zg_graph* g, cudaStream_t s, uint64_t* out);
+
+// The bound check of a running estimate (zg_elp.cu), shared by zg_query and zg_batch_bounded.
+// weight_range: the largest value one estimator of (kind, param, pattern_edges) can return on g.
+int zg_weight_range(const zg_graph* g, int kind, uint32_t param, uint32_t pattern_edges, cudaStream_t s,
+                    double* range);
+// Whether mean +- half lies within error * mean at the confidence: the empirical CLT half-width
+// (z sqrt(var / n), used from 30 hits on) or the empirical Bernstein half-width
+// (sqrt(2 var x / n) + 3 range x / n, x = ln(3 / (1 - confidence)), valid for any n), whichever is
+// smaller where both apply.  var: the empirical (1/n) variance.  *method: ZG_BOUND_CLT or
+// ZG_BOUND_BERNSTEIN, the one that gave *half.
+bool zg_bound_check(double mean, double var, uint64_t n, uint64_t hits, double error, double confidence, double range,
+                    double* half, uint32_t* method);
+// Samples the bound check needs at the observed variance, with headroom 1 + 0.5 / sqrt(hits) for
+// the uncertainty of that variance (fewer hits, more headroom); 2n while hits < 30.
+double zg_samples_needed(double mean, double var, uint64_t n, uint64_t hits, double error, double confidence);

@@ -530,6 +530,13 @@ float lg2(double x) { return (float)log2(x > 1e-300 ? x : 1e-300); }
 constexpr uint64_t kPilotMin = 1ull << 16, kPilotMax = 1ull << 22;
 constexpr uint64_t kPilotHits = 8;
 
+int zg_graph_max_degree(const zg_graph* g, cudaStream_t s, uint64_t* out) {
+  int rc = deg_stats(g, s);
+  if (rc) return rc;
+  *out = (uint64_t)g->deg_stats[6];
+  return ZG_OK;
+}
+
 // The graph part of the features (f[0..7]; the rest zeroed).
 int zg_degree_features(const zg_graph* g, cudaStream_t s, float* f) {
   int rc = deg_stats(g, s);

@@ -22,8 +22,6 @@
 // Internal linkage: every translation unit that includes this header gets its own copy.
 namespace {
 
-#define ZG_LDG(p) __ldg(p)
-
 struct Ctx {
   uint64_t seed;
   uint64_t sample;
@@ -114,6 +112,7 @@ __device__ __forceinline__ uint32_t lb_eid(const uint2* __restrict__ adj, uint32
 // loads).  The build leaves 8 entries of slack after adj_e, so s < 2m never reads past it.
 __device__ __forceinline__ void ld_ids8(const uint2* adj, uint32_t s, uint32_t (&id)[8]) {
   unsigned long long a0, a1, a2, a3, b0, b1, b2, b3;
+  ZG_NOTE_LOAD(adj + s, 64);
   asm("ld.global.nc.v4.u64 {%0, %1, %2, %3}, [%4];" : "=l"(a0), "=l"(a1), "=l"(a2), "=l"(a3) : "l"(adj + s));
   asm("ld.global.nc.v4.u64 {%0, %1, %2, %3}, [%4];" : "=l"(b0), "=l"(b1), "=l"(b2), "=l"(b3) : "l"(adj + s + 4));
   id[0] = (uint32_t)(a0 >> 32);
@@ -182,12 +181,14 @@ __device__ __forceinline__ uint32_t lb_eid_win(const uint2* __restrict__ adj, ui
 // The result is the edge id, or -1 when the edge does not exist.
 // One bucket = one 32-byte sector, read with a single 256-bit load (sm_100 family).
 __device__ __forceinline__ void ld_bucket(const unsigned long long* p, ulonglong2& lo, ulonglong2& hi) {
+  ZG_NOTE_LOAD(p, 32);
   asm("ld.global.nc.v4.u64 {%0, %1, %2, %3}, [%4];" : "=l"(lo.x), "=l"(lo.y), "=l"(hi.x), "=l"(hi.y) : "l"(p));
 }
 
 // One wide edge record (32 bytes, one sector) in a single 256-bit load.
 __device__ __forceinline__ void ld_rec(const ZgRec* r, uint4& e, uint4& p) {
   unsigned long long a, b, c, d;
+  ZG_NOTE_LOAD(r, 32);
   asm("ld.global.nc.v4.u64 {%0, %1, %2, %3}, [%4];" : "=l"(a), "=l"(b), "=l"(c), "=l"(d) : "l"(r));
   e = make_uint4((uint32_t)a, (uint32_t)(a >> 32), (uint32_t)b, (uint32_t)(b >> 32));
   p = make_uint4((uint32_t)c, (uint32_t)(c >> 32), (uint32_t)d, (uint32_t)(d >> 32));

@@ -9,11 +9,9 @@
 #include <mutex>
 #include <vector>
 
-#include "zg_programs.cuh"
+#include "zg_sample_kernel.cuh"
 
 namespace {
-
-constexpr int kBlock = 256;
 
 template <bool DBG>
 __device__ __forceinline__ void run_program(const ZgDevGraph& g, const ZgProgParams& pp, Ctx& c, Res& r) {
@@ -26,119 +24,6 @@ __device__ __forceinline__ void run_program(const ZgDevGraph& g, const ZgProgPar
     case ZG_PROG_CHAIN: prog_chain<DBG>(g, (int)pp.param, c, r); break;
     default: prog_pattern<DBG>(g, pp, c, r); break;
   }
-}
-
-// The 4-chain's sample loop with the warp's samples grouped by program.  FourChain.cpp draws one
-// of three programs per sample, and their dependent-load chains differ in length (the second
-// program adds a lower-bound search): a warp mixing them waits for its slowest lane at every step.
-// Each warp draws the program of its next 32 samples (the same sample indices the plain loop gives
-// its lanes), queues them per program in shared memory and runs a program's queue whenever it
-// holds 32 samples, so most warps run one program on all lanes; leftovers run at the end.
-// Exact sums are unchanged (the same samples, integer sums); the variance term is summed per lane
-// in another order.
-template <int LAYOUT>
-__device__ __forceinline__ void four_chain_grouped(const ZgDevGraph& g, uint64_t n, uint64_t first, uint64_t seed,
-                                                   const ZgKeys& keys, uint32_t stream, uint32_t den, Acc& a,
-                                                   AccSlots<kBlock>& sl) {
-  __shared__ uint32_t queue[kBlock / 32][3][64];
-  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const uint32_t below = (1u << lane) - 1;
-  const uint64_t base = (uint64_t)blockIdx.x * kBlock + warp * 32;
-  const uint64_t stride = (uint64_t)gridDim.x * kBlock;
-  uint32_t(*q)[64] = queue[warp];
-  uint32_t c1 = 0, c2 = 0, c3 = 0;  // queued samples per program, the same on every lane
-  for (uint32_t k = 0;; ++k) {
-    const uint64_t i = base + (uint64_t)k * stride + lane;
-    const bool valid = i < n;
-    if (!__ballot_sync(0xffffffffu, valid)) break;
-    const uint32_t sel = valid ? (uint32_t)zg_draw_map(zg_sample_word_k(keys, stream, first + i, 0), 1, 3) : 0u;
-    const unsigned m1 = __ballot_sync(0xffffffffu, sel == 1), m2 = __ballot_sync(0xffffffffu, sel == 2),
-                   m3 = __ballot_sync(0xffffffffu, sel == 3);
-    // every count is <= 31 before this round, so a queue of 64 never overflows
-    if (sel == 1) q[0][c1 + __popc(m1 & below)] = k * 32 + lane;
-    if (sel == 2) q[1][c2 + __popc(m2 & below)] = k * 32 + lane;
-    if (sel == 3) q[2][c3 + __popc(m3 & below)] = k * 32 + lane;
-    c1 += __popc(m1);
-    c2 += __popc(m2);
-    c3 += __popc(m3);
-    __syncwarp();
-#pragma unroll 1
-    for (;;) {  // run every full queue (at most two fill up in one round)
-      const uint32_t p = c1 >= 32 ? 1u : c2 >= 32 ? 2u : c3 >= 32 ? 3u : 0u;
-      if (!p) break;
-      const uint32_t cp = p == 1 ? c1 : p == 2 ? c2 : c3;
-      const uint32_t slot = q[p - 1][cp - 32 + lane];
-      c1 -= p == 1 ? 32u : 0u;
-      c2 -= p == 2 ? 32u : 0u;
-      c3 -= p == 3 ? 32u : 0u;
-      __syncwarp();  // read before the next round refills the queue
-      const uint64_t si = base + (uint64_t)(slot >> 5) * stride + (slot & 31);
-      Ctx c{seed, first + si, stream, 0, nullptr, 0, 0, &keys};
-      Res r;
-      res_init(r);
-      prog_four_chain<false>(g, c, r, p);
-      acc_add_slots(a, sl, r, den);
-    }
-  }
-  __syncwarp();
-  // the leftovers: fewer than 32 per program
-#pragma unroll 1
-  for (uint32_t p = 1; p <= 3; ++p) {
-    const uint32_t cp = p == 1 ? c1 : p == 2 ? c2 : c3;
-    if (lane < cp) {
-      const uint32_t slot = q[p - 1][lane];
-      const uint64_t si = base + (uint64_t)(slot >> 5) * stride + (slot & 31);
-      Ctx c{seed, first + si, stream, 0, nullptr, 0, 0, &keys};
-      Res r;
-      res_init(r);
-      prog_four_chain<false>(g, c, r, p);
-      acc_add_slots(a, sl, r, den);
-    }
-  }
-}
-
-// Production kernels: one specialisation per program, per register budget (MINB resident blocks
-// of 256 threads requested from the compiler; zg_tune picks the fastest per program) and per record
-// layout (0 compact, 1 wide, 2 packed: the layout tests of the record accessors fold away; each
-// layout gets its own registers).
-template <int KIND, int MINB, int LAYOUT>
-__global__ void __launch_bounds__(kBlock, MINB)
-    k_sample(ZgDevGraph g, ZgProgParams pp, uint64_t n, uint64_t first, uint64_t seed, const __grid_constant__ ZgKeys keys,
-             uint32_t stream, ZgPartial* __restrict__ partials) {
-  g.wide = LAYOUT == 1;
-  g.packed = LAYOUT == 2;
-  // Sums in shared-memory slots for the programs with long dependent chains (measured: 4-clique
-  // and 4-chain faster); the triangle and 3-chain were faster with them in registers.
-  constexpr bool kSlots = KIND != ZG_PROG_THREE_CHAIN && KIND != ZG_PROG_TRIANGLE;
-  __shared__ AccSlots<kBlock> sl;
-  Acc a;
-  acc_init(a);
-  if (kSlots) acc_slots_init(sl);
-  if (KIND == ZG_PROG_FOUR_CHAIN) {
-    four_chain_grouped<LAYOUT>(g, n, first, seed, keys, stream, pp.den_log2, a, sl);
-    acc_from_slots(a, sl);
-    block_reduce_store<kBlock>(a, &partials[blockIdx.x]);
-    return;
-  }
-  uint64_t stride = (uint64_t)gridDim.x * kBlock;
-  for (uint64_t i = blockIdx.x * (uint64_t)kBlock + threadIdx.x; i < n; i += stride) {
-    Ctx c{seed, first + i, stream, 0, nullptr, 0, 0, &keys};
-    Res r;
-    res_init(r);
-    if (KIND == ZG_PROG_TRIANGLE) prog_triangle<false>(g, c, r);
-    else if (KIND == ZG_PROG_FOUR_CLIQUE) prog_four_clique<false>(g, c, r);
-    else if (KIND == ZG_PROG_FOUR_CLIQUE_UNBIASED) prog_four_clique<false, true>(g, c, r);
-    else if (KIND == ZG_PROG_THREE_CHAIN) prog_three_chain<false>(g, c, r);
-    else if (KIND == ZG_PROG_FOUR_CHAIN) prog_four_chain<false>(g, c, r);
-    else if (KIND == ZG_PROG_CHAIN) prog_chain<false>(g, (int)pp.param, c, r);
-    else prog_pattern<false>(g, pp, c, r);
-    if (kSlots)
-      acc_add_slots(a, sl, r, pp.den_log2);
-    else
-      acc_add(a, r, pp.den_log2);
-  }
-  if (kSlots) acc_from_slots(a, sl);
-  block_reduce_store<kBlock>(a, &partials[blockIdx.x]);
 }
 
 __global__ void __launch_bounds__(kBlock) k_sample_debug(ZgDevGraph g, ZgProgParams pp, uint64_t n, uint64_t first,
@@ -553,6 +438,9 @@ double zg_exact_mean_host(const uint64_t s[5], uint32_t den, uint64_t n) { retur
 
 // Shared by the allocation-free entry points of other translation units.
 int zg_sample_grid(int kind, int layout) { return grid_for_kind(kind, layout); }
+
+// A program's kernel parameters, for other translation units.
+ZgProgParams zg_prog_params(const zg_program* p) { return params_for(p); }
 
 // Per-group estimates (device array out[n_groups]) on stream s.
 int zg_launch_groups(const zg_graph* g, const zg_program* p, uint64_t n_groups, uint32_t group, uint64_t first,

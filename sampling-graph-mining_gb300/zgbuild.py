@@ -115,11 +115,11 @@ def build_app(sources, out, include_dirs=(), extra_flags=()):
 
 def build_oracle(verbose=False, force=False):
     os.makedirs(ORACLE_BUILD, exist_ok=True)
-    src = os.path.join(ORACLE_DIR, "zg_oracle.c")
-    deps = [src, os.path.join(ORACLE_DIR, "zg_oracle.h"), os.path.join(ROOT, "include", "zgraph_gpu.h")]
+    srcs = [os.path.join(ORACLE_DIR, f) for f in ("zg_oracle.c", "zgo_gen.c")]
+    deps = srcs + [os.path.join(ORACLE_DIR, "zg_oracle.h"), os.path.join(ROOT, "include", "zgraph_gpu.h")]
     if force or _stale(ORACLE_LIB, deps):
         cc = os.environ.get("CC", "gcc")
-        _run([cc, "-O2", "-fopenmp", "-fPIC", "-shared", "-o", ORACLE_LIB, src, "-lm"])
+        _run([cc, "-O2", "-fopenmp", "-fPIC", "-shared", "-o", ORACLE_LIB] + srcs + ["-lm"])
     return ORACLE_LIB
 
 

@@ -31,8 +31,11 @@ ERRORS = {1: "INVALID_ARG", 2: "OOM", 3: "CUDA", 4: "INVALID_GRAPH", 5: "UNSUPPO
 PROG_TRIANGLE, PROG_FOUR_CLIQUE, PROG_THREE_CHAIN, PROG_FOUR_CHAIN, PROG_CHAIN, PROG_PATTERN = 1, 2, 3, 4, 5, 6
 PROG_FOUR_CLIQUE_UNBIASED = 7  # canonical-path 4-clique estimator (no counterpart in the reference)
 EXACT_TRIANGLE, EXACT_WEDGE, EXACT_THREE_PATH, EXACT_FIVE_STAR, EXACT_FOUR_CLIQUE = 1, 2, 3, 4, 5
+EXACT_FIVE_HOUSE, EXACT_FIVE_CHAIN, EXACT_WEIGHTED_TRIANGLE, EXACT_AT_LEAST_ONE_TRIANGLE = 6, 7, 8, 9
 PRED_GE, PRED_LT, PRED_GT, PRED_LE, PRED_EQ, PRED_NE, PRED_RANGE = 1, 2, 3, 4, 5, 6, 7
 QUERY_THREE_MOTIF = 16
+BOUND_CLT, BOUND_BERNSTEIN = 1, 2
+RESULT_BYTES = 112  # ZG_RESULT_BYTES: one reduced result of zg_run_async
 GRAPH_SAMPLING_ONLY = 1
 RECORDS_AUTO, RECORDS_COMPACT, RECORDS_WIDE, RECORDS_PACKED = 0, 1, 2, 3
 BATCH_MAX_QUERIES, BATCH_MAX_CHUNKS = 65536, 65536
@@ -90,7 +93,8 @@ class ElpResult(C.Structure):
 class QueryResult(C.Structure):
     _fields_ = [("estimate", C.c_double), ("half_width", C.c_double), ("rel_half_width", C.c_double),
                 ("samples", C.c_uint64), ("hits", C.c_uint64), ("bound_met", C.c_uint32), ("rounds", C.c_uint32),
-                ("n_sized", C.c_uint64), ("ms_total", C.c_double)]
+                ("n_sized", C.c_uint64), ("ms_total", C.c_double), ("bound_method", C.c_uint32),
+                ("reserved", C.c_uint32), ("weight_range", C.c_double)]
 
 
 ELP_KEEP_OFFSET, ELP_SHUFFLE_OFFSET, ELP_FILTER_OFFSET, ELP_STREAM = 1, 2, 3, 0x454C5000
@@ -172,6 +176,10 @@ def lib():
             "zg_batch_tune": ([P, P, U32, P, C.POINTER(I32), P], I32),
             "zg_batch_elapsed_ms": ([P, C.POINTER(C.c_float)], I32),
             "zg_read_bandwidth": ([U64, U32, P, C.POINTER(D)], I32),
+            "zg_touch_sectors": ([P, P, U64, U64, U64, U32, P, C.POINTER(U64)], I32),
+            "zg_exact_count_weighted": ([P, I32, U32, P, P], I32),
+            "zg_bound_half_width": ([D, D, U64, U64, D, D, D, C.POINTER(D), C.POINTER(U32), C.POINTER(U32)], I32),
+            "zg_batch_copy_bytes": ([P, C.POINTER(U64), C.POINTER(U64)], I32),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -313,6 +321,12 @@ class Graph:
     def set_meta(self, num_edges, max_degree):
         check(lib().zg_graph_set_meta(self.handle, num_edges, max_degree))
 
+    def download_edges(self):
+        """The COO edge list in edge-id order, (m, 2) uint32 (unpacked on the device)."""
+        e = np.empty((self.num_local_edges, 2), np.uint32)
+        check(lib().zg_graph_download(self.handle, _ptr(e), None, None, None, None, None))
+        return e
+
     def download(self, neighbour_order=True):
         """Device arrays on the host; neighbour_order=False skips adj_n (absent from the graphs a
         batch caches)."""
@@ -349,6 +363,13 @@ class Graph:
     def exact_count(self, kind, stream=None):
         out = (C.c_uint64 * 2)()
         check(lib().zg_exact_count(self.handle, kind, stream, out))
+        return int(out[0]) | (int(out[1]) << 64)
+
+    def exact_count_weighted(self, kind, threshold, stream=None):
+        """zg_exact_count_weighted: EXACT_WEIGHTED_TRIANGLE (all edges' data >= threshold) or
+        EXACT_AT_LEAST_ONE_TRIANGLE (some edge's data >= threshold)."""
+        out = (C.c_uint64 * 2)()
+        check(lib().zg_exact_count_weighted(self.handle, kind, threshold, stream, out))
         return int(out[0]) | (int(out[1]) << 64)
 
     def free(self):
@@ -460,6 +481,12 @@ class Batch:
                  for i in range(nq)]
         return total, [bool(met[i]) for i in range(nq)], int(rounds.value)
 
+    def copy_bytes(self):
+        """zg_batch_copy_bytes: (host->device bytes per submit, device->host bytes per wait)."""
+        a, b = C.c_uint64(), C.c_uint64()
+        check(lib().zg_batch_copy_bytes(self._h, C.byref(a), C.byref(b)))
+        return int(a.value), int(b.value)
+
     def elapsed_ms(self):
         """Device time of the last waited batch (CUDA events around its graph launch)."""
         ms = C.c_float(0)
@@ -548,6 +575,12 @@ class Program:
         check(lib().zg_get_variant(self.kind, C.byref(v), C.byref(mb), C.byref(g)))
         return {"variant": v.value, "min_blocks": mb.value, "grid": g.value}
 
+    def touch_bytes_per_sample(self, graph, n, seed, stream_id=0, first_sample=0):
+        """zg_touch_sectors: 32-byte sectors the production kernel's loads touch, x 32 / n."""
+        out = C.c_uint64()
+        check(lib().zg_touch_sectors(graph.handle, self._h, n, first_sample, seed, stream_id, None, C.byref(out)))
+        return 32.0 * out.value / n
+
     def run_debug(self, graph, n, seed, stream_id=0, first_sample=0):
         tr = np.zeros(n, dtype=TRACE_DTYPE)
         check(lib().zg_run_debug(graph.handle, self._h, n, first_sample, seed, stream_id, _ptr(tr)))
@@ -604,6 +637,13 @@ def query(graph, program, eps, conf, n_initial, seed, stream_id=0, max_samples=0
     check(lib().zg_query(graph.handle, program.handle, eps, conf, n_initial, max_samples, seed, stream_id,
                          cuda_stream, C.byref(out)))
     return out
+
+
+def bound_half_width(mean, var, n, hits, eps, conf, weight_range):
+    """zg_bound_half_width: (half-width, BOUND_CLT or BOUND_BERNSTEIN, met) of a running estimate."""
+    h, m, ok = C.c_double(), C.c_uint32(), C.c_uint32()
+    check(lib().zg_bound_half_width(mean, var, n, hits, eps, conf, weight_range, C.byref(h), C.byref(m), C.byref(ok)))
+    return h.value, m.value, bool(ok.value)
 
 
 def merge_counters(parts):

@@ -76,13 +76,23 @@ def test_all_predicate_triangle(golden):
 def test_naive_exact_counts(golden):
     meta, arr = golden
     kinds = {"triangle": Z.EXACT_TRIANGLE, "wedge": Z.EXACT_WEDGE, "three_path": Z.EXACT_THREE_PATH,
-             "five_star": Z.EXACT_FIVE_STAR, "four_clique": Z.EXACT_FOUR_CLIQUE}
+             "five_star": Z.EXACT_FIVE_STAR, "four_clique": Z.EXACT_FOUR_CLIQUE, "house": Z.EXACT_FIVE_HOUSE,
+             "five_chain": Z.EXACT_FIVE_CHAIN}
+    weighted = {"weighted_triangle_50": Z.EXACT_WEIGHTED_TRIANGLE,
+                "at_least_one_triangle_50": Z.EXACT_AT_LEAST_ONE_TRIANGLE}
+    checked = set()
     for gname, counts in meta["naive"].items():
         e, nv = golden_graph(meta, arr, gname)
-        g = Z.Graph.from_edges(e, nv)
+        w = arr[gname + "_weights"] if any(k in weighted for k in counts) else None
+        g = Z.Graph.from_edges(e, nv, weights=w)
         for k, v in counts.items():
             if k in kinds:
                 assert g.exact_count(kinds[k]) == v, (gname, k)
+            else:  # every committed golden count is checked: no kind may be skipped
+                assert k in weighted, "golden count %s has no device counter" % k
+                assert g.exact_count_weighted(weighted[k], 50) == v, (gname, k)
+            checked.add(k)
+    assert checked == set(kinds) | set(weighted)
 
 
 def test_error_profile_matches_reference(golden):

@@ -196,11 +196,32 @@ def test_exact_counts_match_oracle(graphs, gname):
     e, nv = graphs[gname]
     g = Z.Graph.from_edges(e, nv)
     og = O.OracleGraph(e, nv)
-    for kind in (Z.EXACT_TRIANGLE, Z.EXACT_WEDGE, Z.EXACT_THREE_PATH, Z.EXACT_FIVE_STAR, Z.EXACT_FOUR_CLIQUE):
+    for kind in (Z.EXACT_TRIANGLE, Z.EXACT_WEDGE, Z.EXACT_THREE_PATH, Z.EXACT_FIVE_STAR, Z.EXACT_FOUR_CLIQUE,
+                 Z.EXACT_FIVE_HOUSE, Z.EXACT_FIVE_CHAIN):
         assert g.exact_count(kind) == og.exact_fast(kind), kind
     if gname != "chunglu3k":
         for kind in (Z.EXACT_TRIANGLE, Z.EXACT_WEDGE, Z.EXACT_THREE_PATH, Z.EXACT_FIVE_STAR):
             assert g.exact_count(kind) == og.exact_naive(kind), kind
+    # a graph built without the neighbour-ordered adjacency sorts its own lists
+    gs = Z.Graph.gen_rmat(10, 8, seed=3, sampling_only=True) if gname == "rmat10" else None
+    if gs is not None:
+        for kind in (Z.EXACT_FIVE_HOUSE, Z.EXACT_FIVE_CHAIN, Z.EXACT_TRIANGLE):
+            assert gs.exact_count(kind) == og.exact_fast(kind), kind
+
+
+def test_weighted_exact_counts_match_oracle(graphs):
+    e, nv = graphs["chunglu3k"]
+    w = Z.gen_weights(len(e), 100, seed=4)
+    g = Z.Graph.from_edges(e, nv, weights=w)
+    og = O.OracleGraph(e, nv, w)
+    for t in (0, 10, 50, 90, 100):
+        assert g.exact_count_weighted(Z.EXACT_WEIGHTED_TRIANGLE, t) == og.exact_weighted_triangle(t, False), t
+        assert g.exact_count_weighted(Z.EXACT_AT_LEAST_ONE_TRIANGLE, t) == og.exact_weighted_triangle(t, True), t
+    assert g.exact_count_weighted(Z.EXACT_WEIGHTED_TRIANGLE, 0) == g.exact_count(Z.EXACT_TRIANGLE)
+    with pytest.raises(Z.ZgError):
+        Z.Graph.from_edges(e, nv).exact_count_weighted(Z.EXACT_WEIGHTED_TRIANGLE, 50)  # no edge data
+    with pytest.raises(Z.ZgError):
+        g.exact_count(Z.EXACT_WEIGHTED_TRIANGLE)  # takes a threshold: zg_exact_count_weighted
 
 
 def test_edge_cases(graphs):
