@@ -229,9 +229,11 @@ int zg_result_to_counters(const void* h_result, const zg_program* p, zg_counters
  * latency-critical path where cudaMalloc/cudaFree could synchronise the device.  It has no
  * counterpart in the reference.  The per-block scratch is one fixed device array of
  * ZG_NOALLOC_MAX_BLOCKS x ZG_RESULT_BYTES bytes (448 KiB) that every GPU loading the library keeps
- * until the process exits; a launch that would need more blocks is rejected with ZG_ERR_TOO_LARGE.
- * The first call on each device looks up the array's device address (cudaGetSymbolAddress), so
- * make that first call before any stream capture.  All calls share the array: calls whose
+ * until the process exits; a launch that would need more blocks is rejected with ZG_ERR_TOO_LARGE
+ * (a launch needs at most 8 resident blocks per SM, 1216 on a 152-SM GB300).  The array used is the
+ * current device's: g must have been built on the current device (a graph on another device is
+ * refused with ZG_ERR_INVALID_ARG).  The first call on each device looks up the array's device
+ * address (cudaGetSymbolAddress), so make that first call before any stream capture.  All calls share the array: calls whose
  * executions overlap on the GPU race and must be serialised by the caller.  d_result: device
  * memory of ZG_RESULT_BYTES bytes provided by the caller; read it as for zg_run_async. */
 #define ZG_NOALLOC_MAX_BLOCKS 4096
@@ -260,6 +262,31 @@ int zg_run_three_motif(const zg_graph* g, uint64_t n_chain, uint64_t n_tri, uint
 int zg_run_three_motif_debug(const zg_graph* g, uint64_t n_chain, uint64_t n_tri,
                              uint64_t seed, uint32_t stream_chain, uint32_t stream_tri,
                              zg_sample_trace* chain_traces, zg_sample_trace* tri_traces);
+
+/* ---- the closure primitive on its own ------------------------------------------------- */
+/* ZGraphInstance::conditional_close(min_valid_edge_id, sampled_vertices, edges_to_wait&)
+ * (src/ZGraphInstance.cpp:410-441, include/ZGraphInstance.hpp:131), one query per thread: for each
+ * edge to wait in order, look for it in the lists of the sampled vertices, at an edge id >=
+ * min_valid_edge_id; a found edge's id is written back (the reference stores it in
+ * edge_to_wait.edge_id), and the first edge not found ends the query with closed = 0.  An edge is
+ * found only in the list of a sampled vertex, so an edge none of whose endpoints is sampled is not
+ * found, as in the reference.  The estimator programs answer the same question with a cuckoo-table
+ * look-up (the edges they wait for always join sampled vertices). */
+typedef struct zg_close_query {
+  uint64_t min_valid_edge_id;
+  uint32_t num_vertices;             /* <= ZG_MAX_LIST */
+  uint32_t num_edges;                /* <= ZG_MAX_LIST */
+  uint32_t vertices[ZG_MAX_LIST];
+  uint32_t edges[2 * ZG_MAX_LIST];   /* (src, dst) of each edge to wait */
+} zg_close_query;
+typedef struct zg_close_result {
+  uint32_t closed;                   /* every edge was found: conditional_close's return value */
+  uint32_t found;                    /* edges found before the first miss (their ids are valid) */
+  uint64_t edge_ids[ZG_MAX_LIST];
+} zg_close_result;
+/* queries and results: host arrays of n entries (copied in and out on cuda_stream; synchronous). */
+int zg_conditional_close(const zg_graph* g, const zg_close_query* queries, uint32_t n, void* cuda_stream,
+                         zg_close_result* results);
 
 /* ---- batched mixed queries ----------------------------------------------------- */
 /* Many estimator queries of uneven program, predicate and budget in one persistent launch (no

@@ -76,6 +76,7 @@ def lib():
             "zgo_regression_k": ([P, P, U32], D),
             "zgo_ext_inv_product": ([P, I32], D),
             "zgo_gen_rmat": ([U32, U32, D, D, D, U64, U64, P, C.POINTER(C.c_uint64)], I32),
+            "zgo_conditional_close_ids": ([C.POINTER(_Graph), U64, P, U32, P, U32, P, C.POINTER(C.c_uint32)], I32),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -119,6 +120,17 @@ class OracleGraph:
             return np.ctypeslib.as_array(C.cast(ptr, C.POINTER(np.ctypeslib.as_ctypes_type(dt))), (n,)).copy()
         return {"off": arr(self.g.off, nv + 1, np.uint64), "adj_nbr": arr(self.g.adj_nbr, 2 * m, np.uint32),
                 "adj_eid": arr(self.g.adj_eid, 2 * m, np.uint64)}
+
+    def conditional_close(self, min_valid, vertices, edges):
+        """conditional_close(min_valid, vertices, edges&) (src/ZGraphInstance.cpp:410-441):
+        (closed, found, edge ids of the found edges)."""
+        v = np.ascontiguousarray(vertices, dtype=np.uint32)
+        e = np.ascontiguousarray(edges, dtype=np.uint32).reshape(-1, 2)
+        ids = np.zeros(max(1, len(e)), np.uint64)
+        found = C.c_uint32(0)
+        closed = lib().zgo_conditional_close_ids(C.byref(self.g), min_valid, _p(v), len(v), _p(e), len(e), _p(ids),
+                                                 C.byref(found))
+        return bool(closed), int(found.value), ids[:found.value].copy()
 
     def exact_naive(self, kind):
         out = (C.c_uint64 * 2)()
@@ -168,10 +180,12 @@ class OracleProgram:
             pass
 
 
-def traces(graph, prog, n, seed, stream=0, first=0):
+def traces(graph, prog, n, seed, stream=0, first=0, threads=0):
+    """Per-sample traces (and the run's counters) of samples [first, first + n); each sample's trace
+    is independent of the thread that computes it."""
     tr = np.zeros(n, dtype=TRACE_DTYPE)
     c = Counters()
-    rc = lib().zgo_run(C.byref(graph.g), C.byref(prog.p), n, first, seed, stream, 1, C.byref(c), _p(tr))
+    rc = lib().zgo_run(C.byref(graph.g), C.byref(prog.p), n, first, seed, stream, threads, C.byref(c), _p(tr))
     assert rc == 0
     return tr, c
 

@@ -981,6 +981,31 @@ void zgo_shuffle_perm(uint64_t m, uint64_t shuffle_seed, uint64_t* perm) {
   free(kv);
 }
 
+/* ZGraphInstance::conditional_close(min_valid_edge_id, sampled_vertices, edges_to_wait&)
+ * (src/ZGraphInstance.cpp:410-441): each edge to wait in order, searched in every sampled
+ * vertex's list (ids below min_valid skipped), its edge id written back when found; returns 0 at
+ * the first edge not found.  *found: the edges found before that. */
+int zgo_conditional_close_ids(const zgo_graph* g, uint64_t min_valid, const uint32_t* vertices, uint32_t nv,
+                              const uint32_t* edges, uint32_t ne, uint64_t* edge_ids, uint32_t* found) {
+  *found = 0;
+  for (uint32_t i = 0; i < ne; ++i) {
+    uint32_t ws = edges[2 * i], wd = edges[2 * i + 1];
+    int hit = 0;
+    for (uint32_t j = 0; j < nv && !hit; ++j) {
+      uint32_t v = vertices[j];
+      if (v >= g->nv) continue; /* outgoing_adj_bitmap: no list */
+      for (uint64_t idx = g->off[v]; idx < g->off[v + 1]; ++idx) {
+        if (g->adj_eid[idx] < min_valid) continue;
+        uint32_t s = v, d = g->adj_nbr[idx];
+        if ((s == ws && d == wd) || (d == ws && s == wd)) { edge_ids[i] = g->adj_eid[idx]; hit = 1; break; }
+      }
+    }
+    if (!hit) return 0;
+    *found = i + 1;
+  }
+  return 1;
+}
+
 /* ------------------------------------------------------------------------- */
 /* Exact counts.  u128 results. */
 static void put128(uint64_t out[2], u128 v) { out[0] = (uint64_t)v; out[1] = (uint64_t)(v >> 64); }

@@ -90,6 +90,11 @@ int zgo_subsample_keep(double rate, uint64_t keep_seed, uint64_t e);
 /* The permutation applied by a shuffle seed: perm[i] = input position of output edge i. */
 void zgo_shuffle_perm(uint64_t m, uint64_t shuffle_seed, uint64_t* perm);
 
+/* conditional_close with the found edge ids written back (src/ZGraphInstance.cpp:410-441).
+ * Returns 1 when every edge was found; *found = edges found before the first miss. */
+int zgo_conditional_close_ids(const zgo_graph* g, uint64_t min_valid, const uint32_t* vertices, uint32_t nv,
+                              const uint32_t* edges, uint32_t ne, uint64_t* edge_ids, uint32_t* found);
+
 /* Exact counts, restating naive_implementation/<Counter>.cpp (out: 128-bit). */
 int zgo_exact_naive(const zgo_graph* g, int kind, uint64_t out[2]);
 /* Faster CPU restatements of the same counts (checked against the naive ones). */

@@ -128,6 +128,10 @@ class ZGraphInstance {
   zg_program* program_;      // device program reproducing estimate(), identified on first use
   bool program_owned_;
   bool validating_;          // estimate() is being replayed against device traces
+  // The ASAP primitives run on the host only while estimate() replays a device trace (program
+  // identification, replay_trace, CachedSubPatterns); outside a replay they throw: estimates come
+  // from calculate() on the GPU, and there is no host execution path.
+  void require_replay(const char* primitive) const;
   uint64_t seed_;            // Philox key of this instance's estimators
   uint32_t stream_id_;       // Philox stream of this instance's estimators
   uint64_t next_sample_;     // first sample index of the next calculate()

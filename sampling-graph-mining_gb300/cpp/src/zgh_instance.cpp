@@ -278,7 +278,16 @@ double ZGraphInstance<E>::calculate(unsigned long long num_estmators, VertexId n
 }
 
 template <typename E>
+void ZGraphInstance<E>::require_replay(const char* primitive) const {
+  if (!validating_)
+    throw std::runtime_error(std::string(primitive) +
+                             ": the ASAP primitives run on the host only to replay a device trace; estimates come "
+                             "from calculate() on the GPU (no host execution path, ZG_ERR_UNSUPPORTED_ESTIMATOR)");
+}
+
+template <typename E>
 std::pair<VertexId, double> ZGraphInstance<E>::sample_vertex() {
+  require_replay("sample_vertex");
   if (graph->p.local_partition_offset[0] == graph->p.local_partition_offset[1])
     return std::make_pair((VertexId)0, (double)-1);
   VertexId min_v = graph->p.local_partition_offset[0];
@@ -288,6 +297,7 @@ std::pair<VertexId, double> ZGraphInstance<E>::sample_vertex() {
 
 template <typename E>
 std::pair<Edge<E>, double> ZGraphInstance<E>::sample_edge() {
+  require_replay("sample_edge");
   if (is_counting_sample_edge_calls) ++cnt;
   Edge<E> edge;
   EdgeId m = graph->num_local_edges[0];
@@ -303,6 +313,7 @@ std::pair<Edge<E>, double> ZGraphInstance<E>::sample_edge() {
 
 template <typename E>
 std::pair<VertexId, double> ZGraphInstance<E>::conditional_sample_vertex(const SubGraph<E>& sub_graph) {
+  require_replay("conditional_sample_vertex");
   VertexId lo = sub_graph.get_min_valid_vertex_id();
   VertexId end = graph->p.local_partition_offset[1];
   if (lo >= end) return std::make_pair((VertexId)0, (double)-1);
@@ -315,6 +326,7 @@ std::pair<VertexId, double> ZGraphInstance<E>::conditional_sample_vertex(const S
 template <typename E>
 std::pair<Edge<E>, double> ZGraphInstance<E>::core_conditional_sample_edge(const MyList<Edge<E>>& sampled_edges,
                                                                          const MyList<VertexId>& sampled_vertices) {
+  require_replay("conditional_sample_edge");
   EdgeId min_valid = 0;
   for (int i = 0; i < sampled_edges.list_size; ++i)
     if (sampled_edges.list[i].edge_id + 1 > min_valid) min_valid = sampled_edges.list[i].edge_id + 1;
@@ -406,6 +418,7 @@ bool ZGraphInstance<E>::conditional_close(const SubGraph<E>& sampled_subgraph, c
 template <typename E>
 bool ZGraphInstance<E>::conditional_close(EdgeId min_valid_edge_id, const MyList<VertexId>& sampled_vertices,
                                           MyList<Edge<E>>& edges_to_wait) {
+  require_replay("conditional_close");
   Bitmap* bm = graph->outgoing_adj_bitmap[0];
   const EdgeId* idx = graph->outgoing_adj_index[0];
   const AdjUnit<E>* adj = graph->outgoing_adj_list[0];
@@ -432,6 +445,7 @@ bool ZGraphInstance<E>::conditional_close(EdgeId min_valid_edge_id, const MyList
 
 template <typename E>
 unsigned long long ZGraphInstance<E>::sample_interger(unsigned long long min_int, unsigned long long max_int) {
+  require_replay("sample_interger");
   return randoms[0].rand_int(min_int, max_int);
 }
 

@@ -19,6 +19,7 @@
 #include "zg_internal.cuh"
 
 int zg_sample_grid(int kind, int layout);
+int zg_check_device();
 int zg_launch_sample_with_scratch(const zg_graph* g, const zg_program* p, uint64_t n, uint64_t first, uint64_t seed,
                                   uint32_t stream_id, cudaStream_t s, ZgPartial* scratch, int grid, void* d_result);
 
@@ -32,10 +33,21 @@ ZgPartial* g_scratch_ptr[kMaxDevices] = {nullptr};
 
 // Once per device, with that device current: the device address of the scratch array.  (Host
 // code cannot use &g_noalloc_scratch directly; that is a host-side shadow, not device memory.)
-int scratch_for_current_device(ZgPartial** out) {
+// The array used is the current device's, so the graph must live on the current device; a graph
+// on another device is refused.
+int scratch_for_current_device(const zg_graph* g, ZgPartial** out) {
   int dev = 0;
   ZG_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= kMaxDevices) return zg_set_error(ZG_ERR_INVALID_ARG, "device %d out of range", dev), ZG_ERR_INVALID_ARG;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, g->off) != cudaSuccess) {  // offsets: allocated for every graph
+    cudaGetLastError();
+    return zg_set_error(ZG_ERR_INVALID_ARG, "zg_run_noalloc: the graph's memory is not device memory"), ZG_ERR_INVALID_ARG;
+  }
+  if (a.type != cudaMemoryTypeDevice || a.device != dev)
+    return zg_set_error(ZG_ERR_INVALID_ARG, "zg_run_noalloc: the graph lives on device %d, the current device is %d",
+                        a.device, dev),
+           ZG_ERR_INVALID_ARG;
   std::lock_guard<std::mutex> lk(g_mu);
   if (!g_scratch_ptr[dev]) {
     void* ptr = nullptr;
@@ -52,6 +64,10 @@ int scratch_for_current_device(ZgPartial** out) {
 extern "C" int zg_run_noalloc(const zg_graph* g, const zg_program* p, uint64_t n, uint64_t first_sample,
                               uint64_t seed, uint32_t stream_id, void* cuda_stream, void* d_result) {
   if (!g || !p || !d_result) return zg_set_error(ZG_ERR_INVALID_ARG, "null graph, program or result"), ZG_ERR_INVALID_ARG;
+  if (int rc = zg_check_device()) return rc;
+  ZgPartial* scratch = nullptr;
+  int rc = scratch_for_current_device(g, &scratch);
+  if (rc) return rc;
   int grid = zg_sample_grid(p->kind, g->wide ? 1 : g->packed ? 2 : 0);
   uint64_t need = (n + 255) / 256;
   if ((uint64_t)grid > need) grid = (int)(need ? need : 1);
@@ -60,9 +76,6 @@ extern "C" int zg_run_noalloc(const zg_graph* g, const zg_program* p, uint64_t n
                         "zg_run_noalloc: the launch needs %d blocks of scratch but the fixed array holds %d",
                         grid, ZG_NOALLOC_MAX_BLOCKS),
            ZG_ERR_TOO_LARGE;
-  ZgPartial* scratch = nullptr;
-  int rc = scratch_for_current_device(&scratch);
-  if (rc) return rc;
   return zg_launch_sample_with_scratch(g, p, n, first_sample, seed, stream_id, (cudaStream_t)cuda_stream, scratch,
                                        grid, d_result);
 }

@@ -380,6 +380,19 @@ bool g_tune_init[kMaxDev];
 // Defaults before tuning (register footprints measured with -Xptxas -v).
 constexpr int kDefaultVariant[8] = {3, 3, 2, 3, 2, 3, 3, 3};
 
+// The tuning tables hold kMaxDev devices.  Every entry point checks the current device first
+// (check_device) and refuses one beyond the tables rather than give it another device's launch
+// shapes; current_device() is only reached after that check.
+int check_device() {
+  int d = 0;
+  cudaError_t e = cudaGetDevice(&d);
+  if (e != cudaSuccess) return zg_check_cuda(e, "cudaGetDevice");
+  if (d < 0 || d >= kMaxDev)
+    return zg_set_error(ZG_ERR_INVALID_ARG, "device %d is beyond the %d devices the library tracks", d, kMaxDev),
+           ZG_ERR_INVALID_ARG;
+  return ZG_OK;
+}
+
 int current_device() {
   int d = 0;
   cudaGetDevice(&d);
@@ -410,7 +423,7 @@ int grid_for_kind(int kind, int layout) { return grid_for_variant(kind, variant_
 
 int validate_run(const zg_graph* g, const zg_program* p) {
   if (!g || !p) return zg_set_error(ZG_ERR_INVALID_ARG, "null graph or program"), ZG_ERR_INVALID_ARG;
-  return ZG_OK;
+  return check_device();
 }
 
 int launch_variant(const zg_graph* g, const zg_program* p, int v, uint64_t n, uint64_t first, uint64_t seed,
@@ -436,8 +449,9 @@ void zg_partial_to_counters(const void* partial, uint32_t den, zg_counters* out)
 // The exact mean of a 320-bit sum, for other translation units.
 double zg_exact_mean_host(const uint64_t s[5], uint32_t den, uint64_t n) { return exact_mean(s, den, n); }
 
-// Shared by the allocation-free entry points of other translation units.
+// Shared by the allocation-free entry points of other translation units (after zg_check_device).
 int zg_sample_grid(int kind, int layout) { return grid_for_kind(kind, layout); }
+int zg_check_device() { return check_device(); }
 
 // A program's kernel parameters, for other translation units.
 ZgProgParams zg_prog_params(const zg_program* p) { return params_for(p); }
@@ -514,6 +528,7 @@ extern "C" int zg_set_variant(int kind, int variant) {
     return zg_set_error(ZG_ERR_INVALID_ARG, "launch variant %d outside [0, %d)", variant, kVariants), ZG_ERR_INVALID_ARG;
   if (kind < ZG_PROG_TRIANGLE || kind > ZG_PROG_FOUR_CLIQUE_UNBIASED)
     return zg_set_error(ZG_ERR_INVALID_ARG, "unknown program kind %d", kind), ZG_ERR_INVALID_ARG;
+  if (int rc = check_device()) return rc;
   variant_for(kind);  // initialise the table
   int d = current_device();
   std::lock_guard<std::mutex> lk(g_tune_mu);
@@ -524,6 +539,7 @@ extern "C" int zg_set_variant(int kind, int variant) {
 extern "C" int zg_get_variant(int kind, int* variant, int* min_blocks, int* grid) {
   if (kind < ZG_PROG_TRIANGLE || kind > ZG_PROG_FOUR_CLIQUE_UNBIASED)
     return zg_set_error(ZG_ERR_INVALID_ARG, "unknown program kind %d", kind), ZG_ERR_INVALID_ARG;
+  if (int rc = check_device()) return rc;
   int v = variant_for(kind);
   if (variant) *variant = v;
   if (min_blocks) *min_blocks = kMinBlocks[v];

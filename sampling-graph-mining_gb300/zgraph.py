@@ -90,6 +90,15 @@ class ElpResult(C.Structure):
                 ("sampled_max_degree", C.c_uint64), ("profile_ms", C.c_double)]
 
 
+class CloseQuery(C.Structure):
+    _fields_ = [("min_valid_edge_id", C.c_uint64), ("num_vertices", C.c_uint32), ("num_edges", C.c_uint32),
+                ("vertices", C.c_uint32 * 16), ("edges", C.c_uint32 * 32)]
+
+
+class CloseResult(C.Structure):
+    _fields_ = [("closed", C.c_uint32), ("found", C.c_uint32), ("edge_ids", C.c_uint64 * 16)]
+
+
 class QueryResult(C.Structure):
     _fields_ = [("estimate", C.c_double), ("half_width", C.c_double), ("rel_half_width", C.c_double),
                 ("samples", C.c_uint64), ("hits", C.c_uint64), ("bound_met", C.c_uint32), ("rounds", C.c_uint32),
@@ -178,6 +187,7 @@ def lib():
             "zg_read_bandwidth": ([U64, U32, P, C.POINTER(D)], I32),
             "zg_touch_sectors": ([P, P, U64, U64, U64, U32, P, C.POINTER(U64)], I32),
             "zg_exact_count_weighted": ([P, I32, U32, P, P], I32),
+            "zg_conditional_close": ([P, P, U32, P, P], I32),
             "zg_bound_half_width": ([D, D, U64, U64, D, D, D, C.POINTER(D), C.POINTER(U32), C.POINTER(U32)], I32),
             "zg_batch_copy_bytes": ([P, C.POINTER(U64), C.POINTER(U64)], I32),
         }
@@ -637,6 +647,27 @@ def query(graph, program, eps, conf, n_initial, seed, stream_id=0, max_samples=0
     check(lib().zg_query(graph.handle, program.handle, eps, conf, n_initial, max_samples, seed, stream_id,
                          cuda_stream, C.byref(out)))
     return out
+
+
+def conditional_close(graph, queries, cuda_stream=None):
+    """zg_conditional_close: conditional_close(min_valid, vertices, edges&) (src/ZGraphInstance.cpp:
+    410-441) for a list of (min_valid, vertices, edges) queries on the device; returns
+    [(closed, found, edge ids of the found edges)]."""
+    qs = list(queries)
+    arr = (CloseQuery * max(1, len(qs)))()
+    for i, (mv, verts, edges) in enumerate(qs):
+        edges = [tuple(x) for x in edges]
+        arr[i].min_valid_edge_id = mv
+        arr[i].num_vertices = len(verts)
+        arr[i].num_edges = len(edges)
+        for j, v in enumerate(verts[:16]):  # longer lists are rejected by the library
+            arr[i].vertices[j] = v
+        for j, (a, b) in enumerate(edges[:16]):
+            arr[i].edges[2 * j] = a
+            arr[i].edges[2 * j + 1] = b
+    res = (CloseResult * max(1, len(qs)))()
+    check(lib().zg_conditional_close(graph.handle, arr, len(qs), cuda_stream, res))
+    return [(bool(r.closed), int(r.found), [int(r.edge_ids[j]) for j in range(r.found)]) for r in res[:len(qs)]]
 
 
 def bound_half_width(mean, var, n, hits, eps, conf, weight_range):

@@ -18,7 +18,8 @@ import zgraph as Z
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 CPP = os.path.join(HERE, "cpp")
-REF_APPS = "/root/reference/applications"
+# the reference's sources (present where the oracle's reference drivers are built; absent on the GPU host)
+REF_APPS = os.path.join(os.environ.get("ZG_REFERENCE_DIR", "/root/reference"), "applications")
 
 
 def _build(src, out):

@@ -119,3 +119,25 @@ def test_chunglu_base_graph_wide_layout_matches_oracle():
     oa, ob = O.three_motif(og, nm, nm, seed, 4, 5)[2:]
     _same_counters(ca, oa, "chunglu/motif chain")
     _same_counters(cb, ob, "chunglu/motif triangle")
+
+
+def test_rmat26_headline_graph_and_programs_match_oracle():
+    """The headline graph (1.57 G edges): the device generator's edge list equals the host one the
+    CPU arm samples, and the 4-clique, 5-star and 5-house programs' traces and exact sums on sample
+    prefixes equal the oracle's (which scans the hubs' adjacency linearly, as conditional_close does)."""
+    import gc
+    Z.init(0)
+    g = Z.Graph.gen_rmat(26, 24, seed=26, sampling_only=True)  # as bench.py builds it
+    e = O.gen_rmat(26, 24, seed=26)
+    assert np.array_equal(g.download_edges(), e)
+    og = O.OracleGraph(e, 1 << 26)
+    del e
+    gc.collect()
+    for kind, pat, n in ((Z.PROG_FOUR_CLIQUE, None, 1 << 13), (Z.PROG_PATTERN, STAR, 1 << 12),
+                         (Z.PROG_PATTERN, HOUSE, 1 << 12)):
+        p, op = Z.Program(kind, 0, pat), O.OracleProgram(kind, 0, pat)
+        first = 123456789
+        gt = p.run_debug(g, n, 9, stream_id=1, first_sample=first)
+        ot, oc = O.traces(og, op, n, 9, stream=1, first=first)
+        _assert_traces(gt, ot, "rmat26/%d" % kind)
+        _same_counters(p.run(g, n, 9, stream_id=1, first_sample=first), oc, "rmat26/%d" % kind)
