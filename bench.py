@@ -43,13 +43,22 @@ sys.path.insert(0, os.path.join(ROOT, "sampling-graph-mining_gb300"))
 METRIC = "time-to-1%-error@95% and samples/s, learned vs plain ELP, 1 GB300"
 RMAT = {"a": 0.57, "b": 0.19, "c": 0.19}
 WORKLOADS = {
-    "rmat20": {"scale": 20, "edge_factor": 3, "seed": 1, "samples": 1 << 26,
+    "rmat20": {"gen": "rmat", "scale": 20, "edge_factor": 3, "seed": 1, "samples": 1 << 26,
                "programs": ["triangle", "four_clique", "three_chain", "four_chain"]},
-    "rmat13": {"scale": 13, "edge_factor": 12, "seed": 1, "samples": 1 << 20, "programs": ["triangle"]},
+    "rmat13": {"gen": "rmat", "scale": 13, "edge_factor": 12, "seed": 1, "samples": 1 << 20, "programs": ["triangle"]},
+    # the Chung-Lu batch's base graph (1.7 GB of device arrays, far above the L2): the four programs
+    # alone, for HBM-bound kernel measurements
+    "chunglu4": {"gen": "chung_lu", "n": 4800000, "exponent": 2.3, "avg_degree": 18.0, "seed": 2024,
+                 "max_weight": 100, "weight_seed": 7, "samples": 1 << 26,
+                 "programs": ["triangle", "four_clique", "three_chain", "four_chain"]},
 }
 BATCH_WORKLOADS = {
     "rmat26": {"gen": "rmat", "scale": 26, "edge_factor": 24, "seed": 26, "samples": 1 << 30,
                "programs": ["four_clique", "five_star", "five_house"]},
+    # the headline's programs on R-MAT scale 21 (a few GB on the device): the size an ncu capture of
+    # the batch kernels can take, scaled to the headline by samples
+    "rmat21_batch": {"gen": "rmat", "scale": 21, "edge_factor": 24, "seed": 26, "samples": 1 << 26,
+                     "programs": ["four_clique", "five_star", "five_house"]},
     "chunglu_batch": {"gen": "chung_lu", "n": 4800000, "exponent": 2.3, "avg_degree": 18.0, "seed": 2024,
                       "max_weight": 100, "queries": 512},
 }
@@ -71,6 +80,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-time-to-bound", action="store_true")
     ap.add_argument("--no-coverage", action="store_true")
+    ap.add_argument("--l2-fetch", type=int, default=0,
+                    help="L2 fetch granularity in bytes for this process (32, 64, 128; 0: the library's)")
     ap.add_argument("--variants", default=None,
                     help="fixed launch shapes instead of tuning, e.g. triangle=4,four_clique=3 "
                          "(profiling runs: no tuner probe launches)")
@@ -162,18 +173,15 @@ def profile_traffic(kernel, workload, layout):
 
 def workload_config(name, m):
     """The workload as both arms print it (same dict, so the two lines compare like for like)."""
-    if name in BATCH_WORKLOADS and BATCH_WORKLOADS[name]["gen"] == "rmat":
-        wl = BATCH_WORKLOADS[name]
-        desc = ("%s: R-MAT scale %d, edge factor %d, a/b/c/d=.57/.19/.19/.05, seed %d, simplified (%d undirected "
-                "edges); one step = %s estimators x 2^%d samples each"
-                % (name, wl["scale"], wl["edge_factor"], wl["seed"], m, " + ".join(wl["programs"]),
-                   wl["samples"].bit_length() - 1))
+    wl = BATCH_WORKLOADS.get(name) or WORKLOADS[name]
+    if wl["gen"] == "rmat":
+        graph = "R-MAT scale %d, edge factor %d, a/b/c/d=.57/.19/.19/.05, seed %d" % (wl["scale"], wl["edge_factor"],
+                                                                                   wl["seed"])
     else:
-        wl = WORKLOADS[name]
-        desc = ("%s: R-MAT scale %d, edge factor %d, a/b/c/d=.57/.19/.19/.05, seed %d, simplified (%d undirected "
-                "edges); one step = %s estimators x 2^%d samples each"
-                % (name, wl["scale"], wl["edge_factor"], wl["seed"], m, " + ".join(wl["programs"]),
-                   wl["samples"].bit_length() - 1))
+        graph = "Chung-Lu %d vertices, exponent %.1f, average degree %.0f, seed %d" % (wl["n"], wl["exponent"],
+                                                                                     wl["avg_degree"], wl["seed"])
+    desc = ("%s: %s, simplified (%d undirected edges); one step = %s estimators x 2^%d samples each"
+            % (name, graph, m, " + ".join(wl["programs"]), wl["samples"].bit_length() - 1))
     return {"workload": desc, "inputs": "graph built before the timed steps and kept resident (GPU arm: device memory, L2 flushed "
                                            "between steps)"}
 
@@ -232,11 +240,11 @@ def run_reference(args):
         return
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
-    if args.workload in BATCH_WORKLOADS and BATCH_WORKLOADS[args.workload]["gen"] != "rmat":
-        print(json.dumps({"impl": "reference", "unavailable": "the Chung-Lu batch has no CPU arm: the reference runs "
-                          "one query at a time; see the rmat26 and rmat20 workloads' reference arms"}), flush=True)
-        return
     wl = BATCH_WORKLOADS.get(args.workload) or WORKLOADS[args.workload]
+    if wl["gen"] != "rmat":
+        print(json.dumps({"impl": "reference", "unavailable": "the Chung-Lu workloads have no CPU arm (the oracle's "
+                          "host generator is R-MAT's); see the rmat26 and rmat20 workloads' reference arms"}), flush=True)
+        return
     threads = os.cpu_count() or 1
     t0 = time.perf_counter()
     edges = O.gen_rmat(wl["scale"], wl["edge_factor"], RMAT["a"], RMAT["b"], RMAT["c"], wl["seed"])
@@ -342,11 +350,17 @@ def run_gb300(args):
     torch.cuda.set_device(local)
     import zgraph as Z
     Z.init(local)
+    l2_fetch = Z.set_l2_fetch_granularity(args.l2_fetch)
     wl = WORKLOADS[args.workload]
     n = wl["samples"]
-    nv = 1 << wl["scale"]
     t0 = time.perf_counter()
-    g = Z.Graph.gen_rmat(wl["scale"], wl["edge_factor"], RMAT["a"], RMAT["b"], RMAT["c"], wl["seed"])
+    if wl["gen"] == "rmat":
+        nv = 1 << wl["scale"]
+        g = Z.Graph.gen_rmat(wl["scale"], wl["edge_factor"], RMAT["a"], RMAT["b"], RMAT["c"], wl["seed"])
+    else:
+        nv = wl["n"]
+        g = Z.Graph.gen_chung_lu(wl["n"], wl["exponent"], wl["avg_degree"], seed=wl["seed"],
+                                 max_weight=wl["max_weight"], weight_seed=wl["weight_seed"])
     torch.cuda.synchronize()
     build_s = time.perf_counter() - t0
     names = wl["programs"]
@@ -451,27 +465,31 @@ def run_gb300(args):
                      "closure_checks_per_sample": closures[name], "closure_checks_per_s": closures[name] * n / t,
                      "hits": int(res[j].hits), "estimate": res[j].estimate})
     dom = max(kern, key=lambda k: k["ms"])
-    # The graph's sampling working set is about the L2 size, so the bound is the L2 read bandwidth
-    # (measured live); the DRAM figure says how much of it came from HBM.
-    roofline = {"bound": "l2", "achieved": dom["touched_gbs"], "peak": l2_gbs, "unit": "GB/s",
-                "frac": dom["touched_gbs"] / l2_gbs, "kernel": dom["kernel"],
+    # A graph whose sampling working set is about the L2 size (R-MAT scale 20) is bound by the L2
+    # read bandwidth (measured live); a larger one by HBM.  The DRAM figure says how much came from HBM.
+    near_l2 = g.meta().device_bytes < (1 << 30)
+    bpeak = l2_gbs if near_l2 else hbm
+    roofline = {"bound": "l2" if near_l2 else "hbm", "achieved": dom["touched_gbs"], "peak": bpeak, "unit": "GB/s",
+                "frac": dom["touched_gbs"] / bpeak, "kernel": dom["kernel"],
                 "traffic": dom["dram_bytes_per_sample"] * n if dom["dram_bytes_per_sample"] else None,
                 "traffic_source": dom["dram_source"],
                 "algorithmic_bytes": "zg_touch_sectors: 32-byte sectors the kernel's loads touch, per sample x samples",
-                "peak_source": "measured live: reads of a 48 MiB buffer resident in L2 (zg_read_bandwidth)",
+                "peak_source": ("measured live: reads of a 48 MiB buffer resident in L2 (zg_read_bandwidth)" if near_l2
+                                else hbm_src),
+                "l2": {"peak": l2_gbs, "frac": dom["touched_gbs"] / l2_gbs},
                 "hbm": {"peak": hbm, "peak_source": hbm_src,
                         "dram_frac": dom["dram_gbs"] / hbm if dom["dram_gbs"] else None},
                 "per_kernel": kern}
-    exact = {}
-    acc = {}
-    for j, name in enumerate(names):
-        ex = g.exact_count(EXACT_IDS[name])
-        exact[name] = ex
-        acc[name] = {"exact": ex, "estimate": res[j].estimate, "rel_err": abs(res[j].estimate - ex) / ex if ex else None}
-    if "four_clique" in names:
-        exact["four_clique_unbiased"] = exact["four_clique"]
+    exact, acc = {}, {}
     ttb = None
     if not args.no_time_to_bound:
+        for j, name in enumerate(names):
+            ex = g.exact_count(EXACT_IDS[name])
+            exact[name] = ex
+            acc[name] = {"exact": ex, "estimate": res[j].estimate,
+                         "rel_err": abs(res[j].estimate - ex) / ex if ex else None}
+        if "four_clique" in names:
+            exact["four_clique_unbiased"] = exact["four_clique"]
         ttb = time_to_bound(Z, g, [x for x in ("triangle", "four_clique_unbiased") if x in exact], exact)
         if not args.no_coverage:
             ttb["coverage"] = coverage(Z, g, exact, names=[x for x in ("triangle", "four_clique_unbiased") if x in exact])
@@ -481,7 +499,8 @@ def run_gb300(args):
             "data": "synthetic (seeded R-MAT, generated on the device)",
             "config": workload_config(args.workload, g.num_local_edges),
             "setup": {"graph_gen_and_build_s": round(build_s, 3), "graph_device_bytes": int(g.meta().device_bytes),
-                      "record_layout": layout, "launch_tuning": tuning},
+                      "record_layout": layout, "launch_tuning": tuning,
+                      "l2_fetch_bytes": args.l2_fetch or l2_fetch},
             "e2e": e2e, "gpu_launches": 2 * len(progs) * args.steps, "clocks": clk, "roofline": roofline,
             "accuracy": acc, "time_to_bound": ttb}
     if not args.no_cpu_baseline and world == 1:
@@ -523,6 +542,7 @@ def run_batch(args):
     wl = BATCH_WORKLOADS[args.workload]
     Z.init(0)
     torch.cuda.set_device(0)
+    l2_fetch = Z.set_l2_fetch_granularity(args.l2_fetch)
     t0 = time.perf_counter()
     rmat = wl["gen"] == "rmat"
     if not rmat:
@@ -586,7 +606,7 @@ def run_batch(args):
             "config": config,
             "setup": {"graph_gen_and_build_s": round(gen_s, 3), "graph_device_bytes": int(g.meta().device_bytes),
                       "record_layout": layout, "queries_per_step": len(qs), "samples_per_step": samples,
-                      "first_batch_s": round(first_s, 3), "batch_variant": best,
+                      "first_batch_s": round(first_s, 3), "batch_variant": best, "l2_fetch_bytes": args.l2_fetch or l2_fetch,
                       "ms_per_variant": [round(x, 3) for x in ms_variants]},
             "e2e": {"value": samples * args.steps / sum(wall), "unit": "samples/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "queries_per_s": len(qs) * args.steps / sum(wall),

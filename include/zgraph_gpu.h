@@ -141,6 +141,10 @@ int zg_version(void);
 int zg_init(int device);
 /* Human-readable text of the last error on this thread. */
 const char* zg_last_error(void);
+/* The current device's L2 fetch granularity hint (cudaLimitMaxL2FetchGranularity: 32, 64 or 128
+ * bytes fetched from memory per L2 miss; 0 leaves it as it is), for this process's context only.
+ * *previous (may be NULL) receives the value before the call.  No counterpart in the reference. */
+int zg_set_l2_fetch_granularity(uint32_t bytes, uint32_t* previous);
 
 /* ---- graph store -------------------------------------------------------- */
 /* Uploads a COO edge list in edge-id order (edge id == position, src/Graph.cpp:295-306) and
@@ -242,9 +246,11 @@ int zg_run_noalloc(const zg_graph* g, const zg_program* p, uint64_t n, uint64_t 
 /* Autotuner (no counterpart in the reference, whose thread count comes from libnuma).  Each
  * program kind has ZG_VARIANTS launch shapes: the sampling kernel compiled for
  * min-blocks-per-SM 1, 2, 3, 4, 5, 6, 8 (register caps 255/128/80/64/48/40/32) with a grid of
- * occupancy x SM count.  zg_tune times every variant on g (probe_samples estimators, best of 3)
- * and keeps the fastest for this device and kind; ms_per_variant (may be NULL) receives
- * ZG_VARIANTS timings.  zg_set_variant / zg_get_variant fix or read the choice. */
+ * occupancy x SM count; the 4-chain's shapes with at most 3 blocks per SM interleave two samples
+ * per thread (more registers, two load chains in flight), the others run one.  zg_tune times every
+ * variant on g (probe_samples estimators, best of 3) and keeps the fastest for this device and
+ * kind; ms_per_variant (may be NULL) receives ZG_VARIANTS timings.  zg_set_variant /
+ * zg_get_variant fix or read the choice. */
 #define ZG_VARIANTS 7
 int zg_tune(const zg_graph* g, const zg_program* p, uint64_t probe_samples, void* cuda_stream,
             int* best_variant, float* ms_per_variant);

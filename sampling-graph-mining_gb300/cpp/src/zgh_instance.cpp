@@ -542,6 +542,13 @@ void CachedSubPatterns<E>::materialise() {
   std::vector<zg_sample_trace> tr(n ? n : 1);
   if (n) zgh::check(zg_run_debug(device_graph_, source_->device_program(), n, 0, seed_, stream_, tr.data()), "zg_run_debug");
   Random& rnd = source_->randoms[0];
+  // a replay: the primitives below run on the device trace's draws
+  struct ReplayScope {
+    bool& flag;
+    bool was;
+    explicit ReplayScope(bool& f) : flag(f), was(f) { flag = true; }
+    ~ReplayScope() { flag = was; }
+  } scope(source_->validating_);
   for (unsigned long long i = 0; i < n; ++i) {
     Random::Draw d[ZG_MAX_DRAWS];
     for (uint32_t k = 0; k < tr[i].ndraws && k < ZG_MAX_DRAWS; ++k) d[k] = {tr[i].lo[k], tr[i].hi[k], tr[i].val[k]};

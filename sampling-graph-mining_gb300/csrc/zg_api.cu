@@ -94,6 +94,16 @@ extern "C" int zg_init(int device) {
   return ZG_OK;
 }
 
+extern "C" int zg_set_l2_fetch_granularity(uint32_t bytes, uint32_t* previous) {
+  if (bytes != 0 && bytes != 32 && bytes != 64 && bytes != 128)
+    return zg_set_error(ZG_ERR_INVALID_ARG, "L2 fetch granularity %u: 0, 32, 64 or 128", bytes), ZG_ERR_INVALID_ARG;
+  size_t old = 0;
+  ZG_CUDA(cudaDeviceGetLimit(&old, cudaLimitMaxL2FetchGranularity));
+  if (previous) *previous = (uint32_t)old;
+  if (bytes) ZG_CUDA(cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, bytes));
+  return ZG_OK;
+}
+
 // ---- programs ---------------------------------------------------------------------------
 static uint32_t pair_bit_host(uint32_t i, uint32_t j, uint32_t pv) {
   if (i > j) std::swap(i, j);

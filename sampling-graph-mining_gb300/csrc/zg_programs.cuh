@@ -846,6 +846,125 @@ __device__ __forceinline__ bool canonical(const uint32_t* es, const uint32_t* ed
   return true;
 }
 
+
+// Two 4-chain samples of the same program (sel, already drawn by the caller) per thread, their
+// dependent-load chains interleaved stage by stage so that each stage's loads of both samples are
+// in flight together: the same draws, tests and weights as prog_four_chain<false> on each.
+template <int N>
+__device__ __forceinline__ void prog_four_chain_n(const ZgDevGraph& g, Ctx (&c)[N], Res (&r)[N], uint32_t sel) {
+  uint64_t w2[N], w3[N], e0[N];
+  uint4 q[N], qp[N];
+  bool live[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    w2[i] = c[i].word(2);
+    w3[i] = c[i].word(3);
+    ++c[i].nd;  // the program draw
+    res_mul(r[i], 3);
+    live[i] = g.m != 0;
+    if (!live[i]) r[i].fail = true;
+  }
+#pragma unroll
+  for (int i = 0; i < N; ++i)
+    if (live[i]) {
+      e0[i] = c[i].draw(0, g.m - 1);
+      res_mul(r[i], g.m);
+      edge_rec(g, e0[i], q[i], qp[i]);
+    }
+  if (sel == 3) {  // vertices [a] give e1, vertices [b] give e2: both loads at once
+    uint2 e1[N], e2[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+      if (live[i]) {
+        const uint64_t S1 = q[i].z, S2 = q[i].w;
+        if (S1 == 0 || S2 == 0) {
+          r[i].fail = true;
+          live[i] = false;
+          continue;
+        }
+        const uint64_t r1 = c[i].take(w2[i], 0, S1 - 1), r2 = c[i].take(w3[i], 0, S2 - 1);
+        e1[i] = ZG_LDG(&g.adj_e[after_edge(g, q[i], qp[i], false) + (uint32_t)r1]);
+        e2[i] = ZG_LDG(&g.adj_e[after_edge(g, q[i], qp[i], true) + (uint32_t)r2]);
+        res_mul(r[i], S1);
+        res_mul(r[i], S2);
+      }
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+      if (live[i]) {
+        const uint32_t a = q[i].x, b = q[i].y;
+        if (e1[i].x == a) r[i].shift++;
+        if (e2[i].x == b) r[i].shift++;
+        r[i].hit = !(b == a || b == e1[i].x) && !(e2[i].x == a || e2[i].x == e1[i].x);
+      }
+    return;
+  }
+  // sel 1, 2: vertices [a, b] give e1; its far end v2 gives e2
+  uint2 e1[N];
+  uint32_t v2[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i)
+    if (live[i]) {
+      const uint64_t S1 = (uint64_t)q[i].z + q[i].w;
+      if (S1 == 0) {
+        r[i].fail = true;
+        live[i] = false;
+        continue;
+      }
+      uint64_t r1 = c[i].take(w2[i], 0, S1 - 1);
+      const bool on_b = r1 >= q[i].z;
+      if (on_b) r1 -= q[i].z;
+      e1[i] = ZG_LDG(&g.adj_e[after_edge(g, q[i], qp[i], on_b) + (uint32_t)r1]);
+      res_mul(r[i], S1);
+      v2[i] = on_b ? q[i].y : q[i].x;  // the anchor, resolved below
+    }
+  EdgeAt a1v[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i)
+    if (live[i]) {
+      const uint32_t a = q[i].x, b = q[i].y, anchor = v2[i];
+      if (e1[i].x == a || e1[i].x == b) r[i].shift++;
+      // the second step's anchor: the vertex of e1 not shared with e0 (FourChain.cpp:44-54)
+      uint32_t v;
+      if (a == anchor) v = e1[i].x;
+      else if (a == e1[i].x) v = anchor;
+      else if (b == anchor) v = e1[i].x;
+      else v = anchor;
+      v2[i] = v;
+      a1v[i] = edge_at(g, e1[i].y, v);  // e1 in v's list
+    }
+  uint32_t lb2[N], end2[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i)
+    if (live[i]) {
+      lb2[i] = a1v[i].pos + 1;  // sel 1: min_valid = id1 + 1
+      end2[i] = lb2[i] + a1v[i].suf;
+      if (sel == 2)  // min_valid = id0 + 1, at or before e1's own slot in v2's list
+        lb2[i] = lb_eid_win(g.adj_e, edge_at_start(g, a1v[i], v2[i]), lb2[i], (uint32_t)e0[i] + 1, 0u, e1[i].y);
+    }
+  uint2 e2[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i)
+    if (live[i]) {
+      const uint64_t S2 = (uint64_t)(end2[i] - lb2[i]);
+      if (S2 == 0) {
+        r[i].fail = true;
+        live[i] = false;
+        continue;
+      }
+      const uint64_t r2 = c[i].take(w3[i], 0, S2 - 1);
+      e2[i] = ZG_LDG(&g.adj_e[lb2[i] + (uint32_t)r2]);
+      res_mul(r[i], S2);
+    }
+#pragma unroll
+  for (int i = 0; i < N; ++i)
+    if (live[i]) {
+      const uint32_t a = q[i].x, b = q[i].y;
+      if (e2[i].x == v2[i]) r[i].shift++;
+      bool ok = !(v2[i] == a || v2[i] == b) && !(e2[i].x == a || e2[i].x == b);
+      if (sel == 2) ok = ok && !(e2[i].y >= e1[i].y);
+      r[i].hit = ok;
+    }
+}
 // ---- ChainMining: applications/ChainMining.cpp:240-84 ------------------------------------
 template <bool DBG>
 __device__ void prog_chain(const ZgDevGraph& g, int order, Ctx& c, Res& r) {
@@ -1012,9 +1131,13 @@ __device__ void prog_pattern_small(const ZgDevGraph& g, const ZgProgParams& pp, 
     ++ne;
     if (nbr_slot < 0) {
       if (nvtx >= MV) return;  // more vertices than the pattern (pv <= MV): not a hit
-      const EdgeAt ae = edge_at(g, e.y, e.x);  // e in the new vertex's list
-      const uint32_t nve = ae.pos + 1 + ae.suf;
-      const uint32_t nvl = lb_eid(g.adj_e, edge_at_start(g, ae, e.x), ae.pos + 1, mv, 0u, e.y);
+      // the new vertex's list range past min_valid: needed only if another step draws from it
+      uint32_t nve = 0, nvl = 0;
+      if ((uint32_t)k + 1 < pp.pe) {
+        const EdgeAt ae = edge_at(g, e.y, e.x);  // e in the new vertex's list
+        nve = ae.pos + 1 + ae.suf;
+        nvl = lb_eid(g.adj_e, edge_at_start(g, ae, e.x), ae.pos + 1, mv, 0u, e.y);
+      }
 #pragma unroll
       for (int i = 0; i < MV; ++i)
         if (i == nvtx) {

@@ -12,21 +12,35 @@
 
 ZgProgParams zg_prog_params(const zg_program* p);
 
+int zg_get_variant(int kind, int* variant, int* min_blocks, int* grid);
+
 namespace {
+
+// The counting copy of k_sample under its own name (profiles tell the two apart).
+template <int KIND, int MINB, int LAYOUT>
+__global__ void __launch_bounds__(kBlock, MINB)
+    k_sample_touch(ZgDevGraph g, ZgProgParams pp, uint64_t n, uint64_t first, uint64_t seed,
+                   const __grid_constant__ ZgKeys keys, uint32_t stream, ZgPartial* __restrict__ partials) {
+  sample_loop<KIND, MINB, LAYOUT>(g, pp, n, first, seed, keys, stream, partials);
+}
 
 typedef void (*TouchKernel)(ZgDevGraph, ZgProgParams, uint64_t, uint64_t, uint64_t, const ZgKeys, uint32_t,
                             ZgPartial*);
 
+// Every program's loads are the same under every launch shape except the 4-chain's, whose shapes
+// with at most 3 resident blocks interleave two samples per lane: that one follows the shape the
+// production kernel uses.
 template <int LAYOUT>
-TouchKernel touch_kernel(int kind) {
+TouchKernel touch_kernel(int kind, bool paired) {
   switch (kind) {
-    case ZG_PROG_TRIANGLE: return k_sample<ZG_PROG_TRIANGLE, 4, LAYOUT>;
-    case ZG_PROG_FOUR_CLIQUE: return k_sample<ZG_PROG_FOUR_CLIQUE, 4, LAYOUT>;
-    case ZG_PROG_FOUR_CLIQUE_UNBIASED: return k_sample<ZG_PROG_FOUR_CLIQUE_UNBIASED, 4, LAYOUT>;
-    case ZG_PROG_THREE_CHAIN: return k_sample<ZG_PROG_THREE_CHAIN, 4, LAYOUT>;
-    case ZG_PROG_FOUR_CHAIN: return k_sample<ZG_PROG_FOUR_CHAIN, 4, LAYOUT>;
-    case ZG_PROG_CHAIN: return k_sample<ZG_PROG_CHAIN, 4, LAYOUT>;
-    default: return k_sample<ZG_PROG_PATTERN, 4, LAYOUT>;
+    case ZG_PROG_TRIANGLE: return k_sample_touch<ZG_PROG_TRIANGLE, 4, LAYOUT>;
+    case ZG_PROG_FOUR_CLIQUE: return k_sample_touch<ZG_PROG_FOUR_CLIQUE, 4, LAYOUT>;
+    case ZG_PROG_FOUR_CLIQUE_UNBIASED: return k_sample_touch<ZG_PROG_FOUR_CLIQUE_UNBIASED, 4, LAYOUT>;
+    case ZG_PROG_THREE_CHAIN: return k_sample_touch<ZG_PROG_THREE_CHAIN, 4, LAYOUT>;
+    case ZG_PROG_FOUR_CHAIN:
+      return paired ? k_sample_touch<ZG_PROG_FOUR_CHAIN, 2, LAYOUT> : k_sample_touch<ZG_PROG_FOUR_CHAIN, 4, LAYOUT>;
+    case ZG_PROG_CHAIN: return k_sample_touch<ZG_PROG_CHAIN, 4, LAYOUT>;
+    default: return k_sample_touch<ZG_PROG_PATTERN, 4, LAYOUT>;
   }
 }
 
@@ -39,7 +53,15 @@ extern "C" int zg_touch_sectors(const zg_graph* g, const zg_program* p, uint64_t
     return zg_set_error(ZG_ERR_INVALID_ARG, "zg_touch_sectors: n must be in [1, 2^32]"), ZG_ERR_INVALID_ARG;
   cudaStream_t s = (cudaStream_t)cuda_stream;
   const int layout = g->wide ? 1 : g->packed ? 2 : 0;
-  TouchKernel k = layout == 1 ? touch_kernel<1>(p->kind) : layout == 2 ? touch_kernel<2>(p->kind) : touch_kernel<0>(p->kind);
+  int mb = 4;
+  if (p->kind == ZG_PROG_FOUR_CHAIN) {
+    int rc = zg_get_variant(ZG_PROG_FOUR_CHAIN, nullptr, &mb, nullptr);
+    if (rc) return rc;
+  }
+  const bool paired = mb <= 3;
+  TouchKernel k = layout == 1   ? touch_kernel<1>(p->kind, paired)
+                  : layout == 2 ? touch_kernel<2>(p->kind, paired)
+                                : touch_kernel<0>(p->kind, paired);
   int per_sm = 0;
   ZG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kBlock, 0));
   uint64_t need = (n + kBlock - 1) / kBlock;

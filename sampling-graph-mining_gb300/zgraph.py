@@ -186,6 +186,7 @@ def lib():
             "zg_batch_elapsed_ms": ([P, C.POINTER(C.c_float)], I32),
             "zg_read_bandwidth": ([U64, U32, P, C.POINTER(D)], I32),
             "zg_touch_sectors": ([P, P, U64, U64, U64, U32, P, C.POINTER(U64)], I32),
+            "zg_set_l2_fetch_granularity": ([U32, C.POINTER(U32)], I32),
             "zg_exact_count_weighted": ([P, I32, U32, P, P], I32),
             "zg_conditional_close": ([P, P, U32, P, P], I32),
             "zg_bound_half_width": ([D, D, U64, U64, D, D, D, C.POINTER(D), C.POINTER(U32), C.POINTER(U32)], I32),
@@ -400,6 +401,14 @@ def set_record_layout(layout):
     (RECORDS_AUTO, RECORDS_COMPACT, RECORDS_WIDE or RECORDS_PACKED); estimates are identical under
     each."""
     check(lib().zg_set_record_layout(layout))
+
+
+def set_l2_fetch_granularity(nbytes):
+    """zg_set_l2_fetch_granularity: the bytes the L2 fetches per miss on the current device (0: keep);
+    returns the previous value."""
+    prev = C.c_uint32()
+    check(lib().zg_set_l2_fetch_granularity(nbytes, C.byref(prev)))
+    return prev.value
 
 
 def read_bandwidth(nbytes, reps=200, cuda_stream=None):
