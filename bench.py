@@ -18,7 +18,9 @@ replayed through a CUDA graph).
   cpu_baseline: the oracle (CPU restatement of the reference path, all host threads) on the same
           graph, a bounded sample of each program.
   time_to_bound: triangle and unbiased 4-clique queries to 1 % at 95 %, plain ErrorProfile sizing
-          vs learned sizing, the same empirical bound check; coverage over 40 seeds on R-MAT scale 20.
+          vs learned sizing, the same bound check on the same estimators (2 seeds each; the
+          triangle's exact count on the device beside it); on R-MAT scale 20 the same comparison
+          (3 seeds) and the coverage of 40 independent learned answers of each.
 
 --impl reference times the oracle (the reference's CPU path restated in C, all host threads) on
 the same workload and graph, generated on the host by oracle/zgo_gen.c without the GPU library.
@@ -296,11 +298,13 @@ def touch_bytes(Z, g, progs, names, seed, n=1 << 20):
     return {name: p.touch_bytes_per_sample(g, n, seed) for name, p in zip(names, progs)}
 
 
-def time_to_bound(Z, g, names, exact, eps=0.01, conf=0.95, cap=1 << 37, seed=31):
-    """Time from query submission (graph resident) to an answer whose empirical 95 % half-width is
-    <= 1 % of the estimate: plain ErrorProfile sizing vs the learned network, the same bound check.
-    4-cliques run the unbiased canonical-path program: the reference's estimator finds ~60 % of the
-    cliques, so a tight interval around it is not an accuracy claim."""
+def time_to_bound(Z, g, names, exact, eps=0.01, conf=0.95, cap=1 << 37, seed=31, repeats=1):
+    """Time from query submission (graph resident) to an answer whose 95 % half-width is <= 1 % of
+    the estimate: plain ErrorProfile sizing vs the learned network, the same bound check, the same
+    estimators (common random numbers), `repeats` independent seeds per pattern (the speed-up is
+    the ratio of the mean times).  4-cliques run the unbiased canonical-path program: the
+    reference's estimator finds ~60 % of the cliques, so a tight interval around it is not an
+    accuracy claim."""
     import elp_learn as EL
     model = os.path.join(ROOT, "sampling-graph-mining_gb300", "elp_mlp.npz")
     if not os.path.exists(model):
@@ -309,12 +313,18 @@ def time_to_bound(Z, g, names, exact, eps=0.01, conf=0.95, cap=1 << 37, seed=31)
     out = {"eps": eps, "confidence": conf, "max_samples": cap, "model": "sampling-graph-mining_gb300/elp_mlp.npz",
            "patterns": {}}
     for name in names:
-        r = EL.compare(net, g, name, eps=eps, conf=conf, seed=seed, max_samples=cap)
+        runs = [EL.compare(net, g, name, eps=eps, conf=conf, seed=seed + 1000 * i, max_samples=cap)
+                for i in range(repeats)]
         ex = exact.get(name)
+        for r in runs:
+            for k in ("plain", "learned"):
+                r[k]["rel_err_vs_exact"] = abs(r[k]["estimate"] - ex) / ex if ex else None
+        r = dict(runs[0]) if repeats == 1 else {"pattern": name, "runs": runs}
         for k in ("plain", "learned"):
-            r[k]["rel_err_vs_exact"] = abs(r[k]["estimate"] - ex) / ex if ex else None
+            r["mean_seconds_" + k] = sum(x[k]["seconds"] for x in runs) / repeats
+            r["mean_samples_" + k] = sum(x[k]["samples"] for x in runs) / repeats
         r["exact"] = ex
-        r["speedup_learned_over_plain"] = r["plain"]["seconds"] / r["learned"]["seconds"]
+        r["speedup_learned_over_plain"] = r["mean_seconds_plain"] / r["mean_seconds_learned"]
         out["patterns"][name] = r
     return out
 
@@ -645,10 +655,14 @@ def run_batch(args):
                             "peak_source": hbm_src, "per_kernel": kern}
         line["results"] = {name: {"hits": int(c.hits), "estimate": c.estimate} for name, (c, _) in zip(names, res)}
         if not args.no_time_to_bound:
-            exact = {"triangle": None, "four_clique_unbiased": None}
-            line["time_to_bound"] = time_to_bound(Z, g, ["triangle", "four_clique_unbiased"], exact)
+            t1 = time.perf_counter()
+            exact = {"triangle": g.exact_count(EXACT_IDS["triangle"]), "four_clique_unbiased": None}
+            exact_s = time.perf_counter() - t1
+            line["time_to_bound"] = time_to_bound(Z, g, ["triangle", "four_clique_unbiased"], exact, repeats=2)
+            line["time_to_bound"]["exact_triangle_count"] = {"value": exact["triangle"], "seconds": exact_s,
+                                                            "kernel": "zg_exact_count (degree-oriented DAG)"}
             if not args.no_coverage:
-                line["time_to_bound"]["coverage"] = coverage_rmat20(Z)
+                line["time_to_bound"]["rmat20"] = rmat20_bounds(Z)
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(g.download_edges(), nv, names, os.cpu_count() or 1)
     else:
@@ -675,16 +689,18 @@ def run_batch(args):
     print(json.dumps(line), flush=True)
 
 
-def coverage_rmat20(Z):
-    """Coverage of the 1 %/95 % answers on R-MAT scale 20 (whose exact counts are cheap): triangle and
-    unbiased 4-clique, 40 seeds each, learned sizing + bound check."""
+def rmat20_bounds(Z):
+    """On R-MAT scale 20 (whose exact counts are cheap): plain vs learned time to the 1 %/95 % bound
+    for the triangle and the unbiased 4-clique (3 seeds each), and the coverage of 40 independent
+    learned answers of each."""
     wl = WORKLOADS["rmat20"]
     g = Z.Graph.gen_rmat(wl["scale"], wl["edge_factor"], RMAT["a"], RMAT["b"], RMAT["c"], wl["seed"],
                          sampling_only=False)
     exact = {"triangle": g.exact_count(EXACT_IDS["triangle"]),
              "four_clique_unbiased": g.exact_count(EXACT_IDS["four_clique"])}
-    out = coverage(Z, g, exact)
-    out["graph"] = "rmat20: R-MAT scale 20, edge factor 3, seed 1 (%d edges)" % g.num_local_edges
+    out = {"graph": "rmat20: R-MAT scale 20, edge factor 3, seed 1 (%d edges)" % g.num_local_edges}
+    out["time_to_bound"] = time_to_bound(Z, g, ["triangle", "four_clique_unbiased"], exact, repeats=3)
+    out["coverage"] = coverage(Z, g, exact)
     return out
 
 

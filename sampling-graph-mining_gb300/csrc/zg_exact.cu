@@ -141,20 +141,17 @@ __device__ __forceinline__ unsigned long long dag_edge(const uint32_t* __restric
 // one thread per oriented edge (u,v): keys sorted, so u = key >> 32; heavy edges are queued
 __global__ void __launch_bounds__(kB) k_dag_count(uint64_t m, const unsigned long long* __restrict__ keys,
                                                   const uint32_t* __restrict__ nbr, const int64_t* __restrict__ ooff,
-                                                  int kind, U128* __restrict__ parts, uint64_t* __restrict__ heavy,
-                                                  unsigned long long* __restrict__ nheavy, uint64_t heavy_cap) {
+                                                  int kind, U128* __restrict__ parts, uint32_t* __restrict__ heavy,
+                                                  unsigned long long* __restrict__ nheavy) {
   U128 acc = {0, 0};
   for (uint64_t e = blockIdx.x * (uint64_t)kB + threadIdx.x; e < m; e += (uint64_t)gridDim.x * kB) {
     unsigned long long k = keys[e];
     uint32_t u = (uint32_t)(k >> 32), v = (uint32_t)k;
     int64_t bu = ooff[u], eu = ooff[u + 1], bv = ooff[v], ev = ooff[v + 1];
     int64_t shorter = (eu - bu) < (ev - bv) ? (eu - bu) : (ev - bv);
-    if (shorter > kHeavy) {
-      unsigned long long slot = atomicAdd(nheavy, 1ull);
-      if (slot < heavy_cap) {
-        heavy[slot] = e;
-        continue;
-      }
+    if (shorter > kHeavy) {  // the queue holds every edge (m < 2^32)
+      heavy[atomicAdd(nheavy, 1ull)] = (uint32_t)e;
+      continue;
     }
     bool swap = (eu - bu) > (ev - bv);
     add128(acc, dag_edge(nbr, ooff, kind, bu, eu, bv, ev, swap ? bv : bu, 1));
@@ -163,7 +160,7 @@ __global__ void __launch_bounds__(kB) k_dag_count(uint64_t m, const unsigned lon
 }
 
 // one warp per queued edge, the lanes splitting its shorter out-list
-__global__ void __launch_bounds__(kB) k_dag_heavy(const uint64_t* __restrict__ heavy, uint64_t nheavy,
+__global__ void __launch_bounds__(kB) k_dag_heavy(const uint32_t* __restrict__ heavy, uint64_t nheavy,
                                                   const unsigned long long* __restrict__ keys,
                                                   const uint32_t* __restrict__ nbr, const int64_t* __restrict__ ooff,
                                                   int kind, U128* __restrict__ parts) {
@@ -244,10 +241,9 @@ int dag_count(const zg_graph* g, int kind, int pred, uint32_t t, cudaStream_t s,
   Dev k1, k2, od, ooff, tmp, parts, hv, nh;
   int rc;
   int grid = zg_num_sms() * 8;
-  const uint64_t heavy_cap = m < (1ull << 26) ? m : (1ull << 26);
   if ((rc = alloc(k1, 8 * m)) || (rc = alloc(k2, 8 * m)) || (rc = alloc(od, 8 * ((size_t)nv + 1))) ||
       (rc = alloc(ooff, 8 * ((size_t)nv + 1))) || (rc = alloc(parts, sizeof(U128) * 2 * grid)) ||
-      (rc = alloc(hv, 8 * heavy_cap)) || (rc = alloc(nh, 8)))
+      (rc = alloc(hv, 4 * m)) || (rc = alloc(nh, 8)))
     return rc;
   cudaMemsetAsync(od.p, 0, 8 * ((size_t)nv + 1), s);
   cudaMemsetAsync(nh.p, 0, 8, s);
@@ -280,13 +276,12 @@ int dag_count(const zg_graph* g, int kind, int pred, uint32_t t, cudaStream_t s,
   uint32_t* nbr = (uint32_t*)k1.p;
   k_low32<<<grid, kB, 0, s>>>((const unsigned long long*)k2.p, mk, nbr);
   k_dag_count<<<grid, kB, 0, s>>>(mk, (const unsigned long long*)k2.p, nbr, (const int64_t*)ooff.p, kind,
-                                  (U128*)parts.p, (uint64_t*)hv.p, (unsigned long long*)nh.p, heavy_cap);
+                                  (U128*)parts.p, (uint32_t*)hv.p, (unsigned long long*)nh.p);
   unsigned long long nheavy = 0;
   ce = cudaMemcpyAsync(&nheavy, nh.p, 8, cudaMemcpyDeviceToHost, s);
   if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
   if (ce != cudaSuccess) return zg_check_cuda(ce, "exact count kernel");
-  if (nheavy > heavy_cap) nheavy = heavy_cap;  // the rest ran in their own threads
-  k_dag_heavy<<<grid, kB, 0, s>>>((const uint64_t*)hv.p, nheavy, (const unsigned long long*)k2.p, nbr,
+  k_dag_heavy<<<grid, kB, 0, s>>>((const uint32_t*)hv.p, nheavy, (const unsigned long long*)k2.p, nbr,
                                   (const int64_t*)ooff.p, kind, (U128*)parts.p + grid);
   ce = cudaGetLastError();
   if (ce != cudaSuccess) return zg_check_cuda(ce, "exact count kernel");
