@@ -90,18 +90,23 @@ __device__ __forceinline__ void batch_item(const BatchQuery& sq, uint32_t chunk,
   Acc a, at;
   acc_init(a);
   acc_init(at);
+  // The sums of a (the 3-motif's triangle sums stay in at) live in shared-memory slots, as in
+  // k_sample's long programs: the registers they free let more warps stay resident without
+  // spilling (each thread adds its hits in the same order, so the sums are the same).
+  __shared__ AccSlots<kBB> sl;
+  acc_slots_init(sl);
   for (uint64_t i = lo + threadIdx.x; i < hi; i += kBB) {
     Ctx c{sq.seed, sq.first + i, sq.stream, 0, nullptr, 0};
     Res r;
     res_init(r);
     if (PATTERN) {
       prog_pattern<false>(sq.g, sq.pp, c, r);
-      acc_add(a, r, sq.pp.den_log2);
+      acc_add_slots(a, sl, r, sq.pp.den_log2);
     } else if (motif) {
       Res rt;
       res_init(rt);
       motif_sample(sq.g, c, r, rt);
-      acc_add(a, r, 1);
+      acc_add_slots(a, sl, r, 1);
       acc_add(at, rt, 1);
     } else {
       switch (sq.pp.kind) {
@@ -112,9 +117,10 @@ __device__ __forceinline__ void batch_item(const BatchQuery& sq, uint32_t chunk,
         case ZG_PROG_FOUR_CHAIN: prog_four_chain<false>(sq.g, c, r); break;
         default: prog_chain<false>(sq.g, (int)sq.pp.param, c, r); break;  // ZG_PROG_CHAIN
       }
-      acc_add(a, r, sq.pp.den_log2);
+      acc_add_slots(a, sl, r, sq.pp.den_log2);
     }
   }
+  acc_from_slots(a, sl);
   const uint64_t slot = 2 * (sq.slot0 + chunk);
   block_reduce_store<kBB>(a, &parts[slot]);
   __syncthreads();
