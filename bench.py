@@ -652,6 +652,12 @@ def run_batch(args):
                             "algorithmic_bytes": "zg_touch_sectors: 32-byte sectors the production kernels' loads "
                                                  "touch per sample (%s) x 2^30 samples per program"
                                                  % {k: round(v, 1) for k, v in touched.items()},
+                            "dram": ({"gbs": dram_ps * samples / (total_ms / args.steps / 1000.0) / 1e9,
+                                      "frac": dram_ps * samples / (total_ms / args.steps / 1000.0) / 1e9 / hbm,
+                                      "note": "DRAM bytes with the default 128-byte L2 fills; the kernels are bound "
+                                              "by load latency (the same time with 32-byte fills at the touched "
+                                              "bytes)"} if dram_ps else None),
+                            "bound_note": "latency of each sample's dependent loads (profiles/k_batch_pattern_rmat21.md)",
                             "peak_source": hbm_src, "per_kernel": kern}
         line["results"] = {name: {"hits": int(c.hits), "estimate": c.estimate} for name, (c, _) in zip(names, res)}
         if not args.no_time_to_bound:
