@@ -113,7 +113,8 @@ typedef struct zg_counters {
   double   sum_w2;         /* sum of (1/p)^2 in double (fixed block order); each 1/p
                               truncated to 53 bits first: the variance term          */
   double   estimate;       /* exact mean, rounded once to double                    */
-  double   reserved;
+  double   sum_w4;         /* sum of (1/p)^4 in double (fixed block order): the
+                              uncertainty of the variance term                     */
 } zg_counters;
 
 /* Per-sample trace written by zg_run_debug: the draws a replayed Random::rand_int(min,max)
@@ -436,20 +437,26 @@ typedef struct zg_query_result {
  * the empirical CLT one, z * sqrt(var / n) (from 30 hits on), or the empirical Bernstein one
  * (Audibert, Munos, Szepesvari 2009: for values in [0, R], with probability >= 1 - delta,
  * |mean - mu| <= sqrt(2 var ln(3/delta) / n) + 3 R ln(3/delta) / n, var the empirical variance),
- * whichever is smaller; below 30 hits only the Bernstein one.  R bounds one estimator's weight:
+ * whichever is smaller; below 30 hits only the Bernstein one.  The CLT one takes an upper
+ * confidence bound on the variance from the fourth moment (zg_bound_half_width).  R bounds one
+ * estimator's weight:
  * m * prod over the conditional steps i = 1.. of min((i + 1) * max_degree, 2m) (x 3 for the
  * 4-chain).  Each further round runs what the observed variance needs, with headroom
  * 1 + 0.5 / sqrt(hits). */
 int zg_query(const zg_graph* g, const zg_program* p, double error, double confidence,
              uint64_t n_initial, uint64_t max_samples, uint64_t seed, uint32_t stream_id,
              void* cuda_stream, zg_query_result* out);
-/* The check zg_query applies to a running estimate (host arithmetic only, no device): mean and
- * empirical (1/n) variance of n estimators with `hits` non-zero ones, each in [0, weight_range].
- * *half_width gets the half-width at `confidence` (CLT from 30 hits on, or Bernstein, whichever is
- * smaller; Bernstein alone below 30 hits), *method the bound it came from, *met whether
- * half_width <= error * mean. */
-int zg_bound_half_width(double mean, double var, uint64_t n, uint64_t hits, double error, double confidence,
-                        double weight_range, double* half_width, uint32_t* method, uint32_t* met);
+/* The check zg_query applies to a running estimate (host arithmetic only, no device): mean,
+ * empirical (1/n) variance and empirical mean of w^4 (fourth_moment; 0: unknown) of n estimators
+ * with `hits` non-zero ones, each in [0, weight_range].  *half_width gets the half-width at
+ * `confidence` (CLT from 30 hits on, or Bernstein, whichever is smaller; Bernstein alone below 30
+ * hits), *method the bound it came from, *met whether half_width <= error * mean.  The CLT
+ * half-width uses an upper confidence bound on the variance, var + z sqrt((m4 - var^2) / n) with
+ * m4 <= fourth_moment + 2 mean^2 var, so that heavy-tailed weights, whose variance estimate runs
+ * low in most runs, keep their coverage.  A fourth moment that overflowed (infinite: weights
+ * beyond about 1e77) counts as unknown. */
+int zg_bound_half_width(double mean, double var, double fourth_moment, uint64_t n, uint64_t hits, double error,
+                        double confidence, double weight_range, double* half_width, uint32_t* method, uint32_t* met);
 
 /* ---- learned error-latency profile (no counterpart in the reference) ------------------- */
 /* A 16 -> 64 -> 64 (GELU) -> 2 MLP predicting, for a (graph, program) query, log2 of the

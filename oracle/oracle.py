@@ -34,7 +34,7 @@ class Counters(C.Structure):
     _fields_ = [("samples", C.c_uint64), ("hits", C.c_uint64), ("fails", C.c_uint64),
                 ("den_log2", C.c_uint32), ("overflow", C.c_uint32), ("sum_num", C.c_uint64 * 5),
                 ("sum_w", C.c_double), ("sum_w2", C.c_double), ("estimate", C.c_double),
-                ("reserved", C.c_double)]
+                ("sum_w4", C.c_double)]
 
     def exact_sum(self):
         from fractions import Fraction

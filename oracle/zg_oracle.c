@@ -823,6 +823,7 @@ static void counters_fold(zg_counters* out, const zg_sample_trace* tr, uint32_t 
     acc_add(out->sum_num, tr->num, den - tr->shift);
     out->sum_w += tr->w;
     out->sum_w2 += tr->w * tr->w;
+    out->sum_w4 += (tr->w * tr->w) * (tr->w * tr->w);
   }
 }
 
@@ -837,7 +838,7 @@ static void counters_merge(zg_counters* a, const zg_counters* b) {
     u128 s = (u128)a->sum_num[i] + hi[i - 3] + carry;
     a->sum_num[i] = (uint64_t)s; carry = s >> 64;
   }
-  a->sum_w += b->sum_w; a->sum_w2 += b->sum_w2;
+  a->sum_w += b->sum_w; a->sum_w2 += b->sum_w2; a->sum_w4 += b->sum_w4;
 }
 
 int zgo_run(const zgo_graph* g, const zgo_program* p, uint64_t n, uint64_t first,

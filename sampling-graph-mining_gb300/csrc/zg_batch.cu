@@ -172,7 +172,7 @@ __global__ void __launch_bounds__(kBB) k_batch_finalize(const BatchHeader* __res
       v[2] += p.fails;
       v[3] += p.overflow;
       for (int i = 0; i < 8; ++i) v[4 + i] += p.lane[i];
-      d0 += p.sum_w;
+      d0 += p.sum_w4;
       d1 += p.sum_w2;
     }
 #pragma unroll
@@ -205,7 +205,7 @@ __global__ void __launch_bounds__(kBB) k_batch_finalize(const BatchHeader* __res
       p.fails = t[2];
       p.overflow = t[3];
       for (int i = 0; i < 8; ++i) p.lane[i] = t[4 + i];
-      p.sum_w = s0;
+      p.sum_w4 = s0;
       p.sum_w2 = s1;
       out[2 * q + half] = p;
     }
@@ -678,6 +678,7 @@ void merge_into(zg_counters& a, const zg_counters& c) {
   a.fails += c.fails;
   a.overflow |= c.overflow;
   a.sum_w2 += c.sum_w2;
+  a.sum_w4 += c.sum_w4;
   a.estimate = exact_mean_of(a);
   a.sum_w = zg_exact_mean_host(a.sum_num, a.den_log2, 1);  // the exact sum, rounded once
 }
@@ -739,11 +740,12 @@ extern "C" int zg_batch_bounded(zg_batch* b, const zg_mlp* net, const zg_batch_q
       if ((rc = zg_weight_range(b->base, sized[i].kind, sized[i].param,
                                 sized[i].program ? sized[i].program->pe : 0, s, &range)))
         return rc;
-      if (zg_bound_check(t.estimate, var, t.samples, t.hits, error, confidence, range, &half, &method)) {
+      const double ew4 = n > 0 ? t.sum_w4 / n : 0.0;
+      if (zg_bound_check(t.estimate, var, ew4, t.samples, t.hits, error, confidence, range, &half, &method)) {
         bound_met[i] = 1;
         continue;
       }
-      const double need = zg_samples_needed(t.estimate, var, t.samples, t.hits, error, confidence);
+      const double need = zg_samples_needed(t.estimate, var, ew4, t.samples, t.hits, error, confidence);
       if (ran[i] >= max_samples) continue;
       const double cap = (double)max_samples;
       const uint64_t target = (uint64_t)(need < cap ? need : cap);

@@ -256,13 +256,22 @@ int zg_weight_range(const zg_graph* g, int kind, uint32_t param, uint32_t patter
   return ZG_OK;
 }
 
-bool zg_bound_check(double mean, double var, uint64_t n, uint64_t hits, double eps, double conf, double range,
-                    double* half, uint32_t* method) {
+double zg_variance_bound(double mean, double var, double ew4, uint64_t n, double conf) {
+  // unknown (0) or overflowed (weights past 1e77): no inflation, the plain variance
+  if (n == 0 || !(ew4 > 0) || !isfinite(ew4)) return var;
+  const double z = normal_quantile(1.0 - (1.0 - conf) / 2.0);
+  const double m4 = ew4 + 2.0 * mean * mean * var;  // >= the fourth central moment for w >= 0
+  const double spread = m4 - var * var;
+  return spread > 0 ? var + z * sqrt(spread / (double)n) : var;
+}
+
+bool zg_bound_check(double mean, double var, double ew4, uint64_t n, uint64_t hits, double eps, double conf,
+                    double range, double* half, uint32_t* method) {
   const double z = normal_quantile(1.0 - (1.0 - conf) / 2.0);
   const double x = log(3.0 / (1.0 - conf));
   const double dn = (double)n;
   const double bern = n ? sqrt(2.0 * var * x / dn) + 3.0 * range * x / dn : INFINITY;
-  const double clt = n ? z * sqrt(var / dn) : INFINITY;
+  const double clt = n ? z * sqrt(zg_variance_bound(mean, var, ew4, n, conf) / dn) : INFINITY;
   if (hits >= 30 && clt <= bern) {
     *half = clt;
     *method = ZG_BOUND_CLT;
@@ -273,19 +282,21 @@ bool zg_bound_check(double mean, double var, uint64_t n, uint64_t hits, double e
   return mean > 0 && *half <= eps * mean;
 }
 
-extern "C" int zg_bound_half_width(double mean, double var, uint64_t n, uint64_t hits, double error, double confidence,
-                                   double weight_range, double* half_width, uint32_t* method, uint32_t* met) {
+extern "C" int zg_bound_half_width(double mean, double var, double fourth_moment, uint64_t n, uint64_t hits,
+                                   double error, double confidence, double weight_range, double* half_width,
+                                   uint32_t* method, uint32_t* met) {
   if (!half_width || !method || !met || !(confidence > 0 && confidence < 1) || !(error > 0) || var < 0 ||
-      weight_range < 0)
+      fourth_moment < 0 || weight_range < 0)
     return zg_set_error(ZG_ERR_INVALID_ARG, "zg_bound_half_width: invalid argument"), ZG_ERR_INVALID_ARG;
-  *met = zg_bound_check(mean, var, n, hits, error, confidence, weight_range, half_width, method) ? 1 : 0;
+  *met = zg_bound_check(mean, var, fourth_moment, n, hits, error, confidence, weight_range, half_width, method) ? 1 : 0;
   return ZG_OK;
 }
 
-double zg_samples_needed(double mean, double var, uint64_t n, uint64_t hits, double eps, double conf) {
+double zg_samples_needed(double mean, double var, double ew4, uint64_t n, uint64_t hits, double eps, double conf) {
   if (hits < 30 || !(mean > 0)) return 2.0 * (double)n;
   const double z = normal_quantile(1.0 - (1.0 - conf) / 2.0);
-  return z * z * var / (eps * eps * mean * mean) * (1.0 + 0.5 / sqrt((double)hits));
+  const double v = zg_variance_bound(mean, var, ew4, n, conf);
+  return z * z * v / (eps * eps * mean * mean) * (1.0 + 0.5 / sqrt((double)hits));
 }
 
 extern "C" int zg_query(const zg_graph* g, const zg_program* p, double eps, double conf, uint64_t n_initial,
@@ -303,7 +314,7 @@ extern "C" int zg_query(const zg_graph* g, const zg_program* p, double eps, doub
   uint64_t n_total = 0, hits = 0;
   uint64_t sum[5] = {0, 0, 0, 0, 0};
   uint32_t den = 0;
-  double sw2 = 0;
+  double sw2 = 0, sw4 = 0;
   uint64_t next = std::max<uint64_t>(n_initial, 1ull << 16);
   if (max_samples == 0) max_samples = 1ull << 40;
   for (uint32_t round = 0; round < 64; ++round) {
@@ -322,6 +333,7 @@ extern "C" int zg_query(const zg_graph* g, const zg_program* p, double eps, doub
     n_total += next;
     hits += c.hits;
     sw2 += c.sum_w2;
+    sw4 += c.sum_w4;
     out->rounds = round + 1;
     // exact mean of all samples, then the empirical variance
     double mean = zg_exact_mean_host(sum, den, n_total);
@@ -329,7 +341,8 @@ extern "C" int zg_query(const zg_graph* g, const zg_program* p, double eps, doub
     if (var < 0) var = 0;
     double half = INFINITY;
     uint32_t method = 0;
-    const bool met = zg_bound_check(mean, var, n_total, hits, eps, conf, range, &half, &method);
+    const double ew4 = sw4 / (double)n_total;
+    const bool met = zg_bound_check(mean, var, ew4, n_total, hits, eps, conf, range, &half, &method);
     out->estimate = mean;
     out->half_width = half;
     out->rel_half_width = mean > 0 ? half / mean : INFINITY;
@@ -340,7 +353,7 @@ extern "C" int zg_query(const zg_graph* g, const zg_program* p, double eps, doub
       out->bound_met = 1;
       break;
     }
-    double need = zg_samples_needed(mean, var, n_total, hits, eps, conf);
+    double need = zg_samples_needed(mean, var, ew4, n_total, hits, eps, conf);
     uint64_t want = need > 1e15 ? (uint64_t)1e15 : (uint64_t)need;
     next = want > n_total ? want - n_total : n_total / 4 + 1;
   }

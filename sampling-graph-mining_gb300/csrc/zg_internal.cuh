@@ -209,7 +209,7 @@ struct ZgProgParams {
 struct ZgPartial {
   unsigned long long samples, hits, fails, overflow;
   unsigned long long lane[8];  // 32-bit halves of the exact 256-bit sum, carry-saved
-  double sum_w, sum_w2;
+  double sum_w4, sum_w2;  // sums of (1/p)^4 and (1/p)^2 in double (the mean's sum is the exact lane[])
 };
 
 // ----------------------------------------------------------------------------------------
@@ -392,12 +392,18 @@ int zg_graph_max_degree(const zg_graph* g, cudaStream_t s, uint64_t* out);
 int zg_weight_range(const zg_graph* g, int kind, uint32_t param, uint32_t pattern_edges, cudaStream_t s,
                     double* range);
 // Whether mean +- half lies within error * mean at the confidence: the empirical CLT half-width
-// (z sqrt(var / n), used from 30 hits on) or the empirical Bernstein half-width
+// (z sqrt(v / n), used from 30 hits on) or the empirical Bernstein half-width
 // (sqrt(2 var x / n) + 3 range x / n, x = ln(3 / (1 - confidence)), valid for any n), whichever is
-// smaller where both apply.  var: the empirical (1/n) variance.  *method: ZG_BOUND_CLT or
+// smaller where both apply.  var: the empirical (1/n) variance; ew4: the empirical mean of w^4
+// (0: unknown); v = zg_variance_bound(mean, var, ew4, n, confidence).  *method: ZG_BOUND_CLT or
 // ZG_BOUND_BERNSTEIN, the one that gave *half.
-bool zg_bound_check(double mean, double var, uint64_t n, uint64_t hits, double error, double confidence, double range,
-                    double* half, uint32_t* method);
-// Samples the bound check needs at the observed variance, with headroom 1 + 0.5 / sqrt(hits) for
-// the uncertainty of that variance (fewer hits, more headroom); 2n while hits < 30.
-double zg_samples_needed(double mean, double var, uint64_t n, uint64_t hits, double error, double confidence);
+bool zg_bound_check(double mean, double var, double ew4, uint64_t n, uint64_t hits, double error, double confidence,
+                    double range, double* half, uint32_t* method);
+// An upper confidence bound on the variance, for weights whose variance estimate is itself
+// uncertain (heavy tails): var + z sqrt((m4 - var^2) / n), with the fourth central moment bounded
+// by ew4 + 2 mean^2 var (nonnegative weights) and z the two-sided quantile of the confidence.
+double zg_variance_bound(double mean, double var, double ew4, uint64_t n, double confidence);
+// Samples the bound check needs at the variance bound, with headroom 1 + 0.5 / sqrt(hits);
+// 2n while hits < 30.
+double zg_samples_needed(double mean, double var, double ew4, uint64_t n, uint64_t hits, double error,
+                         double confidence);

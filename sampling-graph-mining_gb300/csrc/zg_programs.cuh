@@ -1290,13 +1290,15 @@ __device__ void prog_pattern(const ZgDevGraph& g, const ZgProgParams& pp, Ctx& c
 struct Acc {
   uint32_t samples, hits, fails, ovf;
   uint64_t s[4];
-  double sw2;  // the mean's sum is the exact s[]; only the variance term is a double
+  double sw2;  // the mean's sum is the exact s[]; only the variance terms are doubles
+  double sw4;  // sum of w^4: the uncertainty of the variance (heavy-tailed weights)
 };
 
 __device__ __forceinline__ void acc_init(Acc& a) {
   a.samples = a.hits = a.fails = a.ovf = 0;
   a.s[0] = a.s[1] = a.s[2] = a.s[3] = 0;
   a.sw2 = 0.0;
+  a.sw4 = 0.0;
 }
 
 // num / 2^shift as a double truncated to 53 bits, built from integer operations only: GB300's
@@ -1340,7 +1342,9 @@ __device__ __forceinline__ void acc_add(Acc& a, const Res& r, uint32_t den) {
       : "l"(v0), "l"(v1), "l"(v2), "l"(v3));
   // sum_w is taken from the exact integer sum at the end; only the square needs the FP64 pipe
   double w = u192_scaled_to_double(r.num, r.shift);
+  const double w2 = w * w;
   a.sw2 = fma(w, w, a.sw2);
+  a.sw4 = fma(w2, w2, a.sw4);
 }
 
 // One thread's counters, 320-bit sum and variance term kept in shared memory (slot threadIdx.x of
@@ -1350,7 +1354,7 @@ __device__ __forceinline__ void acc_add(Acc& a, const Res& r, uint32_t den) {
 template <int BLOCK>
 struct AccSlots {
   unsigned long long s[4][BLOCK];
-  double sw2[BLOCK];
+  double sw2[BLOCK], sw4[BLOCK];
   uint32_t samples[BLOCK], hits[BLOCK], fails[BLOCK], ovf[BLOCK];
 };
 
@@ -1359,6 +1363,7 @@ __device__ __forceinline__ void acc_slots_init(AccSlots<BLOCK>& sl) {
   const int t = threadIdx.x;
   sl.s[0][t] = sl.s[1][t] = sl.s[2][t] = sl.s[3][t] = 0;
   sl.sw2[t] = 0.0;
+  sl.sw4[t] = 0.0;
   sl.samples[t] = sl.hits[t] = sl.fails[t] = sl.ovf[t] = 0;
 }
 
@@ -1387,7 +1392,9 @@ __device__ __forceinline__ void acc_add_slots(Acc& a, AccSlots<BLOCK>& sl, const
   sl.s[2][t] = s2;
   sl.s[3][t] = s3;
   double w = u192_scaled_to_double(r.num, r.shift);
+  const double w2 = w * w;
   sl.sw2[t] = fma(w, w, sl.sw2[t]);
+  sl.sw4[t] = fma(w2, w2, sl.sw4[t]);
 }
 
 // The slots back into the thread's accumulator (after its loop).
@@ -1403,6 +1410,7 @@ __device__ __forceinline__ void acc_from_slots(Acc& a, const AccSlots<BLOCK>& sl
   a.s[2] = sl.s[2][t];
   a.s[3] = sl.s[3][t];
   a.sw2 = sl.sw2[t];
+  a.sw4 = sl.sw4[t];
 }
 
 template <int BLOCK>
@@ -1417,36 +1425,39 @@ __device__ void block_reduce_store(Acc& a, ZgPartial* out) {
     v[4 + 2 * i] = (uint32_t)a.s[i];
     v[5 + 2 * i] = a.s[i] >> 32;
   }
-  double d1 = a.sw2;
+  double d1 = a.sw2, d4 = a.sw4;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
 #pragma unroll
     for (int i = 0; i < 12; ++i) v[i] += __shfl_xor_sync(0xffffffffu, v[i], o);
     d1 += __shfl_xor_sync(0xffffffffu, d1, o);
+    d4 += __shfl_xor_sync(0xffffffffu, d4, o);
   }
   __shared__ unsigned long long sv[BLOCK / 32][12];
-  __shared__ double sd[BLOCK / 32];
+  __shared__ double sd[BLOCK / 32][2];
   int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (lane == 0) {
 #pragma unroll
     for (int i = 0; i < 12; ++i) sv[warp][i] = v[i];
-    sd[warp] = d1;
+    sd[warp][0] = d1;
+    sd[warp][1] = d4;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
     ZgPartial p;
     unsigned long long t[12] = {0};
-    double s1 = 0;
+    double s1 = 0, s4 = 0;
     for (int w = 0; w < BLOCK / 32; ++w) {
       for (int i = 0; i < 12; ++i) t[i] += sv[w][i];
-      s1 += sd[w];
+      s1 += sd[w][0];
+      s4 += sd[w][1];
     }
     p.samples = t[0];
     p.hits = t[1];
     p.fails = t[2];
     p.overflow = t[3];
     for (int i = 0; i < 8; ++i) p.lane[i] = t[4 + i];
-    p.sum_w = 0.0;  // the counters take it from the exact sum
+    p.sum_w4 = s4;
     p.sum_w2 = s1;
     *out = p;
   }

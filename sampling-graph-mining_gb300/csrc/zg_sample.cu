@@ -200,7 +200,7 @@ __global__ void __launch_bounds__(kBlock) k_finalize(const ZgPartial* __restrict
     v[2] += p.fails;
     v[3] += p.overflow;
     for (int i = 0; i < 8; ++i) v[4 + i] += p.lane[i];
-    d0 += p.sum_w;
+    d0 += p.sum_w4;
     d1 += p.sum_w2;
   }
 #pragma unroll
@@ -233,7 +233,7 @@ __global__ void __launch_bounds__(kBlock) k_finalize(const ZgPartial* __restrict
     p.fails = t[2];
     p.overflow = t[3];
     for (int i = 0; i < 8; ++i) p.lane[i] = t[4 + i];
-    p.sum_w = s0;
+    p.sum_w4 = s0;
     p.sum_w2 = s1;
     *out = p;
   }
@@ -296,6 +296,7 @@ void partial_to_counters(const ZgPartial& p, uint32_t den, zg_counters* out) {
   }
   out->sum_w = exact_mean(out->sum_num, den, 1);  // the exact sum, rounded once
   out->sum_w2 = p.sum_w2;
+  out->sum_w4 = p.sum_w4;
   out->estimate = exact_mean(out->sum_num, den, p.samples);
 }
 

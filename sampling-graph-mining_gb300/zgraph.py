@@ -60,7 +60,7 @@ class Counters(C.Structure):
     _fields_ = [("samples", C.c_uint64), ("hits", C.c_uint64), ("fails", C.c_uint64),
                 ("den_log2", C.c_uint32), ("overflow", C.c_uint32), ("sum_num", C.c_uint64 * 5),
                 ("sum_w", C.c_double), ("sum_w2", C.c_double), ("estimate", C.c_double),
-                ("reserved", C.c_double)]
+                ("sum_w4", C.c_double)]
 
     def exact_sum(self):
         """Exact sum of 1/p over the samples as a Python Fraction."""
@@ -189,7 +189,7 @@ def lib():
             "zg_set_l2_fetch_granularity": ([U32, C.POINTER(U32)], I32),
             "zg_exact_count_weighted": ([P, I32, U32, P, P], I32),
             "zg_conditional_close": ([P, P, U32, P, P], I32),
-            "zg_bound_half_width": ([D, D, U64, U64, D, D, D, C.POINTER(D), C.POINTER(U32), C.POINTER(U32)], I32),
+            "zg_bound_half_width": ([D, D, D, U64, U64, D, D, D, C.POINTER(D), C.POINTER(U32), C.POINTER(U32)], I32),
             "zg_batch_copy_bytes": ([P, C.POINTER(U64), C.POINTER(U64)], I32),
         }
         for name, (args, res) in sig.items():
@@ -679,10 +679,11 @@ def conditional_close(graph, queries, cuda_stream=None):
     return [(bool(r.closed), int(r.found), [int(r.edge_ids[j]) for j in range(r.found)]) for r in res[:len(qs)]]
 
 
-def bound_half_width(mean, var, n, hits, eps, conf, weight_range):
+def bound_half_width(mean, var, n, hits, eps, conf, weight_range, fourth_moment=0.0):
     """zg_bound_half_width: (half-width, BOUND_CLT or BOUND_BERNSTEIN, met) of a running estimate."""
     h, m, ok = C.c_double(), C.c_uint32(), C.c_uint32()
-    check(lib().zg_bound_half_width(mean, var, n, hits, eps, conf, weight_range, C.byref(h), C.byref(m), C.byref(ok)))
+    check(lib().zg_bound_half_width(mean, var, fourth_moment, n, hits, eps, conf, weight_range, C.byref(h),
+                                    C.byref(m), C.byref(ok)))
     return h.value, m.value, bool(ok.value)
 
 
