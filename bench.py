@@ -72,6 +72,10 @@ KERNEL_SOURCES = ("zg_internal.cuh", "zg_programs.cuh", "zg_sample_kernel.cuh", 
                   "zg_graph.cu")
 
 
+LAYOUTS = {"auto": 0, "compact": 1, "wide": 2, "packed": 3}
+LAYOUT_NAMES = {v: k for k, v in LAYOUTS.items()}
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -84,6 +88,8 @@ def parse():
     ap.add_argument("--no-coverage", action="store_true")
     ap.add_argument("--l2-fetch", type=int, default=0,
                     help="L2 fetch granularity in bytes for this process (32, 64, 128; 0: the library's)")
+    ap.add_argument("--layout", default="auto", choices=sorted(LAYOUTS),
+                    help="record layout of the graph (zg_set_record_layout; auto: the library's choice)")
     ap.add_argument("--variants", default=None,
                     help="fixed launch shapes instead of tuning, e.g. triangle=4,four_clique=3 "
                          "(profiling runs: no tuner probe launches)")
@@ -361,6 +367,7 @@ def run_gb300(args):
     import zgraph as Z
     Z.init(local)
     l2_fetch = Z.set_l2_fetch_granularity(args.l2_fetch)
+    Z.set_record_layout(LAYOUTS[args.layout])
     wl = WORKLOADS[args.workload]
     n = wl["samples"]
     t0 = time.perf_counter()
@@ -463,7 +470,7 @@ def run_gb300(args):
                 for j, (name, p) in enumerate(zip(names, progs))}
     hbm, hbm_src = peaks()
     l2_gbs = Z.read_bandwidth(48 << 20, 100)
-    layout = {1: "compact", 2: "wide", 3: "packed"}[g.meta().record_layout]
+    layout = LAYOUT_NAMES[g.meta().record_layout]
     kern = []
     for j, name in enumerate(names):
         t = per_prog[j] / args.steps / 1000.0
@@ -553,6 +560,7 @@ def run_batch(args):
     Z.init(0)
     torch.cuda.set_device(0)
     l2_fetch = Z.set_l2_fetch_granularity(args.l2_fetch)
+    Z.set_record_layout(LAYOUTS[args.layout])
     t0 = time.perf_counter()
     rmat = wl["gen"] == "rmat"
     if not rmat:
@@ -609,7 +617,7 @@ def run_batch(args):
     total_ms = sum(dev_ms)
     value = samples * args.steps / (total_ms / 1000.0)
     hbm, hbm_src = peaks()
-    layout = {1: "compact", 2: "wide", 3: "packed"}[g.meta().record_layout]
+    layout = LAYOUT_NAMES[g.meta().record_layout]
     line = {"metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int64/u192 exact", "data": "synthetic (device generator)",

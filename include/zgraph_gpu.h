@@ -323,7 +323,9 @@ typedef struct zg_batch_query {
 typedef struct zg_batch zg_batch;
 /* A batch engine over base (which must outlive it): capacity max_queries per submit; filtered
  * graphs are cached up to cache_bytes of device memory (least recently used first out), each
- * shuffled with a seed derived from filter_seed and its predicate. */
+ * shuffled with a seed derived from filter_seed and its predicate.  A filtered graph whose build
+ * runs out of device memory first frees cached graphs the submit does not use, least recently
+ * used first, and is built again. */
 int zg_batch_create(const zg_graph* base, uint32_t max_queries, uint64_t cache_bytes, uint64_t filter_seed,
                     zg_batch** out);
 int zg_batch_free(zg_batch* b);

@@ -358,8 +358,24 @@ uint64_t filter_seed_of(uint64_t base, int op, int64_t t0, int64_t t1) {
                                   (zg_mix64((uint64_t)t1) << 1)));
 }
 
+// Frees the least recently used cached graph that is neither `keep` nor used by the batch being
+// prepared (`pinned`); false when there is none.
+bool batch_evict_one(zg_batch* b, const std::vector<const zg_graph*>& pinned, const zg_graph* keep) {
+  auto victim = b->cache.end();
+  for (auto jt = b->cache.begin(); jt != b->cache.end(); ++jt) {
+    if (jt->second.g == keep || std::find(pinned.begin(), pinned.end(), jt->second.g) != pinned.end()) continue;
+    if (victim == b->cache.end() || jt->second.last_use < victim->second.last_use) victim = jt;
+  }
+  if (victim == b->cache.end()) return false;
+  b->cached_bytes -= victim->second.bytes;
+  zg_graph_free(victim->second.g);
+  b->cache.erase(victim);
+  return true;
+}
+
 // The cached filtered graph of (op, t0, t1), built on first use; `pinned` holds the graphs the
-// batch being prepared uses (never evicted for it).
+// batch being prepared uses (never evicted for it).  A build that runs out of device memory frees
+// cached graphs, least recently used first, and tries again.
 int batch_filtered(zg_batch* b, int op, int64_t t0, int64_t t1, cudaStream_t s,
                    const std::vector<const zg_graph*>& pinned, const zg_graph** out) {
   auto key = std::make_tuple(op, t0, op == ZG_PRED_RANGE ? t1 : 0);
@@ -371,23 +387,17 @@ int batch_filtered(zg_batch* b, int op, int64_t t0, int64_t t1, cudaStream_t s,
   }
   zg_graph* g = nullptr;
   uint64_t m = 0;
-  int rc = zg_graph_filter_sampling(b->base, op, t0, t1, filter_seed_of(b->filter_seed, op, t0, t1), s, &m, &g);
+  int rc;
+  do {
+    rc = zg_graph_filter_sampling(b->base, op, t0, t1, filter_seed_of(b->filter_seed, op, t0, t1), s, &m, &g);
+  } while (rc == ZG_ERR_OOM && batch_evict_one(b, pinned, nullptr));
   if (rc) return rc;
   zg_graph_meta meta;
   zg_graph_get_meta(g, &meta);
   b->cache[key] = {g, meta.device_bytes, ++b->use_clock};
   b->cached_bytes += meta.device_bytes;
   // evict least recently used graphs not used by this batch while over budget
-  while (b->cached_bytes > b->cache_bytes) {
-    auto victim = b->cache.end();
-    for (auto jt = b->cache.begin(); jt != b->cache.end(); ++jt) {
-      if (jt->second.g == g || std::find(pinned.begin(), pinned.end(), jt->second.g) != pinned.end()) continue;
-      if (victim == b->cache.end() || jt->second.last_use < victim->second.last_use) victim = jt;
-    }
-    if (victim == b->cache.end()) break;
-    b->cached_bytes -= victim->second.bytes;
-    zg_graph_free(victim->second.g);
-    b->cache.erase(victim);
+  while (b->cached_bytes > b->cache_bytes && batch_evict_one(b, pinned, g)) {
   }
   *out = g;
   return ZG_OK;

@@ -1027,6 +1027,7 @@ __device__ void prog_chain(const ZgDevGraph& g, int order, Ctx& c, Res& r) {
     // frontier update (ChainMining.cpp:265-80); here src is a frontier vertex and e.x is new
     int upd = (f[0] == src) ? 0 : 1;
     f[upd] = e.x;
+    if (!DBG && i + 1 >= order - 2) break;  // the last step: the new frontier's range is not used
     const EdgeAt ae = edge_at(g, e.y, e.x);  // e in the new frontier's list
     fe[upd] = ae.pos + 1 + ae.suf;
     fl[upd] = lb_eid(g.adj_e, edge_at_start(g, ae, e.x), ae.pos + 1, mv, 0u, e.y);
