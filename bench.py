@@ -392,9 +392,12 @@ def run_gb300(args):
                 p.set_variant(int(fixed[name]))
             tuning[name] = dict(p.variant(), fixed=True)
             continue
-        best, ms = p.tune(g, 1 << 23, cuda_stream=sp)
-        tuning[name] = {"variant": best, "min_blocks": p.variant()["min_blocks"], "grid": p.variant()["grid"],
-                        "ms_per_variant_2^23": [round(x, 3) for x in ms]}
+        # probes of 2^23 samples; 2^26 on wide-record graphs, whose grids hold six times the
+        # resident blocks (a probe must give every thread more than a few samples)
+        probe_log2 = 26 if g.meta().record_layout == Z.RECORDS_WIDE else 23
+        best, ms = p.tune(g, 1 << probe_log2, cuda_stream=sp)
+        tuning[name] = {"variant": best, "min_blocks": p.variant()["min_blocks"],
+                        "ms_per_variant_2^%d" % probe_log2: [round(x, 3) for x in ms]}
     d_res = torch.zeros((len(progs), Z.RESULT_BYTES), dtype=torch.uint8, device="cuda")
     flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
     seed = 20250101

@@ -235,7 +235,8 @@ int zg_result_to_counters(const void* h_result, const zg_program* p, zg_counters
  * counterpart in the reference.  The per-block scratch is one fixed device array of
  * ZG_NOALLOC_MAX_BLOCKS x ZG_RESULT_BYTES bytes (448 KiB) that every GPU loading the library keeps
  * until the process exits; a launch that would need more blocks is rejected with ZG_ERR_TOO_LARGE
- * (a launch needs at most 8 resident blocks per SM, 1216 on a 152-SM GB300).  The array used is the
+ * (the library's sampling grids never do: at most 8 resident blocks per SM, six times the resident
+ * blocks on wide-record graphs, and never more than ZG_NOALLOC_MAX_BLOCKS).  The array used is the
  * current device's: g must have been built on the current device (a graph on another device is
  * refused with ZG_ERR_INVALID_ARG).  The first call on each device looks up the array's device
  * address (cudaGetSymbolAddress), so make that first call before any stream capture.  All calls share the array: calls whose
@@ -247,11 +248,12 @@ int zg_run_noalloc(const zg_graph* g, const zg_program* p, uint64_t n, uint64_t 
 /* Autotuner (no counterpart in the reference, whose thread count comes from libnuma).  Each
  * program kind has ZG_VARIANTS launch shapes: the sampling kernel compiled for
  * min-blocks-per-SM 1, 2, 3, 4, 5, 6, 8 (register caps 255/128/80/64/48/40/32) with a grid of
- * occupancy x SM count; the 4-chain's shapes with at most 3 blocks per SM interleave two samples
+ * occupancy x SM count (six times that on wide-record graphs, whose SMs progress at different
+ * rates: the block scheduler then balances them; at most ZG_NOALLOC_MAX_BLOCKS); the 4-chain's shapes with at most 3 blocks per SM interleave two samples
  * per thread (more registers, two load chains in flight), the others run one.  zg_tune times every
  * variant on g (probe_samples estimators, best of 3) and keeps the fastest for this device and
  * kind; ms_per_variant (may be NULL) receives ZG_VARIANTS timings.  zg_set_variant /
- * zg_get_variant fix or read the choice. */
+ * zg_get_variant fix or read the choice (zg_get_variant's grid: the compact- and packed-record one). */
 #define ZG_VARIANTS 7
 int zg_tune(const zg_graph* g, const zg_program* p, uint64_t probe_samples, void* cuda_stream,
             int* best_variant, float* ms_per_variant);

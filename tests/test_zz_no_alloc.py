@@ -78,8 +78,10 @@ def test_noalloc_allocates_nothing():
 
 
 def test_noalloc_grid_fits_the_scratch():
-    """Every program kind and launch variant launches at most 8 resident blocks per SM, well within
-    the fixed scratch of ZG_NOALLOC_MAX_BLOCKS blocks."""
+    """Every program kind and launch variant launches at most 8 resident blocks per SM on compact-
+    and packed-record graphs, well within the fixed scratch of ZG_NOALLOC_MAX_BLOCKS blocks (wide-
+    record graphs launch up to six times that, capped at the scratch size: the noalloc parity test
+    above runs one)."""
     import torch
     Z.init(0)
     L = Z.lib()
