@@ -233,22 +233,22 @@ int zg_result_to_counters(const void* h_result, const zg_program* p, zg_counters
  * serve queries: a process whose memory manager reserves all device memory up front, or a
  * latency-critical path where cudaMalloc/cudaFree could synchronise the device.  It has no
  * counterpart in the reference.  The per-block scratch is one fixed device array of
- * ZG_NOALLOC_MAX_BLOCKS x ZG_RESULT_BYTES bytes (448 KiB) that every GPU loading the library keeps
+ * ZG_NOALLOC_MAX_BLOCKS x ZG_RESULT_BYTES bytes (1.75 MiB) that every GPU loading the library keeps
  * until the process exits; a launch that would need more blocks is rejected with ZG_ERR_TOO_LARGE
- * (the library's sampling grids never do: at most 8 resident blocks per SM, six times the resident
+ * (the library's sampling grids never do: at most 8 resident blocks per SM, 24 times the resident
  * blocks on wide-record graphs, and never more than ZG_NOALLOC_MAX_BLOCKS).  The array used is the
  * current device's: g must have been built on the current device (a graph on another device is
  * refused with ZG_ERR_INVALID_ARG).  The first call on each device looks up the array's device
  * address (cudaGetSymbolAddress), so make that first call before any stream capture.  All calls share the array: calls whose
  * executions overlap on the GPU race and must be serialised by the caller.  d_result: device
  * memory of ZG_RESULT_BYTES bytes provided by the caller; read it as for zg_run_async. */
-#define ZG_NOALLOC_MAX_BLOCKS 4096
+#define ZG_NOALLOC_MAX_BLOCKS 16384
 int zg_run_noalloc(const zg_graph* g, const zg_program* p, uint64_t n, uint64_t first_sample,
                    uint64_t seed, uint32_t stream_id, void* cuda_stream, void* d_result);
 /* Autotuner (no counterpart in the reference, whose thread count comes from libnuma).  Each
  * program kind has ZG_VARIANTS launch shapes: the sampling kernel compiled for
  * min-blocks-per-SM 1, 2, 3, 4, 5, 6, 8 (register caps 255/128/80/64/48/40/32) with a grid of
- * occupancy x SM count (six times that on wide-record graphs, whose SMs progress at different
+ * occupancy x SM count (24 times that on wide-record graphs, whose SMs progress at different
  * rates: the block scheduler then balances them; at most ZG_NOALLOC_MAX_BLOCKS); the 4-chain's shapes with at most 3 blocks per SM interleave two samples
  * per thread (more registers, two load chains in flight), the others run one.  zg_tune times every
  * variant on g (probe_samples estimators, best of 3) and keeps the fastest for this device and

@@ -9,7 +9,7 @@
 // device data, so it performs no allocation at all.
 //
 // The scratch holds the sampling kernel's per-block partial sums: ZG_NOALLOC_MAX_BLOCKS blocks of
-// ZG_RESULT_BYTES bytes (4096 x 112 B = 448 KiB).  Every GPU that loads the library keeps that
+// ZG_RESULT_BYTES bytes (16384 x 112 B = 1.75 MiB).  Every GPU that loads the library keeps that
 // array until the process exits.  All calls share it and it keeps the last call's contents; each
 // block overwrites its own slot before the reduction reads it, so nothing needs clearing.  Calls
 // whose executions overlap on the GPU (for example on two streams) race on the array and must be

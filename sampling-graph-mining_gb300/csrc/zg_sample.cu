@@ -414,14 +414,16 @@ int variant_for(int kind) {
 
 // Blocks per launch over the resident ones, per record layout (compact, wide, packed).  On
 // wide-record graphs (read from HBM) SMs progress at different rates, and a grid of exactly the
-// resident blocks gives each SM a fixed share: the launch waits for the slowest one.  With six
-// times the resident blocks the block scheduler hands the remaining blocks to whichever SM frees
-// up first.  Measured on GB300: R-MAT 26 4-clique 134.1 -> 116.9 ms per 2^30 samples, triangle
-// 33.2 -> 28.9 ms per 2^28; Chung-Lu 42 M edges, the four programs 16.2 -> 14.6 ms per 2^26 each.
-// On near-L2 graphs (compact, packed records) the extra blocks cost more than they balance (R-MAT
-// 20: 5.75 -> 5.86 ms), so those launch the resident blocks only.  Every grid stays within the
-// no-allocation entry point's fixed scratch (ZG_NOALLOC_MAX_BLOCKS partials).
-constexpr int kOversubscribe[3] = {1, 6, 1};
+// resident blocks gives each SM a fixed share: the launch waits for the slowest one.  With many
+// times the resident blocks, each short, the block scheduler hands the remaining blocks to
+// whichever SM frees up first and the last wave is short.  Measured on GB300, R-MAT 26, 4-clique
+// per 2^30 samples: 134.1 ms (1x), 117.8 ms (6x), 112.5 ms (24x, as fast as the batch kernel's
+// work queue); triangle per 2^28: 33.2, 29.3, 27.8 ms; Chung-Lu 42 M edges, the four programs
+// per 2^26 each: 16.2 ms (1x), 14.5 ms (6x and 24x).  On near-L2 graphs (compact, packed records)
+// the extra blocks cost more than they balance (R-MAT 20: 5.75 -> 5.86 ms at 6x), so those launch
+// the resident blocks only.  Every grid stays within the no-allocation entry point's fixed
+// scratch (ZG_NOALLOC_MAX_BLOCKS partials).
+constexpr int kOversubscribe[3] = {1, 24, 1};
 
 int grid_for_variant(int kind, int v, int layout) {
   int d = current_device();
