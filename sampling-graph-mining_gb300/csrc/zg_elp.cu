@@ -231,9 +231,8 @@ extern "C" int zg_time_profile(const zg_graph* g, const zg_program* p, uint32_t 
   return ZG_OK;
 }
 
-// Bounded query: sample n_initial estimators (the sizing step's budget), then check the answer by
-// its CLT half-width z * sqrt(var / n) at `conf`; while it exceeds eps * estimate, extend with more
-// estimators (never reusing sample indices) sized from the current variance, up to max_samples.
+// The largest weight one estimator of this program can carry on g (the Bernstein bound's range):
+// m (3m for the four-chain) times, per conditional step i, at most min((i + 1) max_degree, 2m).
 int zg_weight_range(const zg_graph* g, int kind, uint32_t param, uint32_t pattern_edges, cudaStream_t s,
                     double* range) {
   uint64_t dmax = 0;
@@ -299,6 +298,9 @@ double zg_samples_needed(double mean, double var, double ew4, uint64_t n, uint64
   return z * z * v / (eps * eps * mean * mean) * (1.0 + 0.5 / sqrt((double)hits));
 }
 
+// Bounded query: sample n_initial estimators (the sizing step's budget), then check the answer with
+// zg_bound_check at `conf`; while its half-width exceeds eps * estimate, extend with more estimators
+// (never reusing sample indices) sized by zg_samples_needed, up to max_samples.
 extern "C" int zg_query(const zg_graph* g, const zg_program* p, double eps, double conf, uint64_t n_initial,
                         uint64_t max_samples, uint64_t seed, uint32_t stream_id, void* cuda_stream,
                         zg_query_result* out) {
