@@ -336,6 +336,45 @@ def time_to_bound(Z, g, names, exact, eps=0.01, conf=0.95, cap=1 << 37, seed=31,
     return out
 
 
+def random_sector_bytes():
+    """DRAM bytes one random 32-byte sector read moves: the ncu capture of zg_random_sector_rate's
+    kernel in profiles/dram_traffic.txt (bytes of the timed launch / its sectors), used while the
+    kernel sources hash to the value it was captured at."""
+    path = os.path.join(ROOT, "profiles", "dram_traffic.txt")
+    try:
+        lines = [l.split() for l in open(path) if l.strip() and not l.startswith("#")]
+    except OSError:
+        return None, "no capture committed"
+    for f in lines:
+        if len(f) >= 6 and f[0] == "k_random_sectors":
+            if f[3] != kernel_source_hash():
+                return None, "stale: captured at kernel-source hash %s" % f[3]
+            return float(f[4]) / float(f[5]), "ncu capture on %s" % f[1]
+    return None, "no capture of k_random_sectors"
+
+
+def random_sector_view(Z, g, touched_gbs, dram_gbs=None):
+    """The sampling loads are isolated 32-byte sectors at random addresses: their ceiling is the rate
+    at which the memory system serves such reads, measured live after the timed steps by
+    zg_random_sector_rate over this graph's records and adjacency.  `frac` compares the sectors the
+    kernels touch (some share a line, so it can exceed 1); `dram` compares the DRAM bytes the
+    kernels move (ncu) with the DRAM bytes the probe moves at its rate."""
+    peak = Z.random_sector_rate(g, 256)
+    ach = touched_gbs * 1e9 / 32.0
+    out = {"achieved": ach / 1e9, "peak": peak / 1e9, "unit": "G sectors/s", "frac": ach / peak if peak else None,
+           "peak_source": "measured live: zg_random_sector_rate (8 independent 32-byte loads in flight per thread, "
+                          "one full-occupancy grid, over this graph's records and edge-id-ordered adjacency)"}
+    bps, src = random_sector_bytes()
+    if dram_gbs and bps and peak:
+        ceiling = peak * bps / 1e9
+        out["dram"] = {"achieved_gbs": dram_gbs, "ceiling_gbs": ceiling, "frac": dram_gbs / ceiling,
+                       "bytes_per_random_sector": bps, "source": src}
+    else:
+        out["dram"] = None
+        out["dram_source"] = src if not bps else "no DRAM capture of the kernels at this build"
+    return out
+
+
 def wilson(k, n, z=1.959963984540054):
     """Wilson score 95 % interval of a binomial fraction k/n."""
     if n == 0:
@@ -513,6 +552,7 @@ def run_gb300(args):
                 "l2": {"peak": l2_gbs, "frac": dom["touched_gbs"] / l2_gbs},
                 "hbm": {"peak": hbm, "peak_source": hbm_src,
                         "dram_frac": dom["dram_gbs"] / hbm if dom["dram_gbs"] else None},
+                "random_sectors": random_sector_view(Z, g, dom["touched_gbs"], dom["dram_gbs"]),
                 "per_kernel": kern}
     exact, acc = {}, {}
     ttb = None
@@ -686,6 +726,9 @@ def run_batch(args):
                                               "by load latency (the same time with 32-byte fills at the touched "
                                               "bytes)"} if dram_ps else None),
                             "bound_note": "latency of each sample's dependent loads (profiles/k_batch_pattern_rmat21.md)",
+                            "random_sectors": random_sector_view(
+                                Z, g, achieved,
+                                dram_ps * samples / (total_ms / args.steps / 1000.0) / 1e9 if dram_ps else None),
                             "peak_source": hbm_src, "per_kernel": kern}
         line["results"] = {name: {"hits": int(c.hits), "estimate": c.estimate} for name, (c, _) in zip(names, res)}
         if not args.no_time_to_bound:
@@ -717,6 +760,7 @@ def run_batch(args):
                             "kernel": "k_batch (all queries of the step)",
                             "traffic": dram_ps * samples if dram_ps else None, "traffic_source": dram_src,
                             "algorithmic_bytes": "zg_touch_sectors of each (program, graph) pair x its samples",
+                            "random_sectors": random_sector_view(Z, g, ach),
                             "peak_source": hbm_src}
         if not args.no_time_to_bound:
             line["learned_batch"] = learned_batch(Z, b, qs)

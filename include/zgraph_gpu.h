@@ -513,6 +513,12 @@ int zg_query_learned(const zg_mlp* net, const zg_graph* g, const zg_program* p, 
  * timed with CUDA events: below the 129 MB L2 it measures L2, well above it HBM.  The L2 view of
  * the roofline for graphs that nearly fit in L2 (no counterpart in the reference). */
 int zg_read_bandwidth(uint64_t bytes, uint32_t reps, void* cuda_stream, double* gbs);
+/* Random 32-byte sector reads per second over g's edge records and edge-id-ordered adjacency
+ * (every sector of the two arrays equally likely; each thread of one full-occupancy grid keeps 8
+ * independent loads in flight, `iters` rounds of them; CUDA events after a warm-up launch): the
+ * rate at which the memory system serves isolated sectors of the arrays the sampling kernels
+ * read, the ceiling of kernels whose loads are random sectors (no counterpart in the reference). */
+int zg_random_sector_rate(const zg_graph* g, uint32_t iters, void* cuda_stream, double* sectors_per_s);
 /* The bytes zg_run's sampling kernel moves (no counterpart in the reference): the same kernel,
  * compiled a second time with every global load also counting the 32-byte sectors it spans (a
  * sector equal to the thread's previous load's last sector is counted once), run on n estimators

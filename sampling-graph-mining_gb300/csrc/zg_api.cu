@@ -189,7 +189,8 @@ extern "C" int zg_program_info(const zg_program* p, uint32_t* num_unique, uint32
   return ZG_OK;
 }
 
-// ---- bandwidth probe: the L2 view of the roofline ------------------------------------------
+// ---- bandwidth probes: the L2 view of the roofline, random sectors over a graph ------------
+int zg_check_device();  // zg_sample.cu
 namespace {
 __global__ void k_read_probe(const uint4* __restrict__ buf, uint64_t n16, uint32_t reps, uint4* __restrict__ sink) {
   uint4 acc = make_uint4(0, 0, 0, 0);
@@ -204,7 +205,74 @@ __global__ void k_read_probe(const uint4* __restrict__ buf, uint64_t n16, uint32
     }
   if ((acc.x ^ acc.y ^ acc.z ^ acc.w) == 0x9E3779B9u) sink[threadIdx.x] = acc;  // keeps the loads live
 }
+
+// Random 32-byte sector reads over a graph's sampled arrays (its edge records and its edge-id
+// ordered adjacency, each sector of their union equally likely): each thread keeps 8 independent
+// 256-bit loads in flight per iteration; one persistent grid at full occupancy.
+__global__ void __launch_bounds__(256) k_random_sectors(const char* __restrict__ rec, uint64_t rec_sectors,
+                                                        const char* __restrict__ adj, uint64_t adj_sectors,
+                                                        uint32_t iters, uint64_t seed,
+                                                        unsigned long long* __restrict__ sink) {
+  const uint64_t tid = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  const uint64_t total = rec_sectors + adj_sectors;
+  unsigned long long acc = 0;
+  for (uint32_t it = 0; it < iters; ++it) {
+    unsigned long long v[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const uint64_t h = zg_mix64(seed + tid * 0x9E3779B97F4A7C15ull + (((uint64_t)it << 3) | (uint64_t)k));
+      const uint64_t sct = __umul64hi(h, total);  // uniform in [0, total)
+      const char* p = sct < rec_sectors ? rec + sct * 32 : adj + (sct - rec_sectors) * 32;
+      unsigned long long a0, a1, a2, a3;
+      asm volatile("ld.global.nc.v4.u64 {%0, %1, %2, %3}, [%4];" : "=l"(a0), "=l"(a1), "=l"(a2), "=l"(a3) : "l"(p));
+      v[k] = a0 ^ a1 ^ a2 ^ a3;
+    }
+#pragma unroll
+    for (int k = 0; k < 8; ++k) acc ^= v[k];
+  }
+  if (acc == 0x9E3779B97F4A7C15ull) sink[threadIdx.x] = acc;  // keeps the loads live
+}
 }  // namespace
+
+// Random 32-byte sector reads per second over g's records and adjacency (CUDA events, after one
+// warm-up launch): the rate at which the memory system serves isolated sectors from the arrays the
+// sampling kernels read, the ceiling of kernels whose loads are random sectors.
+extern "C" int zg_random_sector_rate(const zg_graph* g, uint32_t iters, void* cuda_stream, double* sectors_per_s) {
+  if (!g || !sectors_per_s || iters == 0 || g->d.m == 0)
+    return zg_set_error(ZG_ERR_INVALID_ARG, "zg_random_sector_rate: bad argument"), ZG_ERR_INVALID_ARG;
+  if (int rc = zg_check_device()) return rc;
+  cudaStream_t s = (cudaStream_t)cuda_stream;
+  const uint64_t m = g->d.m;
+  const uint64_t rec_sectors = (g->wide ? 32ull : 16ull) * m / 32;  // whole sectors of the record array
+  const uint64_t adj_sectors = 16ull * m / 32;                      // of adj_e (2m entries of 8 bytes)
+  unsigned long long* sink = nullptr;
+  cudaError_t e = cudaMalloc(&sink, 256 * sizeof(unsigned long long));
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return zg_set_error(ZG_ERR_OOM, "zg_random_sector_rate: %s", cudaGetErrorString(e)), ZG_ERR_OOM;
+  }
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_random_sectors, 256, 0);
+  const int grid = (per_sm < 1 ? 1 : per_sm) * zg_num_sms();
+  const char* rec = (const char*)g->rec;
+  const char* adj = (const char*)g->adj_e;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  k_random_sectors<<<grid, 256, 0, s>>>(rec, rec_sectors, adj, adj_sectors, 4, 1, sink);  // warm-up
+  cudaEventRecord(e0, s);
+  k_random_sectors<<<grid, 256, 0, s>>>(rec, rec_sectors, adj, adj_sectors, iters, 2, sink);
+  cudaEventRecord(e1, s);
+  e = cudaEventSynchronize(e1);
+  float ms = 0;
+  if (e == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(sink);
+  if (e != cudaSuccess) return zg_check_cuda(e, "zg_random_sector_rate");
+  *sectors_per_s = ms > 0 ? (double)grid * 256 * iters * 8 / (ms / 1000.0) : 0.0;
+  return ZG_OK;
+}
 
 // Read bandwidth of a device buffer of `bytes` read `reps` times by one persistent grid (CUDA
 // events): a buffer well below the 129 MB L2 measures L2 bandwidth, one well above it HBM.

@@ -185,6 +185,7 @@ def lib():
             "zg_batch_tune": ([P, P, U32, P, C.POINTER(I32), P], I32),
             "zg_batch_elapsed_ms": ([P, C.POINTER(C.c_float)], I32),
             "zg_read_bandwidth": ([U64, U32, P, C.POINTER(D)], I32),
+            "zg_random_sector_rate": ([P, U32, P, C.POINTER(D)], I32),
             "zg_touch_sectors": ([P, P, U64, U64, U64, U32, P, C.POINTER(U64)], I32),
             "zg_set_l2_fetch_granularity": ([U32, C.POINTER(U32)], I32),
             "zg_exact_count_weighted": ([P, I32, U32, P, P], I32),
@@ -409,6 +410,13 @@ def set_l2_fetch_granularity(nbytes):
     prev = C.c_uint32()
     check(lib().zg_set_l2_fetch_granularity(nbytes, C.byref(prev)))
     return prev.value
+
+
+def random_sector_rate(graph, iters=64, cuda_stream=None):
+    """zg_random_sector_rate: random 32-byte sector reads per second over graph's records and adjacency."""
+    out = C.c_double(0)
+    check(lib().zg_random_sector_rate(graph.handle, iters, cuda_stream, C.byref(out)))
+    return out.value
 
 
 def read_bandwidth(nbytes, reps=200, cuda_stream=None):

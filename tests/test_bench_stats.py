@@ -15,3 +15,13 @@ def test_wilson_interval(k, n, lo, hi):
     a, b = bench.wilson(k, n)
     assert a == pytest.approx(lo, abs=2e-4) and b == pytest.approx(hi, abs=2e-4)
     assert 0.0 <= a <= k / n <= b <= 1.0
+
+
+def test_random_sector_bytes_from_the_committed_capture():
+    """The DRAM bytes one random 32-byte sector read moves, from profiles/dram_traffic.txt: between
+    one sector and a 256-byte line while the capture matches the kernel sources, else a reason."""
+    bps, src = bench.random_sector_bytes()
+    if bps is None:
+        assert src
+    else:
+        assert 32.0 <= bps <= 256.0 and "ncu capture" in src
