@@ -353,7 +353,7 @@ def random_sector_bytes():
     return None, "no capture of k_random_sectors"
 
 
-def random_sector_view(Z, g, touched_gbs, dram_gbs=None):
+def random_sector_view(Z, g, touched_gbs, dram_gbs=None, near_l2=False):
     """The sampling loads are isolated 32-byte sectors at random addresses: their ceiling is the rate
     at which the memory system serves such reads, measured live after the timed steps by
     zg_random_sector_rate over this graph's records and adjacency.  `frac` compares the sectors the
@@ -365,7 +365,10 @@ def random_sector_view(Z, g, touched_gbs, dram_gbs=None):
            "peak_source": "measured live: zg_random_sector_rate (8 independent 32-byte loads in flight per thread, "
                           "one full-occupancy grid, over this graph's records and edge-id-ordered adjacency)"}
     bps, src = random_sector_bytes()
-    if dram_gbs and bps and peak:
+    if near_l2:
+        out["dram"] = None
+        out["dram_source"] = "near-L2 graph: the probe's sectors mostly hit L2, its DRAM bytes per sector do not apply"
+    elif dram_gbs and bps and peak:
         ceiling = peak * bps / 1e9
         out["dram"] = {"achieved_gbs": dram_gbs, "ceiling_gbs": ceiling, "frac": dram_gbs / ceiling,
                        "bytes_per_random_sector": bps, "source": src}
@@ -552,7 +555,7 @@ def run_gb300(args):
                 "l2": {"peak": l2_gbs, "frac": dom["touched_gbs"] / l2_gbs},
                 "hbm": {"peak": hbm, "peak_source": hbm_src,
                         "dram_frac": dom["dram_gbs"] / hbm if dom["dram_gbs"] else None},
-                "random_sectors": random_sector_view(Z, g, dom["touched_gbs"], dom["dram_gbs"]),
+                "random_sectors": random_sector_view(Z, g, dom["touched_gbs"], dom["dram_gbs"], near_l2),
                 "per_kernel": kern}
     exact, acc = {}, {}
     ttb = None
