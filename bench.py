@@ -699,6 +699,11 @@ def run_batch(args):
         achieved = step_bytes / (total_ms / args.steps / 1000.0) / 1e9
         stream = torch.cuda.current_stream()
         d_res = torch.zeros(Z.RESULT_BYTES, dtype=torch.uint8, device="cuda")
+        # conditional_close look-ups per sample (the access model's count, up to the first missing
+        # edge) from the debug kernel's traces: the 4-clique closes three edges; the generic pattern
+        # programs sample every edge and close none
+        closures = {name: float(progs[name].run_debug(g, 1 << 16, j + 1)["closures"].mean())
+                    for j, name in enumerate(names)}
         kern = []
         for j, name in enumerate(names):
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -715,6 +720,8 @@ def run_batch(args):
                          "samples_per_s": wl["samples"] / (ms / 1000.0), "touched_bytes_per_sample": touched[name],
                          "touched_gbs": touched[name] * wl["samples"] / (ms / 1000.0) / 1e9,
                          "frac_of_hbm_peak": touched[name] * wl["samples"] / (ms / 1000.0) / 1e9 / hbm,
+                         "closure_checks_per_sample": closures[name],
+                         "closure_checks_per_s": closures[name] * wl["samples"] / (ms / 1000.0),
                          "dram_bytes_per_sample": dram_ps, "dram_source": dram_src})
         dram_ps, dram_src = profile_traffic("k_batch", args.workload, layout)
         line["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
