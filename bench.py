@@ -71,6 +71,9 @@ PATTERNS = {"five_star": (5, [(0, 1), (0, 2), (0, 3), (0, 4)]),
 EXACT_IDS = {"triangle": 1, "three_chain": 2, "four_chain": 3, "four_clique": 5, "four_clique_unbiased": 5}
 KERNEL_SOURCES = ("zg_internal.cuh", "zg_programs.cuh", "zg_sample_kernel.cuh", "zg_sample.cu", "zg_batch.cu",
                   "zg_graph.cu")
+# zg_random_sector_rate's probe kernel and the helpers it uses: its DRAM bytes per sector do not
+# depend on the sampling kernels
+PROBE_SOURCES = ("zg_internal.cuh", "zg_api.cu")
 
 
 LAYOUTS = {"auto": 0, "compact": 1, "wide": 2, "packed": 3}
@@ -149,11 +152,12 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def kernel_source_hash():
-    """Hash of the sampling kernels' sources: ties a committed ncu traffic figure to the code it
-    was measured on (the GPU host has no git history to compare against)."""
+def kernel_source_hash(sources=KERNEL_SOURCES):
+    """Hash of the sampling kernels' sources (or of the given csrc files): ties a committed ncu
+    traffic figure to the code it was measured on (the GPU host has no git history to compare
+    against)."""
     h = hashlib.sha256()
-    for name in KERNEL_SOURCES:
+    for name in sources:
         with open(os.path.join(ROOT, "sampling-graph-mining_gb300", "csrc", name), "rb") as f:
             h.update(f.read())
     return h.hexdigest()[:16]
@@ -339,7 +343,7 @@ def time_to_bound(Z, g, names, exact, eps=0.01, conf=0.95, cap=1 << 37, seed=31,
 def random_sector_bytes():
     """DRAM bytes one random 32-byte sector read moves: the ncu capture of zg_random_sector_rate's
     kernel in profiles/dram_traffic.txt (bytes of the timed launch / its sectors), used while the
-    kernel sources hash to the value it was captured at."""
+    probe's own sources (PROBE_SOURCES) hash to the value it was captured at."""
     path = os.path.join(ROOT, "profiles", "dram_traffic.txt")
     try:
         lines = [l.split() for l in open(path) if l.strip() and not l.startswith("#")]
@@ -347,8 +351,8 @@ def random_sector_bytes():
         return None, "no capture committed"
     for f in lines:
         if len(f) >= 6 and f[0] == "k_random_sectors":
-            if f[3] != kernel_source_hash():
-                return None, "stale: captured at kernel-source hash %s" % f[3]
+            if f[3] != kernel_source_hash(PROBE_SOURCES):
+                return None, "stale: captured at probe-source hash %s" % f[3]
             return float(f[4]) / float(f[5]), "ncu capture on %s" % f[1]
     return None, "no capture of k_random_sectors"
 
