@@ -1132,12 +1132,16 @@ __device__ void prog_pattern_small(const ZgDevGraph& g, const ZgProgParams& pp, 
     ++ne;
     if (nbr_slot < 0) {
       if (nvtx >= MV) return;  // more vertices than the pattern (pv <= MV): not a hit
-      // the new vertex's list range past min_valid: needed only if another step draws from it
+      // the new vertex's list range past min_valid: needed only if another step draws from it.
+      // Its list comes from the vertex offsets, not from the sampled edge's record: the vertex is
+      // reached through a random edge, so high-degree vertices come up most often and their
+      // offsets tend to be L2 hits, where the record of a random edge is a DRAM read.  The bound
+      // is searched over the whole list (the sampled edge, id >= min_valid, lies in it).
       uint32_t nve = 0, nvl = 0;
       if ((uint32_t)k + 1 < pp.pe) {
-        const EdgeAt ae = edge_at(g, e.y, e.x);  // e in the new vertex's list
-        nve = ae.pos + 1 + ae.suf;
-        nvl = lb_eid(g.adj_e, edge_at_start(g, ae, e.x), ae.pos + 1, mv, 0u, e.y);
+        const uint32_t ls = ZG_LDG(&g.off32[e.x]);
+        nve = ZG_LDG(&g.off32[e.x + 1]);
+        nvl = lb_eid(g.adj_e, ls, nve, mv, 0u, (uint32_t)(g.m - 1));
       }
 #pragma unroll
       for (int i = 0; i < MV; ++i)
