@@ -73,3 +73,64 @@ def test_generators_are_deterministic_and_simple():
     assert w.min() >= 0 and w.max() < 100 and len(np.unique(w)) == 100
     # R-MAT scale 13, edge factor 12 (the reference's CPU-runnable workload): ~80K edges
     assert 70000 < len(Z.gen_rmat(13, 12, seed=1)) < 100000
+
+
+def _prototypes():
+    """Every zg_* prototype of include/zgraph_gpu.h: name -> (return type, [parameter types])."""
+    text = open(os.path.join(ROOT, "include", "zgraph_gpu.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    text = re.sub(r"^\s*#.*$", "", text, flags=re.M)
+    protos = {}
+    for m in re.finditer(r"([A-Za-z_][\w\s\*]*?)\b(zg_[a-z0-9_]+)\s*\(([^)]*)\)\s*;", text):
+        ret, name, params = " ".join(m.group(1).split()), m.group(2), m.group(3).strip()
+        types = [] if params in ("", "void") else [re.sub(r"\b\w+\s*(\[\d*\])?$", lambda t: "*" if t.group(1) else "",
+                                                          p.strip()).strip() for p in params.split(",")]
+        protos[name] = (ret, types)
+    return protos
+
+
+def _c_kind(t):
+    """A C type as the ABI sees it: ('p',) pointer, ('f', bits) floating, ('i', bits, signed)."""
+    t = " ".join(t.replace("const", "").split())
+    if "*" in t:
+        return ("p",)
+    if t in ("double", "float"):
+        return ("f", 64 if t == "double" else 32)
+    width = {"int": 32, "int32_t": 32, "uint32_t": 32, "int64_t": 64, "uint64_t": 64}[t]
+    return ("i", width, not t.startswith("u"))
+
+
+def _ctypes_kind(ct):
+    if ct is ctypes.c_char_p or ct is ctypes.c_void_p or (isinstance(ct, type) and issubclass(ct, ctypes._Pointer)):
+        return ("p",)
+    if ct in (ctypes.c_double, ctypes.c_float):
+        return ("f", 8 * ctypes.sizeof(ct))
+    signed = ct in (ctypes.c_int, ctypes.c_int32, ctypes.c_int64, ctypes.c_long, ctypes.c_longlong)
+    return ("i", 8 * ctypes.sizeof(ct), signed)
+
+
+def test_binding_signatures_match_the_header():
+    """The ctypes binding (zgraph.lib()) declares every entry point with the header's parameter
+    count, and each parameter and return value with the same kind: pointer, floating point of the
+    same width, or integer of the same width and signedness.  A mismatch would pass arguments in the
+    wrong registers or truncate them without any error."""
+    L = Z.lib()
+    protos = _prototypes()
+    assert set(protos) == set(declared_symbols())
+    bound = [n for n in protos if getattr(L, n).argtypes is not None]
+    assert len(bound) >= len(protos) - 2, sorted(set(protos) - set(bound))
+    bad = []
+    for name in bound:
+        ret, params = protos[name]
+        f = getattr(L, name)
+        if len(f.argtypes) != len(params):
+            bad.append((name, "arity", len(f.argtypes), len(params)))
+            continue
+        for i, (ct, p) in enumerate(zip(f.argtypes, params)):
+            if _ctypes_kind(ct) != _c_kind(p):
+                bad.append((name, i, p, ct))
+        want = _c_kind(ret)
+        got = _ctypes_kind(f.restype)
+        if want != got:
+            bad.append((name, "return", ret, f.restype))
+    assert not bad, bad
