@@ -25,3 +25,16 @@ def test_random_sector_bytes_from_the_committed_capture():
         assert src
     else:
         assert 32.0 <= bps <= 256.0 and "ncu capture" in src
+
+
+def test_headline_traffic_is_current():
+    """The committed ncu DRAM traffic of the headline's batch kernels (profiles/dram_traffic.txt)
+    was captured at the current kernel sources and record layout, so the bench reports it; an edit
+    of the sampling sources without a new capture fails here rather than silently dropping
+    `roofline.traffic` from the headline line."""
+    for workload in ("rmat26", "rmat21_batch"):
+        dps, src = bench.profile_traffic("k_batch", workload, "wide")
+        assert dps is not None, src
+        assert 100.0 < dps < 2000.0
+    bps, src = bench.random_sector_bytes()
+    assert bps is not None, src
