@@ -5,7 +5,7 @@
 #   * src/*.cpp (except Random.cpp) + a replaying Random + single-rank MPI / one-node NUMA
 #     shims  ->  one driver .so per application (oracle/ref/app_*.cpp include the app source);
 #   * the same with the reference's own Random.cpp  ->  libzgtime_*.so, which time its
-#     calculate() (oracle/ref/time_app.cpp);
+#     calculate() (oracle/ref/time_app.cpp; libzgtime_pattern.so: SamplerGenerator on a pattern);
 #   * naive_implementation/*.cpp  ->  executables (with a zero-filling operator new[]);
 #   * tests/Test{Pattern,Pattern2,Subgraph,Regression}.cpp  ->  executables.
 #
@@ -47,6 +47,8 @@ for pair in triangle:Triangle:TriangleCoutingInstance four_clique:FourClique:Fou
   $CXX $FLAGS $INC -DZGREF_APP_FILE="\"applications/$file.cpp\"" -DZGREF_APP_CLASS=$cls -shared \
        -o "$OUT/libzgtime_$app.so" "$HERE/ref/time_app.cpp" $TIME_OBJS "$OUT/obj_time/Random.o" -lm &
 done
+$CXX $FLAGS $INC -DZGREF_PATTERN -shared -o "$OUT/libzgtime_pattern.so" "$HERE/ref/time_app.cpp" $TIME_OBJS \
+     "$OUT/obj_time/Random.o" -lm &
 wait
 
 # naive exact counters (naive_implementation/Makefile builds them with plain g++)

@@ -2,11 +2,18 @@
  * Times the reference's own ZGraphInstance::calculate (its own mt19937 Random and OpenMP
  * threads, src/ZGraphInstance.cpp:257-297) for one application on a given edge list: a CPU
  * measurement of the unmodified estimator path, next to the oracle port.  Compiled by
- * oracle/build_ref.sh with ZGREF_APP_FILE / ZGREF_APP_CLASS set.  Test infrastructure.
+ * oracle/build_ref.sh with ZGREF_APP_FILE / ZGREF_APP_CLASS set, or with ZGREF_PATTERN for
+ * SamplerGenerator<Empty> on a pattern given at run time (as applications/FiveStar.cpp:18-26 and
+ * FiveHouse.cpp:18-27 build theirs).  Test infrastructure.
  */
+#ifdef ZGREF_PATTERN
+#include <vector>
+#include "SamplerGenerator.hpp"
+#else
 #define main zgref_app_main
 #include ZGREF_APP_FILE
 #undef main
+#endif
 
 #include <stdint.h>
 #include <chrono>
@@ -49,11 +56,7 @@ static void zgref_time_graph(Graph<Empty>& g, const uint32_t* edges, uint64_t m,
   g.local_edges = le;
 }
 
-/* Builds the graph, runs calculate(n / 16) once untimed, then times calculate(n) with `threads`
- * OpenMP threads; returns seconds, *estimate the result. */
-extern "C" __attribute__((visibility("default"))) double zgref_time_calculate(const uint32_t* edges, uint64_t m,
-                                                                               uint32_t nv, uint64_t n, int threads,
-                                                                               double* estimate) {
+static void zgref_boot(int threads) {
   static bool booted = false;
   zgref_num_cpus = threads > 0 ? threads : 1;
   if (!booted) {
@@ -65,9 +68,10 @@ extern "C" __attribute__((visibility("default"))) double zgref_time_calculate(co
     NetworkInterface::init_network_interface(&argc, &argv);
     SharedMemSys::init_shared_mem_sys();
   }
-  Graph<Empty> g;
-  zgref_time_graph(g, edges, m, nv);
-  ZGREF_APP_CLASS<Empty>* inst = new ZGREF_APP_CLASS<Empty>(&g);
+}
+
+/* calculate(n / 16) once untimed, then calculate(n) timed; returns seconds, *estimate the result. */
+static double zgref_time_instance(ZGraphInstance<Empty>* inst, uint64_t n, double* estimate) {
   Estimation warm;
   inst->calculate(n / 16 + 1, 3, warm);
   Estimation est;
@@ -77,3 +81,36 @@ extern "C" __attribute__((visibility("default"))) double zgref_time_calculate(co
   *estimate = r;
   return std::chrono::duration<double>(t1 - t0).count();
 }
+
+#ifdef ZGREF_PATTERN
+/* SamplerGenerator<Empty> for the pattern of pv vertices and pe edges (pedges: (src, dst) pairs,
+ * edge_id = index), timed with `threads` OpenMP threads. */
+extern "C" __attribute__((visibility("default"))) double zgref_time_pattern(const uint32_t* edges, uint64_t m,
+                                                                             uint32_t nv, uint32_t pv, uint32_t pe,
+                                                                             const uint32_t* pedges, uint64_t n,
+                                                                             int threads, double* estimate) {
+  zgref_boot(threads);
+  Graph<Empty> g;
+  zgref_time_graph(g, edges, m, nv);
+  std::vector<Edge<Empty>> es(pe);
+  for (uint32_t i = 0; i < pe; ++i) {
+    es[i].src = pedges[2 * i];
+    es[i].dst = pedges[2 * i + 1];
+    es[i].edge_id = i;
+  }
+  Pattern pattern(pv, pe, es.data());
+  SamplerGenerator<Empty>* inst = new SamplerGenerator<Empty>(&g, &pattern);
+  return zgref_time_instance(inst, n, estimate);
+}
+#else
+/* Builds the graph and times the application's instance with `threads` OpenMP threads. */
+extern "C" __attribute__((visibility("default"))) double zgref_time_calculate(const uint32_t* edges, uint64_t m,
+                                                                               uint32_t nv, uint64_t n, int threads,
+                                                                               double* estimate) {
+  zgref_boot(threads);
+  Graph<Empty> g;
+  zgref_time_graph(g, edges, m, nv);
+  ZGREF_APP_CLASS<Empty>* inst = new ZGREF_APP_CLASS<Empty>(&g);
+  return zgref_time_instance(inst, n, estimate);
+}
+#endif
