@@ -446,7 +446,8 @@ typedef struct zg_query_result {
  * estimator's weight:
  * m * prod over the conditional steps i = 1.. of min((i + 1) * max_degree, 2m) (x 3 for the
  * 4-chain).  Each further round runs what the observed variance needs, with headroom
- * 1 + 0.5 / sqrt(hits). */
+ * 1 + 0.5 / sqrt(hits).  A round whose exact weights overflowed 192 bits (zg_counters.overflow;
+ * only programs with more than six weight factors can) ends the query with ZG_ERR_OVERFLOW. */
 int zg_query(const zg_graph* g, const zg_program* p, double error, double confidence,
              uint64_t n_initial, uint64_t max_samples, uint64_t seed, uint32_t stream_id,
              void* cuda_stream, zg_query_result* out);

@@ -325,6 +325,10 @@ extern "C" int zg_query(const zg_graph* g, const zg_program* p, double eps, doub
     zg_counters c;
     rc = zg_run(g, p, next, n_total, seed, stream_id, cuda_stream, &c);
     if (rc) return rc;
+    // a weight past 192 bits makes the sums inexact: no bound can be claimed on them (programs
+    // with at most six weight factors, every factor below 2^32, never get here)
+    if (c.overflow)
+      return zg_set_error(ZG_ERR_OVERFLOW, "zg_query: an estimator's exact weight exceeded 192 bits"), ZG_ERR_OVERFLOW;
     den = c.den_log2;
     unsigned __int128 carry = 0;
     for (int i = 0; i < 5; ++i) {
