@@ -294,7 +294,39 @@ def run_reference(args):
             "impl": "reference", "config": workload_config(args.workload, len(edges)),
             "cpu_baseline": {"value": value, "unit": "samples/s", "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": "samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if not args.no_time_to_bound:
+        try:
+            line["time_to_bound"] = cpu_time_to_bound(O, edges, 1 << wl["scale"], og, threads)
+        except Exception as exc:  # the samples/s line above stands on its own
+            line["time_to_bound"] = {"error": "%s: %s" % (type(exc).__name__, exc)}
     print(json.dumps(line), flush=True)
+
+
+def cpu_time_to_bound(O, edges, nv, og, threads, seed=31, eps=0.01, conf=0.95, min_run_s=2.0):
+    """The reference's own way to a 1 %/95 % triangle answer on the host: ErrorProfile::run, i.e.
+    get_num_estimators (timed: the host restatement with zg_elp_plain's draw plan, so n_required is
+    the count the GPU arm's plain sizing gets for the same seed) followed by calculate(n_required)
+    (its time from the measured samples/s of the triangle program on the whole graph; the billions
+    of samples are not run)."""
+    prog = O.OracleProgram(PROG_IDS["triangle"])
+    t0 = time.perf_counter()
+    n_req = O.plain_elp(edges, nv, prog, 1, seed, eps, conf, og.m, og.max_degree, threads)
+    profile_s = time.perf_counter() - t0
+    n = 1 << 14
+    while True:
+        t0 = time.perf_counter()
+        O.run(og, prog, n, seed + 100, 0x51, 0, threads)
+        dt = time.perf_counter() - t0
+        if dt >= min_run_s or n >= 1 << 36:
+            break
+        n *= 2
+    rate = n / dt
+    return {"pattern": "triangle", "eps": eps, "confidence": conf, "elp_seed": seed, "n_required": n_req,
+            "profile_s": profile_s, "samples_per_s": rate, "calculate_s": n_req / rate,
+            "seconds": profile_s + n_req / rate, "cores": threads,
+            "method": "ErrorProfile::get_num_estimators on the host (oracle.plain_elp: 10 %% subsample, 2^14 x 16 + "
+                      "2^23 estimators, regression), timed; then calculate(n_required) at the triangle's measured "
+                      "samples/s (%d samples in %.2f s), not run" % (n, dt)}
 
 
 # ---- GPU side ---------------------------------------------------------------------------------

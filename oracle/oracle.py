@@ -69,6 +69,8 @@ def lib():
             "zgo_pred": ([I32, I64, I64, U32], I32),
             "zgo_subsample_keep": ([D, U64, U64], I32),
             "zgo_shuffle_perm": ([U64, U64, P], None),
+            "zgo_shuffle_key": ([U64, U64], U64),
+            "zgo_subsample_edges": ([P, U64, D, U64, U64, U64, P, C.POINTER(C.c_uint64)], I32),
             "zgo_exact_naive": ([C.POINTER(_Graph), I32, P], I32),
             "zgo_exact_fast": ([C.POINTER(_Graph), I32, P], I32),
             "zgo_exact_weighted_triangle": ([C.POINTER(_Graph), U32, I32, P], I32),
@@ -235,6 +237,76 @@ def shuffle_perm(m, seed):
     p = np.zeros(max(1, m), dtype=np.uint64)
     lib().zgo_shuffle_perm(m, seed, _p(p))
     return p[:m]
+
+
+def subsample_edges(edges, rate, keep_seed, shuffle_seed):
+    """GraphSampler::sample_graph's kept edges in the device's draw plan (zgo_subsample_edges): the
+    edge list zg_graph_subsample(rate, keep_seed, shuffle_seed) builds its graph from."""
+    e = np.ascontiguousarray(edges, dtype=np.uint32).reshape(-1, 2)
+    out = np.empty((max(1, e.shape[0]), 2), np.uint32)  # pages past the kept edges are never touched
+    k = C.c_uint64(0)
+    rc = lib().zgo_subsample_edges(_p(e), e.shape[0], rate, keep_seed, shuffle_seed, e.shape[0], _p(out), C.byref(k))
+    if rc != 0:
+        raise ValueError("zgo_subsample_edges failed (%d)" % rc)
+    return out[:k.value]
+
+
+# zg_elp_plain's draw plan (ZG_ELP_* in include/zgraph_gpu.h), so that the CPU arm needs no GPU library
+ELP_KEEP_OFFSET, ELP_SHUFFLE_OFFSET, ELP_FILTER_OFFSET, ELP_STREAM = 1, 2, 3, 0x454C5000
+
+
+def elp_solve(groups, group_size, big_estimate, big_n, nse, ncse, sampled_m, sampled_max_degree, orig_m,
+              orig_max_degree, eps, conf):
+    """The host half of ErrorProfile::get_num_estimators (src/ErrorLatencyProfile.cpp:115-206) with
+    its long double intermediates: the running estimate after each group (Estimation::update,
+    src/ZGraphInstance.cpp:24-27), the moving average of the scaled error, the regression
+    through the origin (UnbiasedLinearRegression::solve, src/Regression.cpp:17-28) and the bound
+    on the original graph.  Returns the estimator count as a float (the reference truncates it)."""
+    LD = np.longdouble
+    n, cur = 0, 0.0
+    running = []
+    for v in groups:
+        cur = (1.0 * n / (n + group_size)) * cur + (1.0 * group_size / (n + group_size)) * float(v)
+        n += group_size
+        running.append(cur)
+    est = (1.0 * n / (n + big_n)) * cur + (1.0 * big_n / (n + big_n)) * float(big_estimate)
+    ema, alpha = LD(100), 0.04
+    t0, t1 = LD(0), LD(0)
+    xs, ys = [], []
+    for i, r in enumerate(running):
+        err = (LD(r) - LD(est)) / LD(est) * LD(5)
+        if err < 0:
+            err = -err
+        ema = ema * LD(1 - alpha) + err * LD(alpha)
+        x_tmp = float(LD(calculate_bound(float(ema), 1 - conf, nse, ncse, est, sampled_max_degree, sampled_m)) *
+                      (ema * ema))
+        xs.append(LD(np.sqrt(x_tmp / ((i + 1) * group_size))))
+        ys.append(ema)
+    for x, y in zip(xs, ys):
+        t0 += x * y
+    for x in xs:
+        t1 += x * x
+    k = float(t0 / t1)
+    rough = float(LD(est) / LD(0.1) ** LD(nse + ncse))
+    return calculate_bound(eps, 1 - conf, nse, ncse, rough, orig_max_degree, orig_m) * (k * k)
+
+
+def plain_elp(edges, num_vertices, program, ncse, seed, eps, conf, orig_m, orig_max_degree, threads=0):
+    """ErrorProfile::get_num_estimators (src/ErrorLatencyProfile.cpp:72-207) on the host with
+    zg_elp_plain's draw plan: the 10 % edge subsample, 2^14 groups of 16 estimators (each group's
+    mean summed in sample order, as a one-threaded calculate(16) does) and 2^23 more estimators on
+    it, then the regression and the bound.  Returns the estimator count (truncated)."""
+    sub = subsample_edges(edges, 0.1, seed + ELP_KEEP_OFFSET, seed + ELP_SHUFFLE_OFFSET)
+    og = OracleGraph(sub, num_vertices)
+    tr, _ = traces(og, program, 1 << 18, seed, stream=ELP_STREAM, threads=threads)
+    w = tr["w"].reshape(-1, 16)
+    acc = np.zeros(w.shape[0])
+    for j in range(16):  # sample order within each group
+        acc = acc + w[:, j]
+    big = run(og, program, 1 << 23, seed, ELP_STREAM, 1 << 18, threads)
+    n = elp_solve(acc / 16.0, 16, float(big.exact_sum() / big.samples), 1 << 23, 1.0, float(ncse), og.m,
+                  og.max_degree, orig_m, orig_max_degree, eps, conf)
+    return int(n)
 
 
 def pred(op, t0, t1, w):

@@ -970,11 +970,15 @@ static int kv_cmp(const void* a, const void* b) {
   if (x->key != y->key) return x->key < y->key ? -1 : 1;
   return x->idx < y->idx ? -1 : (x->idx > y->idx);
 }
+uint64_t zgo_shuffle_key(uint64_t shuffle_seed, uint64_t i) {
+  return zgo_draw(shuffle_seed, ZGO_STREAM_SHUFFLE, i, 0, 0, ~0ull);
+}
+
 /* The GPU permutes by sorting (Philox key, position); output edge i comes from perm[i]. */
 void zgo_shuffle_perm(uint64_t m, uint64_t shuffle_seed, uint64_t* perm) {
   zgo_kv* kv = (zgo_kv*)malloc(sizeof(zgo_kv) * (m ? m : 1));
   for (uint64_t i = 0; i < m; ++i) {
-    kv[i].key = zgo_draw(shuffle_seed, ZGO_STREAM_SHUFFLE, i, 0, 0, ~0ull);
+    kv[i].key = zgo_shuffle_key(shuffle_seed, i);
     kv[i].idx = i;
   }
   qsort(kv, m, sizeof(zgo_kv), kv_cmp);

@@ -89,6 +89,16 @@ int zgo_pred(int op, int64_t t0, int64_t t1, uint32_t w);
 int zgo_subsample_keep(double rate, uint64_t keep_seed, uint64_t e);
 /* The permutation applied by a shuffle seed: perm[i] = input position of output edge i. */
 void zgo_shuffle_perm(uint64_t m, uint64_t shuffle_seed, uint64_t* perm);
+/* The sort key of input position i under a shuffle seed: output edges are the inputs in ascending
+ * (key, i) order. */
+uint64_t zgo_shuffle_key(uint64_t shuffle_seed, uint64_t i);
+/* The subsample GraphSampler::sample_graph keeps (src/Graph.cpp:629-780), with the device's draw
+ * plan (zg_graph_subsample): edge e of the m (src, dst) pairs is kept when
+ * zgo_subsample_keep(rate, keep_seed, e), and the kept edges are permuted as
+ * zgo_shuffle_perm(k, shuffle_seed) orders them.  out: room for `capacity` pairs; *k_out: pairs
+ * kept.  Parallel (OpenMP) and m < 2^32: the ELP subsample of the largest benchmark graph. */
+int zgo_subsample_edges(const uint32_t* edges, uint64_t m, double rate, uint64_t keep_seed, uint64_t shuffle_seed,
+                        uint64_t capacity, uint32_t* out, uint64_t* k_out);
 
 /* conditional_close with the found edge ids written back (src/ZGraphInstance.cpp:410-441).
  * Returns 1 when every edge was found; *found = edges found before the first miss. */

@@ -186,3 +186,75 @@ int zgo_gen_rmat(uint32_t scale, uint32_t edge_factor, double a, double b, doubl
   free(idx);
   return ZG_OK;
 }
+
+int zgo_subsample_edges(const uint32_t* edges, uint64_t m, double rate, uint64_t keep_seed, uint64_t shuffle_seed,
+                        uint64_t capacity, uint32_t* out, uint64_t* k_out) {
+  if (!k_out || (m && !edges) || m >= ((uint64_t)1 << 32)) return ZG_ERR_INVALID_ARG;
+  int nt = nthreads(m);
+  uint8_t* keep = (uint8_t*)malloc(m ? m : 1);
+  uint64_t* cnt = (uint64_t*)calloc((size_t)nt + 1, sizeof(uint64_t));
+  if (!keep || !cnt) {
+    free(keep); free(cnt);
+    return ZG_ERR_OOM;
+  }
+  /* the keep draws, counted per contiguous range of edges */
+#ifdef _OPENMP
+#pragma omp parallel num_threads(nt)
+#endif
+  {
+    int t = thread_id();
+    uint64_t lo = m / (uint64_t)nt * (uint64_t)t, hi = t == nt - 1 ? m : lo + m / (uint64_t)nt, c = 0;
+    for (uint64_t e = lo; e < hi; ++e) c += keep[e] = (uint8_t)zgo_subsample_keep(rate, keep_seed, e);
+    cnt[t + 1] = c;
+  }
+  for (int t = 0; t < nt; ++t) cnt[t + 1] += cnt[t];
+  const uint64_t k = cnt[nt];
+  *k_out = k;
+  if (!out) {
+    free(keep); free(cnt);
+    return ZG_OK;
+  }
+  if (capacity < k) {
+    free(keep); free(cnt);
+    return ZG_ERR_INVALID_ARG;
+  }
+  uint32_t* pos = (uint32_t*)malloc(sizeof(uint32_t) * (k ? k : 1));
+  uint64_t* keys = (uint64_t*)malloc(sizeof(uint64_t) * (k ? k : 1));
+  uint32_t* order = (uint32_t*)malloc(sizeof(uint32_t) * (k ? k : 1));
+  if (!pos || !keys || !order) {
+    free(keep); free(cnt); free(pos); free(keys); free(order);
+    return ZG_ERR_OOM;
+  }
+  /* the kept positions in ascending order, and the shuffle key of each kept rank */
+#ifdef _OPENMP
+#pragma omp parallel num_threads(nt)
+#endif
+  {
+    int t = thread_id();
+    uint64_t lo = m / (uint64_t)nt * (uint64_t)t, hi = t == nt - 1 ? m : lo + m / (uint64_t)nt, j = cnt[t];
+    for (uint64_t e = lo; e < hi; ++e)
+      if (keep[e]) pos[j++] = (uint32_t)e;
+  }
+  int nk = nthreads(k);
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(nk) schedule(static)
+#endif
+  for (int64_t j = 0; j < (int64_t)k; ++j) {
+    keys[j] = zgo_shuffle_key(shuffle_seed, (uint64_t)j);
+    order[j] = (uint32_t)j;
+  }
+  /* stable on the keys: ties keep ascending rank, the (key, rank) order of zgo_shuffle_perm */
+  int rc = radix_sort(keys, order, k, 64);
+  if (rc == ZG_OK) {
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(nk) schedule(static)
+#endif
+    for (int64_t i = 0; i < (int64_t)k; ++i) {
+      const uint64_t e = pos[order[i]];
+      out[2 * i] = edges[2 * e];
+      out[2 * i + 1] = edges[2 * e + 1];
+    }
+  }
+  free(keep); free(cnt); free(pos); free(keys); free(order);
+  return rc;
+}

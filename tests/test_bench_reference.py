@@ -1,6 +1,6 @@
 """bench.py's reference arm (CPU): it prints the bench's one JSON line with the GPU arm's config
-for the same workload, and it runs the oracle alone: neither the GPU library nor its Python binding
-is loaded in its process."""
+for the same workload and the reference's plain-ELP time to a 1 %/95 % triangle answer, and it runs
+the oracle alone: neither the GPU library nor its Python binding is loaded in its process."""
 import json
 import os
 import subprocess
@@ -33,3 +33,9 @@ def test_reference_arm_line_and_isolation():
     import bench
     assert line["config"] == bench.workload_config("rmat13", 79403)  # what the GPU arm prints
     assert lines[1] == "LOADED False False True"
+    # the reference's own way to a 1 %/95 % triangle answer: ErrorProfile::get_num_estimators timed on
+    # the host, then calculate(n_required) at the measured rate
+    ttb = line["time_to_bound"]
+    assert "error" not in ttb, ttb
+    assert ttb["pattern"] == "triangle" and ttb["n_required"] > 0 and ttb["samples_per_s"] > 0
+    assert abs(ttb["seconds"] - ttb["profile_s"] - ttb["n_required"] / ttb["samples_per_s"]) < 1e-6 * ttb["seconds"]

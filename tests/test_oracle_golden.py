@@ -228,3 +228,35 @@ def test_oracle_unbiased_four_clique_matches_exact_counts():
         assert abs(mean - ex) < 4 * se, (sc, ef, mean, ex, se)
         r = O.run(og, O.OracleProgram(2), 1 << 21, 11, stream=2)
         assert float(r.exact_sum()) / r.samples < 0.75 * ex
+
+
+def test_subsample_edges_matches_the_per_edge_plan(golden):
+    """zgo_subsample_edges (parallel keep draws and radix-sorted shuffle keys) returns the edge list
+    that the per-edge keep draws and zgo_shuffle_perm give, in the same order."""
+    import zgraph as Z
+    meta, arr = golden
+    for name in sorted(meta["graphs"])[:3]:
+        e, nv = golden_graph(meta, arr, name)
+        for seed in (1, 77):
+            keep = np.array([O.subsample_keep(0.1, seed + 1, i) for i in range(len(e))], dtype=bool)
+            kept = np.nonzero(keep)[0]
+            want = e[kept[O.shuffle_perm(len(kept), seed + 2).astype(np.int64)]]
+            got = O.subsample_edges(e, 0.1, seed + 1, seed + 2)
+            assert np.array_equal(got, want), (name, seed)
+    assert (O.ELP_KEEP_OFFSET, O.ELP_SHUFFLE_OFFSET, O.ELP_FILTER_OFFSET, O.ELP_STREAM) == \
+        (Z.ELP_KEEP_OFFSET, Z.ELP_SHUFFLE_OFFSET, Z.ELP_FILTER_OFFSET, Z.ELP_STREAM)
+
+
+def test_host_plain_elp_matches_reference(golden):
+    """The host restatement of ErrorProfile::get_num_estimators (oracle.plain_elp, which the CPU
+    arm of the benchmark times without the GPU library) gives the reference's own estimator count
+    on every golden case."""
+    meta, arr = golden
+    ncse_of = {1: 1, 3: 1, 4: 2}
+    for case in meta["elp"]["get_num_estimators"]:
+        e, nv = golden_graph(meta, arr, case["graph"])
+        ncse = ncse_of.get(case["kind"], case["param"] - 2)
+        deg = np.bincount(e.ravel(), minlength=nv)
+        n = O.plain_elp(e, nv, O.OracleProgram(case["kind"], case["param"]), ncse, case["seed"], case["eps"],
+                        case["conf"], len(e), int(deg.max()))
+        assert abs(n - case["n_required"]) <= 1e-9 * case["n_required"] + 1, (case, n)
