@@ -226,6 +226,7 @@ typedef struct {
   int overflow;
   uint32_t sectors; /* 32-byte sector access model (see zgo_model_*) */
   uint32_t closures; /* closure checks of the access model */
+  int model;         /* count the access model: only traces report it (an untraced run skips it) */
 } zgo_ctx;
 
 /* Access model of the rebuilt kernels, in 32-byte sectors (the roofline's algorithmic bytes):
@@ -284,7 +285,7 @@ static double prim_cond_sample(zgo_ctx* c, const zgo_edge* edges, int ne, const 
     uint32_t v = verts[i];
     uint64_t b = g->off[v], e = g->off[v + 1];
     if (e == b) continue; /* bitmap bit clear */
-    c->sectors += 1 + zgo_model_search(e - b);
+    if (c->model) c->sectors += 1 + zgo_model_search(e - b);
     if (min_valid <= g->adj_eid[b]) { sum += e - b; pos[np++] = b; }
     else if (min_valid > g->adj_eid[e - 1]) { pos[np++] = e; }
     else if (e - b <= ZGO_BS_THRESHOLD) {
@@ -330,7 +331,7 @@ static int prim_close(zgo_ctx* c, const zgo_sub* sampled, const zgo_sub* wait) {
   for (int i = 0; i < wait->ne; ++i) {
     uint32_t ws = wait->e[i].src, wd = wait->e[i].dst;
     int found = 0;
-    {
+    if (c->model) {
       uint64_t dx = g->off[ws + 1] - g->off[ws], dy = g->off[wd + 1] - g->off[wd];
       c->sectors += 2 + zgo_model_search(dx < dy ? dx : dy);
       c->closures++;
@@ -413,8 +414,10 @@ static double prog_four_clique(zgo_ctx* c) {
 static int64_t find_edge_id(zgo_ctx* c, uint32_t x, uint32_t y) {
   const zgo_graph* g = c->g;
   uint64_t dx = g->off[x + 1] - g->off[x], dy = g->off[y + 1] - g->off[y];
-  c->sectors += 2 + zgo_model_search(dx < dy ? dx : dy);
-  c->closures++;
+  if (c->model) {
+    c->sectors += 2 + zgo_model_search(dx < dy ? dx : dy);
+    c->closures++;
+  }
   uint32_t v = dx <= dy ? x : y, t = dx <= dy ? y : x;
   for (uint64_t idx = g->off[v]; idx < g->off[v + 1]; ++idx)
     if (g->adj_nbr[idx] == t) return (int64_t)g->adj_eid[idx];
@@ -747,11 +750,18 @@ static uint32_t prog_den_log2(const zgo_program* p) {
   return 0;
 }
 
-static void ctx_init(zgo_ctx* c, const zgo_graph* g, uint64_t seed, uint32_t stream,
-                     uint64_t sample, zg_sample_trace* tr) {
+/* model = 0: a run that keeps no trace; its scratch record is not cleared (ctx_finish sets every
+ * field the counters read) and the access model is not counted. */
+static void ctx_init_model(zgo_ctx* c, const zgo_graph* g, uint64_t seed, uint32_t stream,
+                           uint64_t sample, zg_sample_trace* tr, int model) {
   c->g = g; c->seed = seed; c->stream = stream; c->sample = sample; c->nd = 0; c->tr = tr;
   c->shift = 0; c->num_lo = 1; c->num_hi = 0; c->overflow = 0; c->sectors = 0; c->closures = 0;
-  memset(tr, 0, sizeof(*tr));
+  c->model = model;
+  if (model) memset(tr, 0, sizeof(*tr));
+}
+static void ctx_init(zgo_ctx* c, const zgo_graph* g, uint64_t seed, uint32_t stream,
+                     uint64_t sample, zg_sample_trace* tr) {
+  ctx_init_model(c, g, seed, stream, sample, tr, 1);
 }
 
 static void ctx_finish(zgo_ctx* c, double r) {
@@ -759,6 +769,7 @@ static void ctx_finish(zgo_ctx* c, double r) {
   tr->ndraws = c->nd;
   tr->sectors = c->sectors;
   tr->closures = c->closures;
+  tr->fail = 0;
   if (r < 0) { tr->fail = 1; r = 0; }
   tr->w = r;
   tr->hit = r != 0;
@@ -771,10 +782,10 @@ static void ctx_finish(zgo_ctx* c, double r) {
   }
 }
 
-int zgo_sample(const zgo_graph* g, const zgo_program* p, uint64_t seed, uint32_t stream,
-               uint64_t sample, zg_sample_trace* tr) {
+static int sample_one(const zgo_graph* g, const zgo_program* p, uint64_t seed, uint32_t stream,
+                      uint64_t sample, zg_sample_trace* tr, int model) {
   zgo_ctx c;
-  ctx_init(&c, g, seed, stream, sample, tr);
+  ctx_init_model(&c, g, seed, stream, sample, tr, model);
   double r = 0;
   switch (p->kind) {
     case ZG_PROG_TRIANGLE: r = prog_triangle(&c); break;
@@ -788,6 +799,11 @@ int zgo_sample(const zgo_graph* g, const zgo_program* p, uint64_t seed, uint32_t
   }
   ctx_finish(&c, r);
   return ZG_OK;
+}
+
+int zgo_sample(const zgo_graph* g, const zgo_program* p, uint64_t seed, uint32_t stream,
+               uint64_t sample, zg_sample_trace* tr) {
+  return sample_one(g, p, seed, stream, sample, tr, 1);
 }
 
 /* ---- exact accumulation ------------------------------------------------- */
@@ -866,11 +882,16 @@ int zgo_run(const zgo_graph* g, const zgo_program* p, uint64_t n, uint64_t first
     uint64_t lo = n / (uint64_t)nt * (uint64_t)t;
     uint64_t hi = (t == nt - 1) ? n : lo + n / (uint64_t)nt;
     zg_sample_trace tr;
+    /* each thread folds into its own counters and stores them once: per-sample writes to part[t]
+       would share cache lines between neighbouring threads */
+    zg_counters acc;
+    memset(&acc, 0, sizeof(acc));
     for (uint64_t i = lo; i < hi; ++i) {
       zg_sample_trace* tp = traces ? &traces[i] : &tr;
-      if (zgo_sample(g, p, seed, stream, first + i, tp) != ZG_OK) { err = 1; break; }
-      counters_fold(&part[t], tp, den);
+      if (sample_one(g, p, seed, stream, first + i, tp, traces != NULL) != ZG_OK) { err = 1; break; }
+      counters_fold(&acc, tp, den);
     }
+    part[t] = acc;
   }
   for (int t = 0; t < nt; ++t) counters_merge(out, &part[t]);
   free(part);
