@@ -1,11 +1,12 @@
-"""bench.py's coverage report (CPU): the Wilson score interval it prints beside each covered
-fraction, against values worked out by hand."""
+"""bench.py's host-side pieces (CPU): the Wilson score interval it prints beside each covered
+fraction, against values worked out by hand; the committed ncu captures it reads; its CPU leg."""
 import os
 import sys
 
 import pytest
 
-sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
 import bench  # noqa: E402
 
 
@@ -38,3 +39,16 @@ def test_headline_traffic_is_current():
         assert 100.0 < dps < 2000.0
     bps, src = bench.random_sector_bytes()
     assert bps is not None, src
+
+
+def test_cpu_baseline_leg_on_a_small_graph():
+    """The GPU arm's CPU leg (bench.cpu_baseline: the oracle on the graph's edge list, a bounded sample
+    of every program of the workload, the headline's patterns included) returns the fields the bench
+    line carries."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    edges = O.gen_rmat(10, 8, seed=3)
+    out = bench.cpu_baseline(edges, 1 << 10, ["four_clique", "five_star", "five_house", "triangle"], 2,
+                             target_s=0.4)
+    assert out["value"] > 0 and out["unit"] == "samples/s" and out["cores"] == 2 and out["kind"] == "port"
+    assert "five_house" in out["sample"]
