@@ -260,3 +260,28 @@ def test_host_plain_elp_matches_reference(golden):
         n = O.plain_elp(e, nv, O.OracleProgram(case["kind"], case["param"]), ncse, case["seed"], case["eps"],
                         case["conf"], len(e), int(deg.max()))
         assert abs(n - case["n_required"]) <= 1e-9 * case["n_required"] + 1, (case, n)
+
+
+def test_device_elp_solve_matches_host_restatement_on_random_profiles():
+    """zg_elp_solve (the host half of zg_elp_plain, in the product library) and the oracle's own
+    restatement of ErrorProfile::get_num_estimators's host half agree on random group-estimate
+    sequences: heavy-tailed and light-tailed group means, zero groups, several program shapes
+    (sample_edge / conditional_sample_edge call counts) and error / confidence targets."""
+    import zgraph as Z
+    rng = np.random.default_rng(2024)
+    for trial in range(24):
+        n_groups = int(rng.choice([64, 1024, 1 << 14]))
+        mean = float(10 ** rng.uniform(2, 9))
+        if trial % 3 == 0:
+            groups = rng.pareto(1.5, n_groups) * mean
+        else:
+            groups = rng.gamma(2.0, mean / 2.0, n_groups)
+        groups[rng.random(n_groups) < 0.2] = 0.0
+        big = float(groups.mean() * rng.uniform(0.8, 1.2))
+        ncse = float(rng.integers(1, 5))
+        sm, sd = int(rng.integers(10 ** 4, 10 ** 7)), int(rng.integers(10, 10 ** 4))
+        om, od = sm * 10, sd * int(rng.integers(2, 12))
+        eps, conf = float(rng.choice([0.01, 0.05, 0.1])), float(rng.choice([0.9, 0.95, 0.99]))
+        want = O.elp_solve(groups, 16, big, 1 << 23, 1.0, ncse, sm, sd, om, od, eps, conf)
+        got = Z.elp_solve(groups, 16, big, 1 << 23, 1.0, ncse, sm, sd, om, od, eps, conf)
+        assert abs(got.n_required_f - want) <= 1e-9 * abs(want), (trial, got.n_required_f, want)
