@@ -285,3 +285,23 @@ def test_device_elp_solve_matches_host_restatement_on_random_profiles():
         want = O.elp_solve(groups, 16, big, 1 << 23, 1.0, ncse, sm, sd, om, od, eps, conf)
         got = Z.elp_solve(groups, 16, big, 1 << 23, 1.0, ncse, sm, sd, om, od, eps, conf)
         assert abs(got.n_required_f - want) <= 1e-9 * abs(want), (trial, got.n_required_f, want)
+
+
+def test_untraced_and_traced_runs_give_the_same_counters():
+    """An oracle run that keeps no per-sample trace (per-thread counters, no access model) returns
+    the counters of the traced run of the same samples, for every program kind, with 1 and 4
+    threads: the checker the GPU parity tests compare against is the same either way."""
+    import zgraph as Z
+    e = Z.gen_rmat(11, 12, seed=4)
+    og = O.OracleGraph(e, 1 << 11)
+    progs = [O.OracleProgram(k) for k in (1, 2, 3, 4, 7)] + [O.OracleProgram(5, 6)]
+    progs += [O.OracleProgram(6, pattern=(5, [(0, 1), (0, 2), (0, 3), (0, 4)])),
+              O.OracleProgram(6, pattern=(5, [(0, 1), (0, 2), (1, 2), (1, 3), (2, 4), (3, 4)]))]
+    for p in progs:
+        _, want = O.traces(og, p, 1 << 15, 99, stream=3, first=1 << 33)
+        for threads in (1, 4):
+            got = O.run(og, p, 1 << 15, 99, 3, 1 << 33, threads)
+            for f in ("samples", "hits", "fails", "den_log2", "overflow"):
+                assert getattr(got, f) == getattr(want, f), (p.p.kind, threads, f)
+            assert list(got.sum_num) == list(want.sum_num) and got.estimate == want.estimate, (p.p.kind, threads)
+            assert got.sum_w2 == pytest.approx(want.sum_w2, rel=1e-12), (p.p.kind, threads)
