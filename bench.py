@@ -279,10 +279,13 @@ def run_reference(args):
     for i in range(args.warmup):
         for j, (_, p, kind) in enumerate(progs):
             O.run(og, p, n, i * n, 5 + j, kind, threads)
+    per_prog = [0.0] * len(progs)
     t0 = time.perf_counter()
     for i in range(args.steps):
         for j, (_, p, kind) in enumerate(progs):
+            t1 = time.perf_counter()
             O.run(og, p, n, (args.warmup + i) * n, 5 + j, kind, threads)
+            per_prog[j] += time.perf_counter() - t1
     dt = time.perf_counter() - t0
     value = len(progs) * n * args.steps / dt
     sample = ("%d samples of each of %d programs per step (bounded sample of the 2^%d per program), "
@@ -294,6 +297,14 @@ def run_reference(args):
             "impl": "reference", "config": workload_config(args.workload, len(edges)),
             "cpu_baseline": {"value": value, "unit": "samples/s", "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": "samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    # each program's share of the timed steps, and its closure checks (conditional_close look-ups up
+    # to the first missing edge, the access model's count, from the traces of 2^14 samples)
+    line["per_program"] = []
+    for j, (name, p, kind) in enumerate(progs):
+        closures = float(O.traces(og, p, 1 << 14, 5 + j, stream=kind, threads=threads)[0]["closures"].mean())
+        rate = n * args.steps / per_prog[j]
+        line["per_program"].append({"program": name, "samples_per_s": rate, "closure_checks_per_sample": closures,
+                                    "closure_checks_per_s": closures * rate})
     if not args.no_time_to_bound:
         try:
             line["time_to_bound"] = cpu_time_to_bound(O, edges, 1 << wl["scale"], og, threads)

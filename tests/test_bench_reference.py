@@ -33,6 +33,10 @@ def test_reference_arm_line_and_isolation():
     import bench
     assert line["config"] == bench.workload_config("rmat13", 79403)  # what the GPU arm prints
     assert lines[1] == "LOADED False False True"
+    # each program's samples/s and closure checks per second (the triangle closes one edge per sample)
+    (prog,) = line["per_program"]
+    assert prog["program"] == "triangle" and prog["samples_per_s"] > 0
+    assert 0.5 < prog["closure_checks_per_sample"] <= 1.0
     # the reference's own way to a 1 %/95 % triangle answer: ErrorProfile::get_num_estimators timed on
     # the host, then calculate(n_required) at the measured rate
     ttb = line["time_to_bound"]
