@@ -43,8 +43,8 @@ def test_headline_traffic_is_current():
 
 def test_cpu_baseline_leg_on_a_small_graph():
     """The GPU arm's CPU leg (bench.cpu_baseline: the oracle on the graph's edge list, a bounded sample
-    of every program of the workload, the headline's patterns included) returns the fields the bench
-    line carries."""
+    of every program of the workload, the headline's patterns included, and the reference's plain-ELP
+    time to a 1 %/95 % triangle answer) returns the fields the bench line carries."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     edges = O.gen_rmat(10, 8, seed=3)
@@ -52,3 +52,6 @@ def test_cpu_baseline_leg_on_a_small_graph():
                              target_s=0.4)
     assert out["value"] > 0 and out["unit"] == "samples/s" and out["cores"] == 2 and out["kind"] == "port"
     assert "five_house" in out["sample"]
+    ttb = out["time_to_bound"]  # the reference's host time to a 1 %/95 % triangle answer
+    assert "error" not in ttb, ttb
+    assert ttb["n_required"] > 0 and ttb["seconds"] > ttb["profile_s"] > 0
